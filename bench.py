@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark of the two-site DMRG hot path: one H_eff*psi at the middle site.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--form fp64]
+
+A step is one H_eff*psi (sigma = H_eff psi, sigma zeroed first, as the
+reference's Davidson does) of the named workload.  `value` is the whole-job
+H_eff*psi rate in TFLOP/s (FLOP = 2 x the reference's multiply-add count of
+the recorded GEMM pairs) with psi/sigma/operators resident in HBM; `e2e` is
+the same rate through the host-buffer C-ABI entry (b2g_heff_apply_host: psi
+H2D, product, sigma D2H, inside the timed region).  `--impl reference` times
+the CPU restatement of the reference's Tasked replay (BLAS dgemm per pair,
+OpenMP over pairs, per-thread sigma copies) on this host's cores.
+Multi-GPU: the product does not shard within one H_eff here (replicas only):
+each rank runs its own copy and `value` sums the ranks' work over the slowest
+rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "block2-preview_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = ("sweep time & H_eff·ψ TFLOP/s: mixed/batched vs FP64 on 1 GB300 at "
+          "|ΔE|≤1e-8 Ha")
+L2_BYTES = 129 * 1024 * 1024
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """Samples nvidia-smi clocks / throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in out.strip().splitlines():
+            t = [x.strip() for x in ln.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                mx.append(float(t[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- workload
+def load_workload(name: str):
+    from b2g import workloads
+    return workloads.get(name)
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def cpu_replay_timing(prob, max_steps: int, budget_s: float, warmup: int = 1):
+    """Times the oracle's Tasked replay (reference algorithm, BLAS per pair) with all host threads."""
+    from oracle import oracle
+    blas = oracle.load_blas()
+    nthreads = os.cpu_count() or 1
+    seq = prob.seq()
+    psi = prob.psi
+    for _ in range(max(0, warmup)):
+        oracle.replay(seq, prob.ops, psi, prob.sigma_size, nthreads=nthreads)
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max(1, max_steps):
+        t0 = time.perf_counter()
+        oracle.replay(seq, prob.ops, psi, prob.sigma_size, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget_s:
+            break
+    return times, nthreads, blas
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, rank, local_rank, world, dist):
+    import torch
+
+    import b2g
+    from b2g import capi
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    prob = load_workload(args.workload)
+    form = {"fp64": b2g.FP64}[args.form]
+    ctx = b2g.Context(local_rank)
+    heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
+    st = heff.stats
+    flop = 2.0 * st["mnk"]
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
+    psi = torch.from_numpy(prob.psi).to(dev)
+    sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+    ws_bytes = st["ops_bytes"] + st["work_bytes"] + 16 * prob.psi_size
+    flush = None
+    if ws_bytes < 4 * L2_BYTES:
+        flush = torch.empty(4 * L2_BYTES, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step():
+        with torch.cuda.stream(stream):
+            sig.zero_()
+        heff.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, form)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    # ---- timed device leg: per-step CUDA events on the launching stream
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    clocks = ClockSampler(local_rank)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        evs[k][0].record(stream)
+        step()
+        evs[k][1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    ck = clocks.stop()
+    if dist is not None:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_s = sum(step_ms) / 1e3
+    # ---- per-kernel timing (dominant kernel) with events inside the library
+    capi.check(capi.lib().b2g_heff_set_timing(heff._h, 1))
+    ph = []
+    import ctypes as C
+    for _ in range(3):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        step()
+        ms = (C.c_float * 2)()
+        capi.check(capi.lib().b2g_heff_last_timing(heff._h, ms))
+        ph.append((ms[0], ms[1]))
+    capi.check(capi.lib().b2g_heff_set_timing(heff._h, 0))
+    p1 = statistics.median(x[0] for x in ph)
+    p2 = statistics.median(x[1] for x in ph)
+    pk = C.c_double()
+    capi.check(capi.lib().b2g_probe_peak(ctx.handle, b2g.FP64, C.byref(pk)))
+    a = prob.pairs
+    flop0 = 2.0 * float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]))
+    flop1 = 2.0 * float(np.sum(a["m1"].astype(np.float64) * a["n1"] * a["k1"]))
+    if p2 >= p1:
+        kname, kflop, kms = "fp64_phase2 (GEMM1: sigma += alpha op(L) W)", flop1, p2
+    else:
+        kname, kflop, kms = "fp64_phase1 (GEMM0: W = psi op(R))", flop0, p1
+    achieved = kflop / (kms * 1e-3) / 1e12
+    # ---- e2e leg: host buffers through the C ABI host entry
+    psi_h = torch.from_numpy(prob.psi).pin_memory().numpy()
+    sig_h = torch.zeros(prob.sigma_size, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(max(1, args.warmup)):
+        sig_h[:] = 0.0
+        heff(psi_h, sig_h, 1.0, form)
+    e2e_t = []
+    if dist is not None:
+        dist.barrier()
+    for _ in range(args.steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ctx.synchronize()
+        t0 = time.perf_counter()
+        sig_h[:] = 0.0
+        heff(psi_h, sig_h, 1.0, form)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_t)
+    check = float(np.linalg.norm(sig_h))
+    # ---- max over ranks
+    tot = torch.tensor([total_s, e2e_total], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    total_s, e2e_total = float(tot[0]), float(tot[1])
+    value = flop * args.steps * world / total_s / 1e12
+    e2e_value = flop * args.steps * world / e2e_total / 1e12
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "TFLOP/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_s / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": prob.meta.get("data", "synthetic"),
+        "config": {
+            "workload": args.workload,
+            "description": prob.meta.get("description", ""),
+            "form": args.form,
+            "n_pairs": st["n_pairs"], "n_work_dedup": st["n_work"], "n_sigma_regions": st["n_regions"],
+            "mnk": st["mnk"], "mnk_executed": st["mnk_executed"], "psi_size": prob.psi_size,
+            "ops_bytes": st["ops_bytes"],
+            "l2": "flushed between steps (512 MB write)" if flush is not None else
+                  "inputs larger than L2 (operator blob + work > 4x L2)",
+            "parallelism": f"replicas x{world}",
+            "wall_s_timed_region": t_wall,
+        },
+        "roofline": {
+            "bound": "fp64-pipe",
+            "kernel": kname,
+            "achieved": achieved,
+            "peak": pk.value,
+            "unit": "TFLOP/s",
+            "frac": achieved / pk.value if pk.value else None,
+            "peak_source": "measured in this run: register-resident FP64 FMA loop (b2g_probe_peak); "
+                           "GB300 has no FP64 tensor path, MEASURED_PEAKS.json holds no FP64 figure",
+            "phase_ms": {"gemm0": p1, "gemm1": p2},
+            "traffic": None,
+        },
+        "e2e": {
+            "value": e2e_value, "unit": "TFLOP/s",
+            "h2d_bytes_per_step": 8 * (prob.psi_size + prob.sigma_size),
+            "d2h_bytes_per_step": 8 * prob.sigma_size,
+            "ms_per_step": e2e_total / args.steps * 1e3,
+        },
+        "gpu_launches": args.steps * 2,
+        "clocks": ck,
+        "sigma_norm": check,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        times, nth, blas = cpu_replay_timing(prob, max_steps=10, budget_s=20.0, warmup=1)
+        result["cpu_baseline"] = {
+            "value": flop / statistics.median(times) / 1e12, "unit": "TFLOP/s", "cores": nth,
+            "kind": "port",
+            "sample": f"{len(times)} full H_eff*psi products of this workload (median), oracle replay "
+                      f"with {'BLAS dgemm' if blas else 'loop'} per pair, {nth} OpenMP threads",
+        }
+    heff.close()
+    ctx.close()
+    return result
+
+
+def run_reference(args):
+    prob = load_workload(args.workload)
+    flop = 2.0 * prob.mnk
+    times, nth, blas = cpu_replay_timing(prob, max_steps=args.steps, budget_s=120.0,
+                                         warmup=min(args.warmup, 1))
+    v = flop * len(times) / sum(times) / 1e12
+    return {
+        "metric": METRIC, "value": v, "unit": "TFLOP/s", "impl": "reference", "n_gpus": 0,
+        "steps": len(times), "warmup": min(args.warmup, 1), "ms_per_step": sum(times) / len(times) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": prob.meta.get("data", "synthetic"),
+        "config": {"workload": args.workload, "form": "fp64", "mnk": prob.mnk, "psi_size": prob.psi_size},
+        "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": nth, "kind": "port",
+                         "sample": f"{len(times)} H_eff*psi products (of {args.steps} requested, "
+                                   f"120 s budget), {'BLAS dgemm' if blas else 'loop'} per pair"},
+        "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=None)
+    ap.add_argument("--form", default="fp64", choices=["fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    from b2g import workloads
+    if args.workload is None:
+        args.workload = workloads.DEFAULT
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local_rank)
+        td.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        dist = td
+    res = run_ours(args, rank, local_rank, world, dist)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

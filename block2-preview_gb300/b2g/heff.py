@@ -1,0 +1,135 @@
+"""Host-side mirror of block2's EffectiveHamiltonian for the GB300 path.
+
+The reference builds one EffectiveHamiltonian per site
+(src/dmrg/effective_hamiltonian.hpp:99-1160): ``precompute`` records the GEMM
+pairs of H_eff*psi into BatchGEMMSeq, the Davidson operator replays them
+through ``TensorFunctions::operator()(b, c, scale)`` (c += scale * H b), and
+``eigs`` returns (energy, ndav, nflop, tdav).  This class keeps those names
+and meanings; the recorded pairs and the operator blob become a device plan
+(b2g_heff_create), every product runs on the GPU (b2g_heff_apply), and
+Davidson runs device-resident (b2g_davidson).  Errors surface as B2GError
+(the reference throws std::runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import capi
+from .capi import FP64, TF32X3, B2GError, PairSeq, check, lib
+
+
+class Context:
+    """One device context (b2g_context): the device and the stream kernels run on."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().b2g_context_create(device, C.byref(self._h)))
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream_ptr(self) -> int:
+        return lib().b2g_context_stream(self._h) or 0
+
+    def synchronize(self):
+        check(lib().b2g_context_synchronize(self._h))
+
+    def close(self):
+        if self._h:
+            lib().b2g_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(x):
+    """Raw data pointer of a numpy array or a torch tensor."""
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+class EffectiveHamiltonian:
+    """Device plan of one H_eff built from its recorded pair sequence.
+
+    seq: PairSeq (or dict of arrays) -- BatchGEMMSeq batch[0]/batch[1] pairs
+    ops: float64 operator blob (numpy, host) the pair offsets index
+    psi_size / sigma_size: lengths of the ket / bra wavefunctions
+    """
+
+    def __init__(self, ctx: Context, seq, ops, psi_size: int, sigma_size: int):
+        if not isinstance(seq, PairSeq):
+            seq = PairSeq(seq)
+        self.ctx = ctx
+        self.seq = seq
+        ops = np.ascontiguousarray(ops, dtype=np.float64)
+        self.psi_size, self.sigma_size = int(psi_size), int(sigma_size)
+        self._h = C.c_void_p()
+        check(lib().b2g_heff_create(ctx.handle, C.byref(seq.c), ops.ctypes.data, ops.size, 0,
+                                    self.psi_size, self.sigma_size, C.byref(self._h)))
+        st = capi.HeffStatsC()
+        check(lib().b2g_heff_stats_get(self._h, C.byref(st)))
+        self.stats = st.as_dict()
+        self.nflop = 2.0 * self.stats["mnk"]    # FLOP of one product (2 x reference mnk)
+
+    # c += scale * H_eff * b   (TensorFunctions::operator(), tensor_functions.hpp:59-62)
+    def __call__(self, b, c, scale: float = 1.0, form: int = FP64):
+        if isinstance(b, np.ndarray) != isinstance(c, np.ndarray):
+            raise TypeError("b and c must both be host numpy arrays or both device tensors")
+        if isinstance(b, np.ndarray):
+            if b.dtype != np.float64 or c.dtype != np.float64 or not c.flags.c_contiguous:
+                raise TypeError("host buffers must be contiguous float64")
+            if b.size != self.psi_size or c.size != self.sigma_size:
+                raise ValueError("wavefunction sizes do not match the effective Hamiltonian")
+            bb = np.ascontiguousarray(b)
+            check(lib().b2g_heff_apply_host(self._h, bb.ctypes.data, c.ctypes.data, scale, form))
+        else:
+            if b.numel() != self.psi_size or c.numel() != self.sigma_size:
+                raise ValueError("wavefunction sizes do not match the effective Hamiltonian")
+            if not (b.is_cuda and c.is_cuda and b.is_contiguous() and c.is_contiguous()):
+                raise TypeError("device buffers must be contiguous CUDA tensors")
+            check(lib().b2g_heff_apply(self._h, _ptr(b), _ptr(c), scale, form))
+        return c
+
+    def apply_ptr(self, psi_ptr: int, sigma_ptr: int, scale: float = 1.0, form: int = FP64):
+        """Raw device-pointer entry (asynchronous on the context stream)."""
+        check(lib().b2g_heff_apply(self._h, psi_ptr, sigma_ptr, scale, form))
+
+    # EffectiveHamiltonian::eigs (effective_hamiltonian.hpp:481-568) for one root
+    def eigs(self, diag, psi, conv_thrd: float = 5e-6, max_iter: int = 5000,
+             def_min: int = 2, def_max: int = 50, form: int = FP64):
+        """Lowest eigenpair; psi (host float64) is the initial guess and is
+        overwritten with the eigenvector.  Returns (energy, ndav, nflop, tdav)."""
+        diag = np.ascontiguousarray(diag, dtype=np.float64)
+        if psi.dtype != np.float64 or not psi.flags.c_contiguous:
+            raise TypeError("psi must be a contiguous float64 array")
+        res = capi.DavidsonResultC()
+        t0 = time.perf_counter()
+        rc = lib().b2g_davidson(self._h, diag.ctypes.data, psi.ctypes.data, conv_thrd, max_iter,
+                                def_min, def_max, form, C.byref(res))
+        tdav = time.perf_counter() - t0
+        check(rc)
+        self.last_davidson = res
+        nflop = self.nflop * (res.n_apply_fp64 + res.n_apply_mixed)
+        return res.energy, res.n_iter, nflop, tdav
+
+    def close(self):
+        if self._h:
+            lib().b2g_heff_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,284 @@
+// C ABI entry points (declared in include/b2g.h): context, H_eff plan
+// creation/upload, H_eff*psi in the FP64 and tensor-core forms.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "b2g_internal.h"
+
+namespace b2g {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg) {
+    set_error(msg);
+    return code;
+}
+
+template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaStream_t s) {
+    *dst = nullptr;
+    if (v.empty())
+        return B2G_OK;
+    if (cudaMalloc((void **)dst, sizeof(T) * v.size()) != cudaSuccess) {
+        *dst = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for plan table");
+    }
+    B2G_CUDA_TRY(cudaMemcpyAsync(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return B2G_OK;
+}
+
+static void free_plan(DevicePlan &p) {
+    cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
+    cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
+    p = DevicePlan();
+}
+
+} // namespace b2g
+
+using namespace b2g;
+
+extern "C" {
+
+int b2g_version(void) { return 1; }
+
+const char *b2g_last_error(void) { return g_last_error.c_str(); }
+
+int b2g_context_create(int device, b2g_context **out) {
+    if (out == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_context_create: null output");
+    *out = nullptr;
+    int n = 0;
+    B2G_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n)
+        return fail(B2G_ERR_ARG, "b2g_context_create: no CUDA device " + std::to_string(device));
+    B2G_CUDA_TRY(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    B2G_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (prop.major * 10 + prop.minor < 100)
+        return fail(B2G_ERR_UNSUPPORTED, std::string("b2g: device ") + prop.name +
+                                             " is not a Blackwell (sm_10x) GPU");
+    b2g_context *c = new b2g_context();
+    c->device = device;
+    c->n_sm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return fail(B2G_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    *out = c;
+    return B2G_OK;
+}
+
+int b2g_context_destroy(b2g_context *ctx) {
+    if (ctx == nullptr)
+        return B2G_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return B2G_OK;
+}
+
+void *b2g_context_stream(b2g_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int b2g_context_synchronize(b2g_context *ctx) {
+    if (ctx == nullptr)
+        return fail(B2G_ERR_ARG, "null context");
+    B2G_CUDA_TRY(cudaSetDevice(ctx->device));
+    B2G_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2G_OK;
+}
+
+int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops,
+                    uint64_t ops_size, int ops_on_device, uint64_t psi_size, uint64_t sigma_size,
+                    b2g_heff **out) {
+    if (ctx == nullptr || seq == nullptr || out == nullptr || (ops == nullptr && ops_size != 0))
+        return fail(B2G_ERR_ARG, "b2g_heff_create: null argument");
+    *out = nullptr;
+    B2G_CUDA_TRY(cudaSetDevice(ctx->device));
+    HostPlan hp;
+    int rc = build_plan(seq, ops_size, psi_size, sigma_size, hp);
+    if (rc != B2G_OK)
+        return rc;
+    b2g_heff *h = new b2g_heff();
+    h->ctx = ctx;
+    h->ops_size = ops_size, h->psi_size = psi_size, h->sigma_size = sigma_size;
+    h->work_size = hp.work_size;
+    auto bail = [&](int code) {
+        free_plan(h->plan);
+        cudaFree(h->ops), cudaFree(h->work);
+        delete h;
+        return code;
+    };
+    cudaStream_t s = ctx->stream;
+    if (ops_size) {
+        if (cudaMalloc(&h->ops, sizeof(double) * ops_size) != cudaSuccess) {
+            h->ops = nullptr;
+            return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the operator blob"));
+        }
+        if (cudaMemcpyAsync(h->ops, ops, sizeof(double) * ops_size,
+                            ops_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            s) != cudaSuccess)
+            return bail(fail(B2G_ERR_CUDA, "operator blob upload failed"));
+    }
+    if (hp.work_size && cudaMalloc(&h->work, sizeof(double) * hp.work_size) != cudaSuccess) {
+        h->work = nullptr;
+        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the work buffer"));
+    }
+    DevicePlan &p = h->plan;
+    if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
+        (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
+        (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)))
+        return bail(rc);
+    p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
+    p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
+    p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+        return bail(fail(B2G_ERR_CUDA, "plan upload failed"));
+    b2g_heff_stats &st = h->stats;
+    st.n_pairs = seq->n_pairs;
+    st.n_work = p.n_works;
+    st.n_regions = p.n_regions;
+    st.n_tiles = p.n_t2;
+    st.mnk = hp.mnk;
+    st.mnk_executed = hp.mnk_exec;
+    st.ops_bytes = sizeof(double) * ops_size;
+    st.work_bytes = sizeof(double) * hp.work_size;
+    st.plan_bytes = sizeof(WorkDesc) * hp.works.size() + sizeof(Contrib) * hp.contribs.size() +
+                    sizeof(Region) * hp.regions.size() + sizeof(Task1) * hp.t1.size() +
+                    sizeof(Task2) * hp.t2.size() + sizeof(int32_t) * hp.lists.size();
+    st.psi_size = psi_size, st.sigma_size = sigma_size;
+    *out = h;
+    return B2G_OK;
+}
+
+int b2g_heff_destroy(b2g_heff *h) {
+    if (h == nullptr)
+        return B2G_OK;
+    cudaSetDevice(h->ctx->device);
+    cudaStreamSynchronize(h->ctx->stream);
+    free_plan(h->plan);
+    cudaFree(h->ops), cudaFree(h->work), cudaFree(h->psi_stage), cudaFree(h->sigma_stage);
+    for (auto &e : h->ev)
+        if (e)
+            cudaEventDestroy(e);
+    delete h;
+    return B2G_OK;
+}
+
+int b2g_heff_set_timing(b2g_heff *h, int enable) {
+    if (h == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_set_timing: null handle");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    if (enable && h->ev[0] == nullptr)
+        for (auto &e : h->ev)
+            B2G_CUDA_TRY(cudaEventCreate(&e));
+    h->timing = enable != 0;
+    return B2G_OK;
+}
+
+int b2g_heff_last_timing(b2g_heff *h, float *ms) {
+    if (h == nullptr || ms == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_last_timing: null argument");
+    if (!h->timing)
+        return fail(B2G_ERR_STATE, "b2g_heff_last_timing: timing not enabled");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    B2G_CUDA_TRY(cudaEventSynchronize(h->ev[2]));
+    B2G_CUDA_TRY(cudaEventElapsedTime(&ms[0], h->ev[0], h->ev[1]));
+    B2G_CUDA_TRY(cudaEventElapsedTime(&ms[1], h->ev[1], h->ev[2]));
+    return B2G_OK;
+}
+
+int b2g_probe_peak(b2g_context *ctx, int form, double *tflops) {
+    if (ctx == nullptr || tflops == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_probe_peak: null argument");
+    B2G_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (form == B2G_FP64) {
+        B2G_CUDA_TRY(probe_fp64_peak(ctx->stream, ctx->n_sm, tflops));
+        return B2G_OK;
+    }
+    return fail(B2G_ERR_UNSUPPORTED, "b2g_probe_peak: form not available");
+}
+
+int b2g_heff_stats_get(const b2g_heff *h, b2g_heff_stats *out) {
+    if (h == nullptr || out == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_stats_get: null argument");
+    *out = h->stats;
+    return B2G_OK;
+}
+
+int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size,
+                   uint64_t sigma_size, b2g_heff_stats *out) {
+    if (seq == nullptr || out == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_plan_stats: null argument");
+    HostPlan hp;
+    int rc = build_plan(seq, ops_size, psi_size, sigma_size, hp);
+    if (rc != B2G_OK)
+        return rc;
+    b2g_heff_stats st{};
+    st.n_pairs = seq->n_pairs;
+    st.n_work = (int64_t)hp.works.size();
+    st.n_regions = (int64_t)hp.regions.size();
+    st.n_tiles = (int64_t)hp.t2.size();
+    st.mnk = hp.mnk;
+    st.mnk_executed = hp.mnk_exec;
+    st.ops_bytes = sizeof(double) * ops_size;
+    st.work_bytes = sizeof(double) * hp.work_size;
+    st.plan_bytes = sizeof(WorkDesc) * hp.works.size() + sizeof(Contrib) * hp.contribs.size() +
+                    sizeof(Region) * hp.regions.size() + sizeof(Task1) * hp.t1.size() +
+                    sizeof(Task2) * hp.t2.size() + sizeof(int32_t) * hp.lists.size();
+    st.psi_size = psi_size, st.sigma_size = sigma_size;
+    *out = st;
+    return B2G_OK;
+}
+
+int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {
+    if (h == nullptr || (h->psi_size && psi == nullptr) || (h->sigma_size && sigma == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_apply: null argument");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    cudaStream_t s = h->ctx->stream;
+    if (form == B2G_FP64) {
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+        B2G_CUDA_TRY(launch_fp64_phase1(h->plan, h->ops, psi, h->work, s));
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+        B2G_CUDA_TRY(launch_fp64_phase2(h->plan, h->ops, h->work, sigma, scale, s));
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+        return B2G_OK;
+    }
+    return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_apply: unknown form " + std::to_string(form));
+}
+
+int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {
+    if (h == nullptr || (h->psi_size && psi == nullptr) || (h->sigma_size && sigma == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_apply_host: null argument");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    cudaStream_t s = h->ctx->stream;
+    if (h->psi_stage == nullptr && h->psi_size &&
+        cudaMalloc(&h->psi_stage, sizeof(double) * h->psi_size) != cudaSuccess) {
+        h->psi_stage = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for psi staging");
+    }
+    if (h->sigma_stage == nullptr && h->sigma_size &&
+        cudaMalloc(&h->sigma_stage, sizeof(double) * h->sigma_size) != cudaSuccess) {
+        h->sigma_stage = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for sigma staging");
+    }
+    B2G_CUDA_TRY(cudaMemcpyAsync(h->psi_stage, psi, sizeof(double) * h->psi_size,
+                                 cudaMemcpyHostToDevice, s));
+    B2G_CUDA_TRY(cudaMemcpyAsync(h->sigma_stage, sigma, sizeof(double) * h->sigma_size,
+                                 cudaMemcpyHostToDevice, s));
+    int rc = b2g_heff_apply(h, h->psi_stage, h->sigma_stage, scale, form);
+    if (rc != B2G_OK)
+        return rc;
+    B2G_CUDA_TRY(cudaMemcpyAsync(sigma, h->sigma_stage, sizeof(double) * h->sigma_size,
+                                 cudaMemcpyDeviceToHost, s));
+    B2G_CUDA_TRY(cudaStreamSynchronize(s));
+    return B2G_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,408 @@
+// Device-resident Davidson eigensolver for the lowest eigenpair of H_eff.
+//
+// Restates IterativeMatrixFunctions::davidson for one root, Normal type,
+// Olsen preconditioner (src/core/iterative_matrix_functions.hpp:864-1173,
+// 93-108) with the same basis growth, convergence test (|r|^2 < conv_thrd),
+// restart to def_min vectors when def_max is reached, and orthogonalisation
+// of the correction vector.  Arithmetic differences from the reference,
+// all exact in exact arithmetic:
+//   * the basis is not rotated to Ritz vectors every iteration; the Ritz
+//     vector x = B v and its H-image s = Sigma v are formed directly and the
+//     subspace matrix grows by one row per new vector (the reference rotates
+//     all m vectors and recomputes all m^2 dot products each iteration);
+//     the rotation to the def_min lowest Ritz vectors happens only at restart;
+//   * the small subspace eigenproblem (LAPACK dsyev in the reference) is
+//     solved on the device by parallel cyclic Jacobi (one CTA, FP64);
+//   * the correction vector is orthogonalised by classical Gram-Schmidt
+//     applied twice (the reference applies modified Gram-Schmidt once).
+// All vectors live in HBM; per iteration only (lambda, |r|^2) come back to
+// the host for the convergence decision.  Reductions are two-stage
+// (per-block partials, then a fixed-order sum): results are bit-reproducible.
+#include <cmath>
+#include <vector>
+
+#include "b2g_internal.h"
+
+namespace b2g {
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 304;   // 2 x 152 SMs
+constexpr int kMaxSub = 64;       // def_max limit (Jacobi in one CTA)
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// partial[j * gridDim.x + block] = sum over this block's slice of X_j . y
+// X_j = X + j * ldx (j < nv)
+__global__ void __launch_bounds__(kRedThreads) multidot_partial(const double *__restrict__ X,
+                                                                uint64_t ldx, int nv,
+                                                                const double *__restrict__ y,
+                                                                uint64_t n, double *partial) {
+    __shared__ double red[kRedThreads / 32];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int j = 0; j < nv; j++) {
+        const double *x = X + (uint64_t)j * ldx;
+        double s = 0.0;
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+            s = fma(x[i], y[i], s);
+        s = warp_sum(s);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = threadIdx.x < kRedThreads / 32 ? red[threadIdx.x] : 0.0;
+            v = warp_sum(v);
+            if (threadIdx.x == 0)
+                partial[(uint64_t)j * gridDim.x + blockIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// out[j] = sum_b partial[j * nb + b] (fixed order), one warp per j
+__global__ void multidot_final(const double *__restrict__ partial, int nb, int nv, double *out) {
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (j >= nv)
+        return;
+    double s = 0.0;
+    for (int b = lane; b < nb; b += 32)
+        s += partial[(uint64_t)j * nb + b];
+    s = warp_sum(s);
+    if (lane == 0)
+        out[j] = s;
+}
+
+// y = beta * y + sum_j coef[j] * X_j   (coef on device, optionally negated)
+__global__ void combine(double *__restrict__ y, double beta, const double *__restrict__ X,
+                        uint64_t ldx, int nv, const double *__restrict__ coef, double coef_sign,
+                        uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double s = beta == 0.0 ? 0.0 : beta * y[i];
+        for (int j = 0; j < nv; j++)
+            s = fma(coef_sign * coef[j], X[(uint64_t)j * ldx + i], s);
+        y[i] = s;
+    }
+}
+
+// Y_j = sum_i X_i V[i, j] for j < nout (V row-major ldv) -- restart rotation
+__global__ void rotate_basis(double *__restrict__ Y, const double *__restrict__ X, uint64_t ld,
+                             int m, int nout, const double *__restrict__ V, int ldv, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        for (int j = 0; j < nout; j++) {
+            double s = 0.0;
+            for (int k = 0; k < m; k++)
+                s = fma(X[(uint64_t)k * ld + i], V[k * ldv + j], s);
+            Y[(uint64_t)j * ld + i] = s;
+        }
+}
+
+// q = s - lambda x ; in the same pass the Olsen quantities
+//   t = x / (lambda - d), q' = q / (lambda - d) where |lambda - d| > 1e-12
+__global__ void residual_olsen(double *__restrict__ q, double *__restrict__ t,
+                               const double *__restrict__ s, const double *__restrict__ x,
+                               const double *__restrict__ diag, const double *__restrict__ lam,
+                               uint64_t n, int precondition) {
+    const double l = lam[0];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double qi = s[i] - l * x[i];
+        double ti = x[i];
+        if (precondition) {
+            const double den = l - diag[i];
+            if (fabs(den) > 1e-12)
+                qi /= den, ti /= den;
+        }
+        q[i] = qi;
+        t[i] = ti;
+    }
+}
+
+// q -= (d[0] / d[1]) * t   (Olsen: (x, K^-1 q) / (x, K^-1 x))
+__global__ void olsen_update(double *__restrict__ q, const double *__restrict__ t,
+                             const double *__restrict__ d, uint64_t n) {
+    const double r = d[0] / d[1];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        q[i] = fma(-r, t[i], q[i]);
+}
+
+// y = x / sqrt(d[0])
+__global__ void normalize_into(double *__restrict__ y, const double *__restrict__ x,
+                               const double *__restrict__ d, uint64_t n) {
+    const double f = 1.0 / sqrt(d[0]);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        y[i] = x[i] * f;
+}
+
+// Parallel cyclic Jacobi (round-robin pairing) on the m x m symmetric matrix
+// A (row-major, lda), one CTA.  Outputs eigenvalues ascending in w[0..m) and
+// eigenvectors as columns of V (row-major, ldv = kMaxSub).
+__global__ void __launch_bounds__(256) jacobi_eig(const double *__restrict__ Ain, int lda, int m,
+                                                  double *__restrict__ w, double *__restrict__ V) {
+    __shared__ double A[kMaxSub][kMaxSub + 1];
+    __shared__ double Vs[kMaxSub][kMaxSub + 1];
+    __shared__ double cs[kMaxSub / 2], sn[kMaxSub / 2];
+    __shared__ int pp[kMaxSub / 2], qq[kMaxSub / 2];
+    __shared__ int perm[kMaxSub];
+    __shared__ double off_s;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int mm = m + (m & 1);  // padded to even: the extra index is a dummy
+    for (int i = tid; i < mm * mm; i += nt) {
+        const int r = i / mm, c = i % mm;
+        A[r][c] = (r < m && c < m) ? Ain[r * lda + c] : 0.0;
+        Vs[r][c] = r == c ? 1.0 : 0.0;
+    }
+    for (int i = tid; i < mm; i += nt)
+        perm[i] = i;
+    __syncthreads();
+    const int half = mm / 2;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        if (tid == 0) {
+            double off = 0.0, tot = 0.0;
+            for (int r = 0; r < m; r++)
+                for (int c = 0; c < m; c++)
+                    (r == c ? tot : off) += A[r][c] * A[r][c];
+            off_s = (off <= 1e-30 * (tot + off)) ? -1.0 : off;
+        }
+        __syncthreads();
+        if (off_s < 0.0)
+            break;
+        for (int step = 0; step < mm - 1; step++) {
+            // pairs of this round: (perm[k], perm[mm-1-k])
+            for (int k = tid; k < half; k += nt) {
+                int p = perm[k], q = perm[mm - 1 - k];
+                if (p > q) {
+                    int t = p;
+                    p = q, q = t;
+                }
+                pp[k] = p, qq[k] = q;
+                double c = 1.0, s = 0.0;
+                if (q < m && A[p][q] != 0.0) {
+                    const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                    const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                    c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                }
+                cs[k] = c, sn[k] = s;
+            }
+            __syncthreads();
+            // columns: A <- A J
+            for (int i = tid; i < half * mm; i += nt) {
+                const int k = i / mm, r = i % mm, p = pp[k], q = qq[k];
+                const double c = cs[k], s = sn[k];
+                const double arp = A[r][p], arq = A[r][q];
+                A[r][p] = c * arp - s * arq;
+                A[r][q] = s * arp + c * arq;
+                const double vrp = Vs[r][p], vrq = Vs[r][q];
+                Vs[r][p] = c * vrp - s * vrq;
+                Vs[r][q] = s * vrp + c * vrq;
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int i = tid; i < half * mm; i += nt) {
+                const int k = i / mm, r = i % mm, p = pp[k], q = qq[k];
+                const double c = cs[k], s = sn[k];
+                const double apr = A[p][r], aqr = A[q][r];
+                A[p][r] = c * apr - s * aqr;
+                A[q][r] = s * apr + c * aqr;
+            }
+            __syncthreads();
+            // rotate the tournament (index 0 fixed)
+            if (tid == 0) {
+                const int last = perm[mm - 1];
+                for (int k = mm - 1; k > 1; k--)
+                    perm[k] = perm[k - 1];
+                perm[1] = last;
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0) {
+        // sort ascending (selection), record order in perm
+        for (int i = 0; i < m; i++)
+            perm[i] = i;
+        for (int i = 0; i < m; i++) {
+            int b = i;
+            for (int j = i + 1; j < m; j++)
+                if (A[perm[j]][perm[j]] < A[perm[b]][perm[b]])
+                    b = j;
+            const int t = perm[i];
+            perm[i] = perm[b], perm[b] = t;
+        }
+        for (int i = 0; i < m; i++)
+            w[i] = A[perm[i]][perm[i]];
+    }
+    __syncthreads();
+    for (int i = tid; i < m * m; i += nt) {
+        const int r = i / m, c = i % m;
+        V[r * kMaxSub + c] = Vs[r][perm[c]];
+    }
+}
+
+// A[i * lda + j] = A[j * lda + i] = v[j] for j <= i (new subspace row)
+__global__ void set_sub_row(double *A, int lda, int i, const double *v) {
+    const int j = threadIdx.x;
+    if (j <= i) {
+        A[i * lda + j] = v[j];
+        A[j * lda + i] = v[j];
+    }
+}
+
+// A = diag(w[0..m)) (restart)
+__global__ void set_sub_diag(double *A, int lda, int m, const double *w) {
+    for (int i = threadIdx.x; i < lda * lda; i += blockDim.x) {
+        const int r = i / lda, c = i % lda;
+        A[i] = (r == c && r < m) ? w[r] : 0.0;
+    }
+}
+
+int grid_for(uint64_t n) {
+    uint64_t b = (n + 255) / 256;
+    return (int)std::min<uint64_t>(b ? b : 1, 152 * 8);
+}
+
+} // namespace
+
+} // namespace b2g
+
+using namespace b2g;
+
+extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double conv_thrd,
+                            int max_iter, int def_min, int def_max, int form,
+                            b2g_davidson_result *res) {
+    if (h == nullptr || diag == nullptr || psi == nullptr || res == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_davidson: null argument");
+    if (h->psi_size != h->sigma_size)
+        return fail(B2G_ERR_ARG, "b2g_davidson: H_eff is not square (bra != ket size)");
+    if (def_min < 1)
+        def_min = 1;
+    if (def_max < def_min + 1)
+        def_max = def_min + 1;
+    if (def_max > kMaxSub)
+        return fail(B2G_ERR_ARG, "b2g_davidson: def_max above 64");
+    if (form != B2G_FP64)
+        return fail(B2G_ERR_UNSUPPORTED, "b2g_davidson: form not available");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    cudaStream_t st = h->ctx->stream;
+    const uint64_t n = h->psi_size;
+    const int g = grid_for(n);
+    // device workspace: B, S (def_max vectors each), x, s, q, t, tmp (def_min vectors), diag
+    double *B = nullptr, *S = nullptr, *x = nullptr, *s = nullptr, *q = nullptr, *t = nullptr,
+           *R = nullptr, *D = nullptr, *small = nullptr, *partial = nullptr;
+    const size_t nsmall = (size_t)kMaxSub * kMaxSub * 2 + 4 * kMaxSub + 16;
+    auto cleanup = [&]() {
+        cudaFree(B), cudaFree(S), cudaFree(x), cudaFree(s), cudaFree(q), cudaFree(t), cudaFree(R);
+        cudaFree(D), cudaFree(small), cudaFree(partial);
+    };
+    if (cudaMalloc(&B, sizeof(double) * n * def_max) || cudaMalloc(&S, sizeof(double) * n * def_max) ||
+        cudaMalloc(&x, sizeof(double) * n) || cudaMalloc(&s, sizeof(double) * n) ||
+        cudaMalloc(&q, sizeof(double) * n) || cudaMalloc(&t, sizeof(double) * n) ||
+        cudaMalloc(&R, sizeof(double) * n * def_min) || cudaMalloc(&D, sizeof(double) * n) ||
+        cudaMalloc(&small, sizeof(double) * nsmall) ||
+        cudaMalloc(&partial, sizeof(double) * kRedBlocks * kMaxSub)) {
+        cleanup();
+        return fail(B2G_ERR_NOMEM, "b2g_davidson: device workspace allocation failed");
+    }
+    double *A = small;                          // kMaxSub x kMaxSub subspace matrix
+    double *V = A + kMaxSub * kMaxSub;          // eigenvectors (columns), ld kMaxSub
+    double *w = V + kMaxSub * kMaxSub;          // eigenvalues
+    double *dots = w + kMaxSub;                 // kMaxSub dot results
+    double *sc = dots + kMaxSub;                // scalars: [0] lambda, [1] |q|^2, [2..3] olsen
+    double *coef = sc + 16;                     // kMaxSub coefficients
+    auto dot_many = [&](const double *X, int nv, const double *y, double *out) {
+        multidot_partial<<<kRedBlocks, kRedThreads, 0, st>>>(X, n, nv, y, n, partial);
+        multidot_final<<<(nv + 7) / 8, 256, 0, st>>>(partial, kRedBlocks, nv, out);
+    };
+    int rc = B2G_OK;
+#define DAV_TRY(expr)                                                                       \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            rc = fail(B2G_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));    \
+            goto done;                                                                      \
+        }                                                                                   \
+    } while (0)
+    {
+        DAV_TRY(cudaMemcpyAsync(D, diag, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        DAV_TRY(cudaMemcpyAsync(q, psi, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        DAV_TRY(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st));
+        dot_many(q, 1, q, sc + 1);
+        normalize_into<<<g, 256, 0, st>>>(B, q, sc + 1, n);
+        int m = 1, msig = 0, xiter = 0, n_apply = 0;
+        double lam = 0.0, qq = 0.0;
+        bool converged = false;
+        while (xiter < max_iter) {
+            xiter++;
+            for (int i = msig; i < m; i++, msig++) {
+                double *si = S + (uint64_t)i * n;
+                DAV_TRY(cudaMemsetAsync(si, 0, sizeof(double) * n, st));
+                rc = b2g_heff_apply(h, B + (uint64_t)i * n, si, 1.0, B2G_FP64);
+                if (rc != B2G_OK)
+                    goto done;
+                n_apply++;
+                // A(i, j) = <b_i | sigma_j>, j <= i
+                dot_many(S, i + 1, B + (uint64_t)i * n, dots);
+                set_sub_row<<<1, kMaxSub, 0, st>>>(A, kMaxSub, i, dots);
+            }
+            jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
+            // x = B v0, s = S v0 (v0 = column 0 of V, stride kMaxSub)
+            rotate_basis<<<g, 256, 0, st>>>(x, B, n, m, 1, V, kMaxSub, n);
+            rotate_basis<<<g, 256, 0, st>>>(s, S, n, m, 1, V, kMaxSub, n);
+            residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 0);
+            dot_many(q, 1, q, sc + 1);
+            DAV_TRY(cudaMemcpyAsync(&lam, w, sizeof(double), cudaMemcpyDeviceToHost, st));
+            DAV_TRY(cudaMemcpyAsync(&qq, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+            DAV_TRY(cudaStreamSynchronize(st));
+            if (qq < conv_thrd) {
+                converged = true;
+                break;
+            }
+            // Olsen correction: q = K^-1 r - (x,K^-1 r)/(x,K^-1 x) K^-1 x
+            residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 1);
+            dot_many(q, 1, x, sc + 2);
+            dot_many(t, 1, x, sc + 3);
+            olsen_update<<<g, 256, 0, st>>>(q, t, sc + 2, n);
+            if (m >= def_max) {
+                // restart with the def_min lowest Ritz vectors
+                rotate_basis<<<g, 256, 0, st>>>(R, B, n, m, def_min, V, kMaxSub, n);
+                DAV_TRY(cudaMemcpyAsync(B, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st));
+                rotate_basis<<<g, 256, 0, st>>>(R, S, n, m, def_min, V, kMaxSub, n);
+                DAV_TRY(cudaMemcpyAsync(S, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st));
+                set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, def_min, w);
+                m = msig = def_min;
+            }
+            // classical Gram-Schmidt, twice
+            for (int pass = 0; pass < 2; pass++) {
+                dot_many(B, m, q, coef);
+                combine<<<g, 256, 0, st>>>(q, 1.0, B, n, m, coef, -1.0, n);
+            }
+            dot_many(q, 1, q, sc + 1);
+            normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)m * n, q, sc + 1, n);
+            m++;
+        }
+        DAV_TRY(cudaGetLastError());
+        DAV_TRY(cudaMemcpyAsync(psi, x, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        DAV_TRY(cudaStreamSynchronize(st));
+        res->energy = lam;
+        res->n_iter = xiter;
+        res->n_apply_fp64 = n_apply;
+        res->n_apply_mixed = 0;
+        res->residual_norm2 = qq;
+        if (!converged)
+            rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_davidson: max_iter reached");
+    }
+done:
+#undef DAV_TRY
+    cudaStreamSynchronize(st);
+    cleanup();
+    return rc;
+}

@@ -1,0 +1,188 @@
+// Plain FP64 form of H_eff*psi on sm_103a.
+//
+// GB300 executes FP64 on CUDA-core DFMA units only (no FP64 tensor path), at
+// a small fraction of its tensor rate, so these kernels are DFMA-issue bound:
+// the design goal is that every issued DFMA lane does useful work (no padded
+// tiles) and that enough independent warps are resident to hide latency.
+// Operands are re-read through L1/L2 (the operator blocks of one H_eff are
+// reused by many pairs and stay L2-resident); see the phase comments below.
+#include "b2g_internal.h"
+
+namespace b2g {
+
+namespace {
+
+constexpr int kLanesCols = 8;   // column chunks of 32 per warp (256 columns)
+
+// Phase 1: one warp per row r of a distinct product W_u (m0 x n0):
+//   W_u[r, c] = sum_k psi[a0 + r*lda0 + k] * B(k, c),
+//   B(k, c) = ops[b0 + k*ldb0 + c] (tb0 = 0) or ops[b0 + c*ldb0 + k] (tb0 = 1).
+// psi loads are warp-broadcast; B loads are coalesced for tb0 = 0 and
+// L1-served column walks for tb0 = 1.
+__global__ void __launch_bounds__(128) fp64_phase1(const WorkDesc *__restrict__ works,
+                                                   const Task1 *__restrict__ tasks, int64_t n_tasks,
+                                                   const double *__restrict__ ops,
+                                                   const double *__restrict__ psi,
+                                                   double *__restrict__ work) {
+    const int64_t t = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (t >= n_tasks)
+        return;
+    const Task1 tk = tasks[t];
+    const WorkDesc wd = works[tk.u];
+    const double *prow = psi + wd.a0 + (uint64_t)tk.r * wd.lda0;
+    const double *B = ops + wd.b0;
+    double *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
+    for (int cbase = 0; cbase < wd.n0; cbase += 32 * kLanesCols) {
+        double acc[kLanesCols];
+#pragma unroll
+        for (int j = 0; j < kLanesCols; j++)
+            acc[j] = 0.0;
+        const int nj = min(kLanesCols, (wd.n0 - cbase + 31) >> 5);
+        if (!wd.tb0) {
+            for (int k = 0; k < wd.k0; k++) {
+                const double a = __ldg(prow + k);
+                const double *brow = B + (uint64_t)k * wd.ldb0 + cbase + lane;
+#pragma unroll
+                for (int j = 0; j < kLanesCols; j++)
+                    if (j < nj && cbase + lane + 32 * j < wd.n0)
+                        acc[j] = fma(a, __ldg(brow + 32 * j), acc[j]);
+            }
+        } else {
+            for (int k = 0; k < wd.k0; k++) {
+                const double a = __ldg(prow + k);
+#pragma unroll
+                for (int j = 0; j < kLanesCols; j++) {
+                    const int c = cbase + lane + 32 * j;
+                    if (j < nj && c < wd.n0)
+                        acc[j] = fma(a, __ldg(B + (uint64_t)c * wd.ldb0 + k), acc[j]);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kLanesCols; j++) {
+            const int c = cbase + lane + 32 * j;
+            if (j < nj && c < wd.n0)
+                wrow[c] = acc[j];
+        }
+    }
+}
+
+// Phase 2: one CTA per task (4 rows x 256 columns of one sigma region), one
+// warp per row, lane -> columns lane + 32 j.  The task owns its cells: it
+// loops over its contribution list (pairs whose row window covers its rows)
+// and adds alpha * sum_k A(r - row0, k) * W_u(k, c - col0) in a fixed order,
+// then writes sigma += scale * acc once (no atomics, deterministic).
+__global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tasks,
+                                                   const int32_t *__restrict__ lists,
+                                                   const Contrib *__restrict__ contribs,
+                                                   const Region *__restrict__ regions,
+                                                   const WorkDesc *__restrict__ works,
+                                                   const double *__restrict__ ops,
+                                                   const double *__restrict__ work,
+                                                   double *__restrict__ sigma, double scale) {
+    const Task2 tk = tasks[blockIdx.x];
+    const Region rg = regions[tk.g];
+    const int lane = threadIdx.x & 31;
+    const int r = tk.rb * 4 + (threadIdx.x >> 5);
+    if (r >= rg.rows)
+        return;
+    double acc[kLanesCols];
+#pragma unroll
+    for (int j = 0; j < kLanesCols; j++)
+        acc[j] = 0.0;
+    for (int64_t li = tk.lb; li < tk.le; li++) {
+        const Contrib c = contribs[lists[li]];
+        const int ar = r - c.row0;
+        if (ar < 0 || ar >= c.m1)
+            continue;  // warp-uniform
+        const double *A = ops + c.a1;
+        const double *W = work + works[c.u].woff;
+        // columns of this lane inside the contribution window
+        int cc[kLanesCols];
+#pragma unroll
+        for (int j = 0; j < kLanesCols; j++) {
+            const int col = tk.col0 + lane + 32 * j - c.col0;
+            cc[j] = (col >= 0 && col < c.n1) ? col : -1;
+        }
+        for (int k = 0; k < c.k1; k++) {
+            const double a = c.alpha * __ldg(c.ta1 ? A + (uint64_t)k * c.lda1 + ar
+                                                    : A + (uint64_t)ar * c.lda1 + k);
+            const double *wrow = W + (uint64_t)k * c.n1;
+#pragma unroll
+            for (int j = 0; j < kLanesCols; j++)
+                if (cc[j] >= 0)
+                    acc[j] = fma(a, __ldg(wrow + cc[j]), acc[j]);
+        }
+    }
+    double *srow = sigma + rg.base + (uint64_t)r * rg.ld;
+#pragma unroll
+    for (int j = 0; j < kLanesCols; j++) {
+        const int col = tk.col0 + lane + 32 * j;
+        if (col < rg.cols)
+            srow[col] += scale * acc[j];
+    }
+}
+
+// FP64 ceiling probe: 8 independent FMA chains per thread, no memory traffic
+__global__ void __launch_bounds__(256) fp64_fma_loop(double *out, int iters, double x, double y) {
+    double a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        a[j] = threadIdx.x * 1e-3 + j;
+    for (int i = 0; i < iters; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            a[j] = fma(a[j], x, y);
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        s += a[j];
+    if (s == 12345.678)  // never true: keeps the loop live
+        out[0] = s;
+}
+
+} // namespace
+
+cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops) {
+    double *out = nullptr;
+    cudaError_t e = cudaMalloc(&out, sizeof(double));
+    if (e != cudaSuccess)
+        return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a), cudaEventCreate(&b);
+    const int blocks = n_sm * 8, iters = 4096;
+    fp64_fma_loop<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);  // warm-up
+    cudaEventRecord(a, s);
+    fp64_fma_loop<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b, s);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * 256 / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(a), cudaEventDestroy(b);
+    cudaFree(out);
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    return e;
+}
+
+cudaError_t launch_fp64_phase1(const DevicePlan &p, const double *ops, const double *psi,
+                               double *work, cudaStream_t s) {
+    if (p.n_t1 == 0)
+        return cudaSuccess;
+    const int64_t blocks = (p.n_t1 + 3) / 4;
+    fp64_phase1<<<(unsigned)blocks, 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi, work);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_phase2(const DevicePlan &p, const double *ops, const double *work,
+                               double *sigma, double scale, cudaStream_t s) {
+    if (p.n_t2 == 0)
+        return cudaSuccess;
+    fp64_phase2<<<(unsigned)p.n_t2, 128, 0, s>>>(p.t2, p.lists, p.contribs, p.regions, p.works, ops,
+                                                 work, sigma, scale);
+    return cudaGetLastError();
+}
+
+} // namespace b2g

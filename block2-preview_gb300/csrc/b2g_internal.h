@@ -1,0 +1,107 @@
+// Internal types of the GB300 DMRG hot-path library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/b2g.h"
+
+namespace b2g {
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+
+#define B2G_CUDA_TRY(expr)                                                                  \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess)                                                              \
+            return ::b2g::fail(B2G_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Device plan of one H_eff (built once per site from the recorded pairs).
+//
+// Phase 1 (GEMM0, de-duplicated): distinct products W_u = psi[a0:] * op(ops[b0:])
+//   are computed once each into the work buffer; one warp per row of W_u.
+// Phase 2 (GEMM1, atomic-free): sigma is partitioned into disjoint regions
+//   (the sigma blocks the pairs write); each region is cut into tasks of
+//   4 rows x up to 256 columns, each task owns its cells and loops over the
+//   list of pair contributions alpha * op(A1) * W_u that overlap its rows.
+// ---------------------------------------------------------------------------
+struct WorkDesc {       // one distinct GEMM0 product
+    uint64_t a0, b0, woff;
+    int32_t m0, n0, k0, lda0, ldb0, tb0;
+};
+struct Contrib {        // one GEMM1 contribution (one recorded pair)
+    uint64_t a1;        // operator offset
+    double alpha;       // alpha0 * alpha1
+    int32_t u;          // work product index
+    int32_t row0, col0; // placement inside the region
+    int32_t m1, n1, k1, lda1, ta1;
+};
+struct Region {
+    uint64_t base;      // sigma offset of (0, 0)
+    int32_t ld, rows, cols, pad;
+};
+struct Task1 {          // phase 1: one row of one work product
+    int32_t u, r;
+};
+struct Task2 {          // phase 2: rows [4*rb, 4*rb+4) x cols [col0, col0+256) of a region
+    int32_t g, rb, col0, pad;
+    int64_t lb, le;     // contribution list range
+};
+
+struct HostPlan {
+    std::vector<WorkDesc> works;
+    std::vector<Contrib> contribs;
+    std::vector<Region> regions;
+    std::vector<Task1> t1;
+    std::vector<Task2> t2;
+    std::vector<int32_t> lists;
+    uint64_t work_size = 0;
+    double mnk = 0, mnk_exec = 0;
+};
+
+int build_plan(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size, uint64_t sigma_size,
+               HostPlan &plan);
+
+struct DevicePlan {
+    WorkDesc *works = nullptr;
+    Contrib *contribs = nullptr;
+    Region *regions = nullptr;
+    Task1 *t1 = nullptr;
+    Task2 *t2 = nullptr;
+    int32_t *lists = nullptr;
+    int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
+};
+
+// FP64 launchers (b2g_fp64.cu)
+cudaError_t launch_fp64_phase1(const DevicePlan &p, const double *ops, const double *psi,
+                               double *work, cudaStream_t s);
+cudaError_t launch_fp64_phase2(const DevicePlan &p, const double *ops, const double *work,
+                               double *sigma, double scale, cudaStream_t s);
+// compute-ceiling probe: TFLOP/s of a register-resident FP64 FMA loop
+cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops);
+
+} // namespace b2g
+
+struct b2g_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int n_sm = 0;
+};
+
+struct b2g_heff {
+    b2g_context *ctx = nullptr;
+    b2g::DevicePlan plan;
+    double *ops = nullptr;
+    double *work = nullptr;
+    double *psi_stage = nullptr, *sigma_stage = nullptr; // device staging for the host entry
+    uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;
+    b2g_heff_stats stats{};
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};

@@ -1,0 +1,162 @@
+/*
+ * b2g.h -- C ABI of the GB300 (sm_103a) two-site DMRG hot path.
+ *
+ * The library replaces, behind block2's own C++ API, the part of a two-site
+ * DMRG sweep where the time goes: the block-sparse effective-Hamiltonian
+ * product H_eff*psi replayed every Davidson iteration, the Davidson
+ * eigensolver around it.
+ *
+ * Boundary (reference interfaces each entry point replaces):
+ *   b2g_heff_create   <- EffectiveHamiltonian::precompute, which records the
+ *                        GEMM pairs of one H_eff*psi into BatchGEMMSeq
+ *                        (src/dmrg/effective_hamiltonian.hpp:226-246,
+ *                         src/core/batch_gemm.hpp:893-902 rotate,
+ *                         src/core/batch_gemm.hpp:952-1065 three_rotate)
+ *   b2g_heff_apply    <- BatchGEMMSeq::operator()(c, v, scale) in Tasked mode
+ *                        (src/core/batch_gemm.hpp:1570-1690), reached through
+ *                        TensorFunctions::operator() (src/core/tensor_functions.hpp:59-62)
+ *   b2g_heff_apply_host  same, with host buffers (H2D psi, D2H sigma inside)
+ *   b2g_heff_destroy  <- EffectiveHamiltonian::post_precompute / deallocate
+ *                        (src/dmrg/effective_hamiltonian.hpp:247-253)
+ *   b2g_davidson      <- IterativeMatrixFunctions::davidson, Normal type,
+ *                        Olsen preconditioner
+ *                        (src/core/iterative_matrix_functions.hpp:864-1173, 93-108)
+ *                        as called by EffectiveHamiltonian::eigs
+ *                        (src/dmrg/effective_hamiltonian.hpp:481-568)
+ *
+ * Conventions: row-major matrices (as GMatrix, src/core/matrix.hpp:94-106);
+ * offsets and sizes count doubles; every function returns 0 on success and a
+ * B2G_ERR_* code otherwise, with a message in b2g_last_error() (the C++ shim
+ * turns a non-zero status into std::runtime_error, the reference's error
+ * convention).  No torch or C++ types cross this boundary.
+ */
+#ifndef B2G_H
+#define B2G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define B2G_OK 0
+#define B2G_ERR_ARG 1          /* invalid argument / inconsistent sequence */
+#define B2G_ERR_CUDA 2         /* CUDA runtime error */
+#define B2G_ERR_NOMEM 3        /* device allocation failed */
+#define B2G_ERR_UNSUPPORTED 4  /* sequence shape the plan builder cannot take */
+#define B2G_ERR_NOT_CONVERGED 5/* Davidson reached max_iter */
+#define B2G_ERR_STATE 6        /* wrong call order / destroyed object */
+
+/* arithmetic forms of H_eff*psi */
+#define B2G_FP64 0             /* plain FP64 (CUDA-core DFMA) */
+#define B2G_TF32X3 1           /* split-TF32 x3 on tcgen05 tensor cores, FP32 accumulate */
+
+/*
+ * The recorded GEMM-pair sequence of one H_eff*psi: BatchGEMMSeq::batch[0]
+ * (GEMM0) and batch[1] (GEMM1) after EffectiveHamiltonian::precompute, one
+ * entry per pair, struct-of-arrays, with every pointer replaced by an offset:
+ * a0 into psi (precompute sets cmat->data = 0), b0/a1 into the packed operator
+ * blob, c1 into sigma (vmat->data = 0).  Pair i computes
+ *
+ *   W  = alpha0[i] * psi[a0:](m0 x k0, ld lda0) * op_b0(ops[b0:])(k0 x n0, ld ldb0)
+ *   sigma[c1:](m1 x n1, ld ldc1) += scale * alpha1[i] * op_a1(ops[a1:])(m1 x k1, ld lda1) * W
+ *
+ * with op_b0 = transpose when tb0[i] != 0, op_a1 = transpose when ta1[i] != 0,
+ * and k1 == m0, n1 == n0 (W is the per-pair work matrix of
+ * AdvancedGEMM::rotate, src/core/batch_gemm.hpp:564-575).
+ */
+typedef struct {
+    int64_t n_pairs;
+    const int32_t *tb0, *m0, *n0, *k0, *lda0, *ldb0;
+    const int32_t *ta1, *m1, *n1, *k1, *lda1, *ldc1;
+    const double *alpha0, *alpha1;
+    const uint64_t *a0, *b0, *a1, *c1;
+} b2g_pair_seq;
+
+typedef struct b2g_context b2g_context;
+typedef struct b2g_heff b2g_heff;
+
+typedef struct {
+    int64_t n_pairs;        /* recorded pairs */
+    int64_t n_work;         /* distinct GEMM0 products after de-duplication */
+    int64_t n_regions;      /* disjoint sigma regions (atomic-free owners) */
+    int64_t n_tiles;        /* GEMM1 output tiles launched per apply */
+    double mnk;             /* reference multiply-add count: sum m0 n0 k0 + m1 n1 k1 */
+    double mnk_executed;    /* multiply-adds the plan executes (after de-duplication) */
+    uint64_t ops_bytes;     /* operator blob bytes resident in HBM */
+    uint64_t work_bytes;    /* GEMM0 work buffer bytes */
+    uint64_t plan_bytes;    /* schedule tables bytes */
+    uint64_t psi_size, sigma_size;
+} b2g_heff_stats;
+
+/* version and error reporting */
+int b2g_version(void);
+const char *b2g_last_error(void);
+
+/* one context per device (the device is made current by every call) */
+int b2g_context_create(int device, b2g_context **out);
+int b2g_context_destroy(b2g_context *ctx);
+/* the CUDA stream the context launches on (cudaStream_t), for callers that sync/overlap */
+void *b2g_context_stream(b2g_context *ctx);
+int b2g_context_synchronize(b2g_context *ctx);
+
+/*
+ * Build the device plan of one H_eff from its recorded pair sequence and
+ * upload the operator blob (ops_size doubles; host memory when
+ * ops_on_device == 0, else a device pointer that is copied).
+ */
+int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops,
+                    uint64_t ops_size, int ops_on_device, uint64_t psi_size,
+                    uint64_t sigma_size, b2g_heff **out);
+int b2g_heff_destroy(b2g_heff *h);
+int b2g_heff_stats_get(const b2g_heff *h, b2g_heff_stats *out);
+/* Host-only dry run of the plan builder (no device touched): validates the
+ * sequence against the sizes and reports the schedule statistics. */
+int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size,
+                   uint64_t sigma_size, b2g_heff_stats *out);
+
+/* sigma += scale * H_eff * psi; psi and sigma are DEVICE pointers (sizes as created),
+ * form = B2G_FP64 or B2G_TF32X3.  Asynchronous on the context stream. */
+int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form);
+/* same with HOST psi/sigma: copies psi in, applies, copies sigma out, synchronizes. */
+int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double scale, int form);
+
+/* Per-kernel timing of b2g_heff_apply (CUDA events recorded on the context
+ * stream around each phase when enabled; no work is skipped).  ms[0] =
+ * GEMM0 phase, ms[1] = GEMM1 phase of the most recent apply (synchronizes). */
+int b2g_heff_set_timing(b2g_heff *h, int enable);
+int b2g_heff_last_timing(b2g_heff *h, float *ms);
+
+/* Measured compute ceiling of one arithmetic form on this device (a
+ * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as
+ * the roofline denominator where no measured peak exists (FP64). */
+int b2g_probe_peak(b2g_context *ctx, int form, double *tflops);
+
+/*
+ * Davidson for the lowest eigenpair of H_eff (one root), the reference's
+ * Normal Davidson with Olsen preconditioning and thick restart to
+ * def_min vectors when def_max is reached.  diag: diag(H_eff) (host),
+ * psi: initial guess in, converged eigenvector out (host).  Convergence on
+ * |r|^2 < conv_thrd.  form selects the arithmetic of the H_eff products; with
+ * B2G_TF32X3 every residual is recomputed with an FP64 product (defect
+ * correction).  Outputs: energy (eigenvalue, without const_e), iterations,
+ * number of H_eff products by form.
+ */
+typedef struct {
+    double energy;
+    int32_t n_iter;
+    int32_t n_apply_fp64;
+    int32_t n_apply_mixed;
+    double residual_norm2;
+} b2g_davidson_result;
+
+int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double conv_thrd,
+                 int max_iter, int def_min, int def_max, int form,
+                 b2g_davidson_result *res);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* B2G_H */

@@ -1,0 +1,101 @@
+"""Python access to the C restatement in b2g_oracle.c -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+legs, always as the checker or the timed CPU reference, never as the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "libb2g_oracle.so")
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "block2-preview_gb300"))
+
+from b2g.capi import PairSeq, PairSeqC  # noqa: E402  (the boundary's plain-data struct)
+
+_lib = None
+
+
+def build():
+    src = os.path.join(HERE, "b2g_oracle.c")
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["bash", os.path.join(HERE, "build.sh")], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.b2g_oracle_load_blas.argtypes = [C.c_char_p, C.c_char_p]
+        L.b2g_oracle_load_blas.restype = C.c_int
+        L.b2g_oracle_blas_loaded.restype = C.c_int
+        L.b2g_oracle_replay.argtypes = [C.POINTER(PairSeqC), C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_uint64, C.c_double, C.c_int]
+        L.b2g_oracle_replay.restype = C.c_int
+        L.b2g_oracle_syev.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.b2g_oracle_davidson.argtypes = [C.POINTER(PairSeqC), C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        L.b2g_oracle_davidson.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def find_blas():
+    """Path of scipy's bundled OpenBLAS (symbols prefixed scipy_), or None."""
+    try:
+        import scipy
+    except ImportError:
+        return None
+    d = os.path.join(os.path.dirname(scipy.__file__), os.pardir, "scipy.libs")
+    c = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+    return os.path.abspath(c[0]) if c else None
+
+
+def load_blas() -> bool:
+    if lib().b2g_oracle_blas_loaded():
+        return True
+    p = find_blas()
+    if p is None:
+        return False
+    return lib().b2g_oracle_load_blas(p.encode(), b"scipy_") == 0
+
+
+def replay(seq: PairSeq, ops, psi, sigma_size, scale=1.0, nthreads=1, sigma=None):
+    ops = np.ascontiguousarray(ops, dtype=np.float64)
+    psi = np.ascontiguousarray(psi, dtype=np.float64)
+    out = np.zeros(sigma_size) if sigma is None else sigma
+    rc = lib().b2g_oracle_replay(C.byref(seq.c), ops.ctypes.data, psi.ctypes.data, out.ctypes.data,
+                                 sigma_size, scale, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle replay failed")
+    return out
+
+
+def syev(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    m = a.shape[0]
+    w = np.zeros(m)
+    v = np.zeros((m, m))
+    lib().b2g_oracle_syev(m, a.ctypes.data, w.ctypes.data, v.ctypes.data)
+    return w, v
+
+
+def davidson(seq: PairSeq, ops, diag, psi0, conv_thrd, max_iter=500, def_min=2, def_max=50, nthreads=1):
+    psi = np.array(psi0, dtype=np.float64, copy=True)
+    e = C.c_double()
+    it = C.c_int()
+    ops = np.ascontiguousarray(ops, dtype=np.float64)
+    diag = np.ascontiguousarray(diag, dtype=np.float64)
+    rc = lib().b2g_oracle_davidson(C.byref(seq.c), ops.ctypes.data, diag.ctypes.data, psi.ctypes.data,
+                                   psi.size, conv_thrd, max_iter, def_min, def_max, nthreads,
+                                   C.byref(e), C.byref(it))
+    return e.value, it.value, psi, rc

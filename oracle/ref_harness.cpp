@@ -1,0 +1,396 @@
+// ref_harness.cpp -- TEST INFRASTRUCTURE ONLY (never shipped, never measured).
+//
+// Drives the reference's own CPU implementation of two-site DMRG (block2,
+// header-only build against the reference's src/ directory, not vendored) and
+// writes, for selected sites of selected sweeps, everything the GPU hot path
+// must reproduce:
+//
+//   * the recorded GEMM-pair sequence of H_eff*psi, exactly as
+//     EffectiveHamiltonian::precompute (src/dmrg/effective_hamiltonian.hpp:226-246)
+//     leaves it in BatchGEMMSeq::batch[0] / batch[1]
+//     (src/core/batch_gemm.hpp:847-1707), with every operator pointer
+//     translated into an offset of a packed operator blob;
+//   * the packed operator blob itself (all L/R block data those pairs read);
+//   * psi (the two-site wavefunction entering Davidson), sigma = H_eff*psi
+//     computed by the reference's Tasked replay (batch_gemm.hpp:1613-1689),
+//     diag(H_eff) (effective_hamiltonian.hpp:172-182);
+//   * after Davidson: the converged psi and its energy;
+//   * per sweep: energies, discarded weights, bond dimensions.
+//
+// Output: one directory per dumped site, holding raw little-endian arrays and
+// a manifest.txt ("name dtype count" lines, "#key value" scalars).
+// Build recipe: oracle/build_ref.sh. Fixture conversion: tests/golden/make_fixtures.py.
+
+#include "block2_core.hpp"
+#include "block2_dmrg.hpp"
+#include <sys/stat.h>
+
+using namespace block2;
+
+namespace harness {
+
+struct Opts {
+    string ham = "hubbard";   // "hubbard" or a FCIDUMP path
+    int L = 8;                // hubbard sites
+    double t = 1.0, U = 4.0;  // hubbard parameters
+    string sym = "su2";       // su2 | sz
+    int M = 100, nsweeps = 4, nthreads = 4, seed = 0;
+    vector<double> noises = {0.0};
+    vector<double> dav_thrds = {1e-10};
+    double tol = 0.0;
+    string out = "/tmp/b2g_dump";
+    int dump_sweep = 0;       // -1: all sweeps
+    int dump_site = -1;       // -1: middle site (n/2-1); -2: all sites
+    bool with_data = true;    // false: structure only (no operator blob)
+    bool dump_dm = true;      // density-matrix / split data after Davidson
+};
+
+static void mkdirs(const string &p) {
+    string cur;
+    for (size_t i = 0; i < p.size(); i++) {
+        cur.push_back(p[i]);
+        if (p[i] == '/' || i + 1 == p.size())
+            mkdir(cur.c_str(), 0755);
+    }
+}
+
+struct Writer {
+    string dir;
+    ofstream man;
+    explicit Writer(const string &d) : dir(d) {
+        mkdirs(d);
+        man.open(d + "/manifest.txt");
+        man << setprecision(17);
+    }
+    template <typename T>
+    void arr(const string &name, const T *p, size_t n, const char *dtype) {
+        ofstream f(dir + "/" + name + ".bin", ios::binary);
+        f.write((const char *)p, sizeof(T) * n);
+        man << name << " " << dtype << " " << n << "\n";
+    }
+    template <typename T>
+    void vec(const string &name, const vector<T> &v, const char *dtype) {
+        arr(name, v.data(), v.size(), dtype);
+    }
+    void scalar(const string &name, double v) { man << "#" << name << " " << v << "\n"; }
+};
+
+// one contiguous operator data region (SparseMatrix::data, total_memory)
+struct Region {
+    const double *p;
+    size_t n;
+    size_t blob_off = 0;
+    bool used = false;
+};
+
+template <typename S> struct Dumper : CallbackKernel {
+    typedef DMRG<S, double, double> DMRGT;
+    DMRGT *d = nullptr;
+    Opts o;
+    mutable vector<Region> regions;
+
+    bool selected() const {
+        if (o.dump_sweep != -1 && d->isweep != o.dump_sweep)
+            return false;
+        int site = d->me->center;
+        if (o.dump_site == -2)
+            return true;
+        int want = o.dump_site == -1 ? d->me->n_sites / 2 - 1 : o.dump_site;
+        return site == want;
+    }
+    string site_dir() const {
+        stringstream ss;
+        ss << o.out << "/sweep" << d->isweep << "_site" << d->me->center;
+        return ss.str();
+    }
+    static void add_tensor(vector<Region> &r,
+                           const shared_ptr<OperatorTensor<S, double>> &t) {
+        if (t == nullptr)
+            return;
+        for (auto &kv : t->ops)
+            if (kv.second != nullptr && kv.second->data != nullptr &&
+                kv.second->total_memory != 0)
+                r.push_back(Region{kv.second->data, kv.second->total_memory});
+        if (t->get_type() == OperatorTensorTypes::Delayed) {
+            auto dt = dynamic_pointer_cast<DelayedOperatorTensor<S, double>>(t);
+            add_tensor(r, dt->lopt);
+            add_tensor(r, dt->ropt);
+        }
+    }
+    void collect_regions(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        regions.clear();
+        add_tensor(regions, h->op->lopt);
+        add_tensor(regions, h->op->ropt);
+        sort(regions.begin(), regions.end(),
+             [](const Region &a, const Region &b) { return a.p < b.p; });
+        vector<Region> u;
+        for (auto &r : regions)
+            if (u.empty() || r.p != u.back().p)
+                u.push_back(r);
+            else
+                u.back().n = max(u.back().n, r.n);
+        regions = u;
+    }
+    // extent (in doubles) of an operand op(X) of shape rows x cols, leading dim ld
+    static size_t extent(bool trans, int rows, int cols, int ld) {
+        if (rows == 0 || cols == 0)
+            return 0;
+        return trans ? (size_t)(cols - 1) * ld + rows : (size_t)(rows - 1) * ld + cols;
+    }
+    long find_region(const double *p, size_t ext) const {
+        auto it = upper_bound(regions.begin(), regions.end(), p,
+                              [](const double *x, const Region &r) { return x < r.p; });
+        if (it == regions.begin())
+            return -1;
+        --it;
+        if (p >= it->p && p + ext <= it->p + it->n)
+            return it - regions.begin();
+        return -1;
+    }
+
+    void dump_pre(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        Writer w(site_dir());
+        const size_t nket = h->ket->total_memory, nbra = h->bra->total_memory;
+        collect_regions(h);
+        h->precompute();
+        auto seq = h->tf->opf->seq;
+        auto b0 = seq->batch[0], b1 = seq->batch[1];
+        if (!b0->acidxs.empty() || b0->c.size() != b0->gp.size() ||
+            b1->c.size() != b1->gp.size() || b0->c.size() != b1->c.size())
+            throw runtime_error("harness: recorded sequence is not a plain pair list");
+        const size_t np = b0->c.size();
+        const double *zero = (const double *)0;
+        vector<int32_t> ta0(np), tb0(np), m0(np), n0(np), k0(np), lda0(np), ldb0(np);
+        vector<int32_t> ta1(np), tb1(np), m1(np), n1(np), k1(np), lda1(np), ldb1(np), ldc1(np);
+        vector<double> al0(np), be0(np), al1(np), be1(np);
+        vector<uint64_t> a0(np), b0off(np), w0(np), a1(np), w1(np), c1(np);
+        vector<int64_t> rb0(np), ra1(np);
+        for (size_t i = 0; i < np; i++) {
+            ta0[i] = b0->ta[i] != CblasNoTrans, tb0[i] = b0->tb[i] != CblasNoTrans;
+            m0[i] = b0->m[i], n0[i] = b0->n[i], k0[i] = b0->k[i];
+            lda0[i] = b0->lda[i], ldb0[i] = b0->ldb[i];
+            al0[i] = b0->alpha[i], be0[i] = b0->beta[i];
+            ta1[i] = b1->ta[i] != CblasNoTrans, tb1[i] = b1->tb[i] != CblasNoTrans;
+            m1[i] = b1->m[i], n1[i] = b1->n[i], k1[i] = b1->k[i];
+            lda1[i] = b1->lda[i], ldb1[i] = b1->ldb[i], ldc1[i] = b1->ldc[i];
+            al1[i] = b1->alpha[i], be1[i] = b1->beta[i];
+            if (b0->ldc[i] != b0->n[i] || ldb1[i] != n1[i] || tb1[i] != 0 || ta0[i] != 0)
+                throw runtime_error("harness: unexpected work layout");
+            a0[i] = (uint64_t)(b0->a[i] - zero);
+            w0[i] = (uint64_t)(b0->c[i] - zero);
+            w1[i] = (uint64_t)(b1->b[i] - zero);
+            c1[i] = (uint64_t)(b1->c[i] - zero);
+            if (w0[i] != w1[i])
+                throw runtime_error("harness: work offsets differ within a pair");
+            if (a0[i] + extent(false, m0[i], k0[i], lda0[i]) > nket)
+                throw runtime_error("harness: psi operand out of range");
+            if (c1[i] + extent(false, m1[i], n1[i], ldc1[i]) > nbra)
+                throw runtime_error("harness: sigma operand out of range");
+            rb0[i] = find_region(b0->b[i], extent(tb0[i], k0[i], n0[i], ldb0[i]));
+            ra1[i] = find_region(b1->a[i], extent(ta1[i], m1[i], k1[i], lda1[i]));
+            if (rb0[i] < 0 || ra1[i] < 0)
+                throw runtime_error("harness: operator pointer outside the H_eff operators");
+            regions[rb0[i]].used = regions[ra1[i]].used = true;
+        }
+        size_t blob = 0;
+        for (auto &r : regions)
+            if (r.used)
+                r.blob_off = blob, blob += r.n;
+        for (size_t i = 0; i < np; i++) {
+            b0off[i] = regions[rb0[i]].blob_off + (b0->b[i] - regions[rb0[i]].p);
+            a1[i] = regions[ra1[i]].blob_off + (b1->a[i] - regions[ra1[i]].p);
+        }
+        // sigma = H_eff * psi through the reference's own Tasked replay
+        vector<double> psi(h->ket->data, h->ket->data + nket), sigma(nbra, 0.0);
+        h->tf->operator()(GMatrix<double>(psi.data(), (MKL_INT)nket, 1),
+                          GMatrix<double>(sigma.data(), (MKL_INT)nbra, 1), 1.0);
+        size_t nflop = 0;
+        for (size_t i = 0; i < np; i++)
+            nflop += (size_t)m0[i] * n0[i] * k0[i] + (size_t)m1[i] * n1[i] * k1[i];
+        h->post_precompute();
+        w.scalar("n_pairs", (double)np);
+        w.scalar("psi_size", (double)nket);
+        w.scalar("sigma_size", (double)nbra);
+        w.scalar("ops_size", (double)blob);
+        w.scalar("mnk", (double)nflop);
+        w.scalar("const_e", (double)d->me->mpo->const_e);
+        w.scalar("isweep", d->isweep);
+        w.scalar("site", d->me->center);
+        w.scalar("n_sites", d->me->n_sites);
+        w.scalar("forward", d->forward);
+        w.scalar("conv_thrd", d->davidson_conv_thrds[min((size_t)d->isweep, d->davidson_conv_thrds.size() - 1)]);
+        w.scalar("def_min", d->davidson_def_min_size);
+        w.scalar("def_max", d->davidson_def_max_size);
+        w.vec("ta0", ta0, "i4"), w.vec("tb0", tb0, "i4"), w.vec("m0", m0, "i4");
+        w.vec("n0", n0, "i4"), w.vec("k0", k0, "i4"), w.vec("lda0", lda0, "i4");
+        w.vec("ldb0", ldb0, "i4"), w.vec("alpha0", al0, "f8"), w.vec("beta0", be0, "f8");
+        w.vec("ta1", ta1, "i4"), w.vec("tb1", tb1, "i4"), w.vec("m1", m1, "i4");
+        w.vec("n1", n1, "i4"), w.vec("k1", k1, "i4"), w.vec("lda1", lda1, "i4");
+        w.vec("ldb1", ldb1, "i4"), w.vec("ldc1", ldc1, "i4"), w.vec("alpha1", al1, "f8");
+        w.vec("beta1", be1, "f8");
+        w.vec("a0", a0, "u8"), w.vec("b0", b0off, "u8"), w.vec("w0", w0, "u8");
+        w.vec("a1", a1, "u8"), w.vec("c1", c1, "u8");
+        w.vec("psi", psi, "f8");
+        w.vec("sigma", sigma, "f8");
+        w.arr("diag", h->diag->data, h->diag->total_memory, "f8");
+        // block structure of psi (= sigma for the ground state): quanta offsets and shapes
+        {
+            auto info = h->ket->info;
+            vector<int32_t> rows(info->n), cols(info->n);
+            vector<uint64_t> shifts(info->n);
+            for (int i = 0; i < info->n; i++)
+                rows[i] = info->n_states_bra[i], cols[i] = info->n_states_ket[i],
+                shifts[i] = info->block_shifts[i];
+            w.vec("psi_block_rows", rows, "i4");
+            w.vec("psi_block_cols", cols, "i4");
+            w.vec("psi_block_shift", shifts, "u8");
+        }
+        if (o.with_data) {
+            vector<double> ops(blob);
+            for (auto &r : regions)
+                if (r.used)
+                    memcpy(ops.data() + r.blob_off, r.p, sizeof(double) * r.n);
+            w.vec("ops", ops, "f8");
+        }
+        w.man.flush();
+    }
+    void dump_post(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        Writer w(site_dir() + "/post");
+        const size_t nket = h->ket->total_memory, nbra = h->bra->total_memory;
+        vector<double> psi(h->ket->data, h->ket->data + nket), sigma(nbra, 0.0);
+        h->precompute();
+        h->tf->operator()(GMatrix<double>(psi.data(), (MKL_INT)nket, 1),
+                          GMatrix<double>(sigma.data(), (MKL_INT)nbra, 1), 1.0);
+        h->post_precompute();
+        double e = 0, nn = 0;
+        for (size_t i = 0; i < nket; i++)
+            e += psi[i] * sigma[i], nn += psi[i] * psi[i];
+        w.scalar("energy", e / nn + (double)d->me->mpo->const_e);
+        w.scalar("norm2", nn);
+        w.vec("psi", psi, "f8");
+        w.man.flush();
+    }
+    void compute(const string &name, int iprint) const override {
+        if (d == nullptr || d->current_eff_ham == nullptr || !selected())
+            return;
+        if (name == "DMRG::sweep::iter.eff_ham")
+            dump_pre(d->current_eff_ham);
+        else if (name == "DMRG::sweep::iter.eff_ham.end")
+            dump_post(d->current_eff_ham);
+    }
+};
+
+template <typename S> int run(const Opts &o) {
+    typedef double FL;
+    Random::rand_seed(o.seed);
+    string scratch = o.out + "/_scratch";
+    mkdirs(scratch);
+    frame_<FL>() = make_shared<DataFrame<FL>>((size_t)1 << 26, (size_t)1 << 32, scratch);
+    frame_<FL>()->use_main_stack = false;
+    frame_<FL>()->minimal_disk_usage = true;
+    threading_() = make_shared<Threading>(
+        ThreadingTypes::OperatorBatchedGEMM | ThreadingTypes::Global, o.nthreads, o.nthreads, 1);
+    threading_()->seq_type = SeqTypes::Tasked;
+    shared_ptr<FCIDUMP<FL>> fcidump;
+    if (o.ham == "hubbard")
+        fcidump = make_shared<HubbardFCIDUMP>(o.L, o.t, o.U);
+    else {
+        fcidump = make_shared<FCIDUMP<FL>>();
+        fcidump->read(o.ham);
+    }
+    const int n = fcidump->n_sites();
+    vector<uint8_t> orbsym(n, 0); // no point-group symmetry in these Hamiltonians
+    S vacuum(0);
+    S target(fcidump->n_elec(), fcidump->twos(), 0);
+    auto hamil = make_shared<HamiltonianQC<S, FL>>(vacuum, n, orbsym, fcidump);
+    shared_ptr<MPO<S, FL>> mpo = make_shared<MPOQC<S, FL>>(hamil, QCTypes::Conventional, "HQC");
+    mpo = make_shared<SimplifiedMPO<S, FL>>(mpo, make_shared<RuleQC<S, FL>>(), true, true,
+                                            OpNamesSet({OpNames::R, OpNames::RD}));
+    auto mps_info = make_shared<MPSInfo<S>>(n, vacuum, target, hamil->basis);
+    mps_info->set_bond_dimension(o.M);
+    auto mps = make_shared<MPS<S, FL>>(n, 0, 2);
+    mps->initialize(mps_info);
+    mps->random_canonicalize();
+    mps->save_mutable();
+    mps->deallocate();
+    mps_info->save_mutable();
+    mps_info->deallocate_mutable();
+    auto me = make_shared<MovingEnvironment<S, FL, FL>>(mpo, mps, mps, "DMRG");
+    me->init_environments(false);
+    me->delayed_contraction = OpNamesSet::normal_ops();
+    me->cached_contraction = true;
+    vector<ubond_t> bdims = {(ubond_t)o.M};
+    auto dmrg = make_shared<DMRG<S, FL, FL>>(me, bdims, o.noises);
+    dmrg->davidson_conv_thrds = o.dav_thrds;
+    dmrg->noise_type = NoiseTypes::DensityMatrix;
+    dmrg->iprint = 2;
+    auto dumper = make_shared<Dumper<S>>();
+    dumper->d = dmrg.get();
+    dumper->o = o;
+    callback_() = dumper;
+    Timer t;
+    t.get_time();
+    double e = dmrg->solve(o.nsweeps, true, o.tol);
+    double tt = t.get_time();
+    callback_() = make_shared<CallbackKernel>();
+    Writer w(o.out + "/result");
+    w.scalar("energy", e);
+    w.scalar("time", tt);
+    w.scalar("n_sites", n);
+    vector<double> es, dws;
+    for (auto &x : dmrg->energies)
+        es.push_back(x.back());
+    for (auto &x : dmrg->discarded_weights)
+        dws.push_back(x);
+    w.vec("sweep_energies", es, "f8");
+    w.vec("discarded_weights", dws, "f8");
+    cout << setprecision(12) << "FINAL E = " << e << " T = " << tt << endl;
+    mps_info->deallocate();
+    mpo->deallocate();
+    me->remove_partition_files();
+    return 0;
+}
+
+static vector<double> parse_list(const string &s) {
+    vector<double> r;
+    stringstream ss(s);
+    string x;
+    while (getline(ss, x, ','))
+        r.push_back(atof(x.c_str()));
+    return r;
+}
+
+} // namespace harness
+
+int main(int argc, char **argv) {
+    harness::Opts o;
+    for (int i = 1; i + 1 < argc; i += 2) {
+        string k = argv[i], v = argv[i + 1];
+        if (k == "--ham") o.ham = v;
+        else if (k == "--L") o.L = atoi(v.c_str());
+        else if (k == "--t") o.t = atof(v.c_str());
+        else if (k == "--U") o.U = atof(v.c_str());
+        else if (k == "--sym") o.sym = v;
+        else if (k == "--M") o.M = atoi(v.c_str());
+        else if (k == "--sweeps") o.nsweeps = atoi(v.c_str());
+        else if (k == "--threads") o.nthreads = atoi(v.c_str());
+        else if (k == "--seed") o.seed = atoi(v.c_str());
+        else if (k == "--noises") o.noises = harness::parse_list(v);
+        else if (k == "--dav") o.dav_thrds = harness::parse_list(v);
+        else if (k == "--tol") o.tol = atof(v.c_str());
+        else if (k == "--out") o.out = v;
+        else if (k == "--dump-sweep") o.dump_sweep = atoi(v.c_str());
+        else if (k == "--dump-site") o.dump_site = atoi(v.c_str());
+        else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
+        else {
+            cerr << "unknown option " << k << endl;
+            return 2;
+        }
+    }
+    if (o.sym == "su2")
+        return harness::run<SU2>(o);
+    else if (o.sym == "sz")
+        return harness::run<SZ>(o);
+    cerr << "unknown symmetry " << o.sym << endl;
+    return 2;
+}

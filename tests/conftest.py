@@ -1,0 +1,28 @@
+import glob
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "block2-preview_gb300"))
+sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def fixture_paths():
+    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def fixture_ids():
+    return [os.path.basename(p)[:-4] for p in fixture_paths()]
+
+
+@pytest.fixture(scope="session")
+def problems():
+    from b2g.problem import load_problem
+    return {os.path.basename(p)[:-4]: load_problem(p) for p in fixture_paths()}
