@@ -88,9 +88,10 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
     if (r >= rg.rows)
         return;
     double acc[kLanesCols];
+    bool cov[kLanesCols];  // cell written by at least one pair (only those are stored)
 #pragma unroll
     for (int j = 0; j < kLanesCols; j++)
-        acc[j] = 0.0;
+        acc[j] = 0.0, cov[j] = false;
     for (int64_t li = tk.lb; li < tk.le; li++) {
         const Contrib c = contribs[lists[li]];
         const int ar = r - c.row0;
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
         for (int j = 0; j < kLanesCols; j++) {
             const int col = tk.col0 + lane + 32 * j - c.col0;
             cc[j] = (col >= 0 && col < c.n1) ? col : -1;
+            cov[j] = cov[j] || cc[j] >= 0;
         }
         for (int k = 0; k < c.k1; k++) {
             const double a = c.alpha * __ldg(c.ta1 ? A + (uint64_t)k * c.lda1 + ar
@@ -117,11 +119,9 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
     }
     double *srow = sigma + rg.base + (uint64_t)r * rg.ld;
 #pragma unroll
-    for (int j = 0; j < kLanesCols; j++) {
-        const int col = tk.col0 + lane + 32 * j;
-        if (col < rg.cols)
-            srow[col] += scale * acc[j];
-    }
+    for (int j = 0; j < kLanesCols; j++)
+        if (cov[j])
+            srow[tk.col0 + lane + 32 * j] += scale * acc[j];
 }
 
 // FP64 ceiling probe: 8 independent FMA chains per thread, no memory traffic
