@@ -62,9 +62,14 @@ class ClockSampler:
         except (OSError, FileNotFoundError):
             self.proc = None
 
+    def start_time(self):
+        return getattr(self, "_t0", None)
+
     def stop(self):
         if self.proc is None:
             return None
+        # nvidia-smi needs a few sampling periods; short timed regions still get samples
+        time.sleep(0.7)
         self.proc.terminate()
         try:
             out, _ = self.proc.communicate(timeout=5)
