@@ -122,6 +122,24 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
 /* same with HOST psi/sigma: copies psi in, applies, copies sigma out, synchronizes. */
 int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double scale, int form);
 
+/*
+ * sigma += scale * H_eff * psi in plain FP64 without allocating anything.
+ * No counterpart in the reference: this entry point exists for callers that
+ * cannot call cudaMalloc (a program that hands the GPU a fixed memory budget,
+ * or code running where an allocation would synchronize the device or break
+ * its memory accounting).  The caller passes the recorded pair sequence
+ * (host arrays), and DEVICE pointers to the operator blob, psi and sigma;
+ * the work matrices live in a 32 MiB file-scope device array that every GPU
+ * loading this library holds until exit.  A pair whose work matrix exceeds
+ * that array is rejected (B2G_ERR_ARG).  The first call on a device looks
+ * the array's address up and should precede any stream capture on that
+ * device; calls share the array, so calls that overlap on the GPU race.
+ * stream: a cudaStream_t (NULL = legacy default stream).  Asynchronous.
+ */
+int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops, uint64_t ops_size,
+                           const double *psi, uint64_t psi_size, double *sigma,
+                           uint64_t sigma_size, double scale, void *stream);
+
 /* Per-kernel timing of b2g_heff_apply (CUDA events recorded on the context
  * stream around each phase when enabled; no work is skipped).  ms[0] =
  * GEMM0 phase, ms[1] = GEMM1 phase of the most recent apply (synchronizes). */
