@@ -24,6 +24,7 @@ B2G_ERR_STATE = 6
 
 FP64 = 0
 TF32X3 = 1
+FP32 = 2
 
 _i32p = C.POINTER(C.c_int32)
 _u64p = C.POINTER(C.c_uint64)

@@ -18,7 +18,7 @@ import time
 import numpy as np
 
 from . import capi
-from .capi import FP64, TF32X3, B2GError, PairSeq, check, lib
+from .capi import FP32, FP64, TF32X3, B2GError, PairSeq, check, lib
 
 
 class Context:

@@ -160,7 +160,8 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaSetDevice(h->ctx->device);
     cudaStreamSynchronize(h->ctx->stream);
     free_plan(h->plan);
-    cudaFree(h->ops), cudaFree(h->work), cudaFree(h->psi_stage), cudaFree(h->sigma_stage);
+    cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->work);
+    cudaFree(h->psi_stage), cudaFree(h->sigma_stage);
     for (auto &e : h->ev)
         if (e)
             cudaEventDestroy(e);
@@ -242,10 +243,29 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
     if (form == B2G_FP64) {
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-        B2G_CUDA_TRY(launch_fp64_phase1(h->plan, h->ops, psi, h->work, s));
+        B2G_CUDA_TRY(launch_simt_phase1<double>(h->plan, h->ops, psi, h->work, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-        B2G_CUDA_TRY(launch_fp64_phase2(h->plan, h->ops, h->work, sigma, scale, s));
+        B2G_CUDA_TRY(launch_simt_phase2<double>(h->plan, h->ops, h->work, sigma, scale, s));
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+        return B2G_OK;
+    }
+    if (form == B2G_FP32) {
+        if (h->ops32 == nullptr && h->ops_size) {
+            if (cudaMalloc(&h->ops32, sizeof(float) * h->ops_size) != cudaSuccess) {
+                h->ops32 = nullptr;
+                return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the float operator copy");
+            }
+            B2G_CUDA_TRY(launch_to_float(h->ops, h->ops32, h->ops_size, s));
+        }
+        float *w32 = (float *)h->work;
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+        B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, psi, w32, s));
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+        B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, scale, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;

@@ -289,8 +289,8 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
         def_max = def_min + 1;
     if (def_max > kMaxSub)
         return fail(B2G_ERR_ARG, "b2g_davidson: def_max above 64");
-    if (form != B2G_FP64)
-        return fail(B2G_ERR_UNSUPPORTED, "b2g_davidson: form not available");
+    if (form != B2G_FP64 && form != B2G_FP32 && form != B2G_TF32X3)
+        return fail(B2G_ERR_UNSUPPORTED, "b2g_davidson: unknown form");
     B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
     cudaStream_t st = h->ctx->stream;
     const uint64_t n = h->psi_size;
@@ -337,18 +337,19 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
         DAV_TRY(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st));
         dot_many(q, 1, q, sc + 1);
         normalize_into<<<g, 256, 0, st>>>(B, q, sc + 1, n);
-        int m = 1, msig = 0, xiter = 0, n_apply = 0;
+        int m = 1, msig = 0, xiter = 0, n_fp64 = 0, n_mixed = 0, n_refine = 0, since_refine = 0;
         double lam = 0.0, qq = 0.0;
-        bool converged = false;
+        bool converged = false, have_exact = false;
         while (xiter < max_iter) {
             xiter++;
+            since_refine++;
             for (int i = msig; i < m; i++, msig++) {
                 double *si = S + (uint64_t)i * n;
                 DAV_TRY(cudaMemsetAsync(si, 0, sizeof(double) * n, st));
-                rc = b2g_heff_apply(h, B + (uint64_t)i * n, si, 1.0, B2G_FP64);
+                rc = b2g_heff_apply(h, B + (uint64_t)i * n, si, 1.0, form);
                 if (rc != B2G_OK)
                     goto done;
-                n_apply++;
+                (form == B2G_FP64 ? n_fp64 : n_mixed)++;
                 // A(i, j) = <b_i | sigma_j>, j <= i
                 dot_many(S, i + 1, B + (uint64_t)i * n, dots);
                 set_sub_row<<<1, kMaxSub, 0, st>>>(A, kMaxSub, i, dots);
@@ -362,9 +363,47 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
             DAV_TRY(cudaMemcpyAsync(&lam, w, sizeof(double), cudaMemcpyDeviceToHost, st));
             DAV_TRY(cudaMemcpyAsync(&qq, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
             DAV_TRY(cudaStreamSynchronize(st));
-            if (qq < conv_thrd) {
-                converged = true;
-                break;
+            // reduced-precision forms: before any exact product is in the basis,
+            // the subspace residual cannot fall below the product's rounding
+            // level, so the first pass stops at max(conv_thrd, (1e-6 lambda)^2)
+            const double thr = (form != B2G_FP64 && !have_exact)
+                                   ? std::max(conv_thrd, 1e-12 * lam * lam) : conv_thrd;
+            if (qq < thr || (form != B2G_FP64 && since_refine >= 40)) {
+                if (form == B2G_FP64) {
+                    converged = true;
+                    break;
+                }
+                // Defect correction: one FP64 product on the Ritz vector gives
+                // the exact residual r = H x - (x,Hx) x.  Converged when |r|^2 is
+                // below conv_thrd; otherwise the basis restarts from x with its
+                // exact sigma, and the correction built from r continues in the
+                // reduced-precision form (its rounding now only enters through
+                // the small correction coefficients).
+                dot_many(x, 1, x, sc + 1);
+                normalize_into<<<g, 256, 0, st>>>(B, x, sc + 1, n);
+                DAV_TRY(cudaMemcpyAsync(x, B, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+                DAV_TRY(cudaMemsetAsync(s, 0, sizeof(double) * n, st));
+                rc = b2g_heff_apply(h, x, s, 1.0, B2G_FP64);
+                if (rc != B2G_OK)
+                    goto done;
+                n_fp64++;
+                dot_many(x, 1, s, w);
+                residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 0);
+                dot_many(q, 1, q, sc + 1);
+                DAV_TRY(cudaMemcpyAsync(&lam, w, sizeof(double), cudaMemcpyDeviceToHost, st));
+                DAV_TRY(cudaMemcpyAsync(&qq, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+                DAV_TRY(cudaStreamSynchronize(st));
+                if (qq < conv_thrd) {
+                    converged = true;
+                    break;
+                }
+                if (++n_refine > 30)
+                    break;
+                DAV_TRY(cudaMemcpyAsync(S, s, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+                set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, 1, w);
+                m = msig = 1;
+                have_exact = true;
+                since_refine = 0;
             }
             // Olsen correction: q = K^-1 r - (x,K^-1 r)/(x,K^-1 x) K^-1 x
             residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 1);
@@ -394,8 +433,8 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
         DAV_TRY(cudaStreamSynchronize(st));
         res->energy = lam;
         res->n_iter = xiter;
-        res->n_apply_fp64 = n_apply;
-        res->n_apply_mixed = 0;
+        res->n_apply_fp64 = n_fp64;
+        res->n_apply_mixed = n_mixed;
         res->residual_norm2 = qq;
         if (!converged)
             rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_davidson: max_iter reached");

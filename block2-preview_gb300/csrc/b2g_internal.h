@@ -78,11 +78,14 @@ struct DevicePlan {
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
 };
 
-// FP64 launchers (b2g_fp64.cu)
-cudaError_t launch_fp64_phase1(const DevicePlan &p, const double *ops, const double *psi,
-                               double *work, cudaStream_t s);
-cudaError_t launch_fp64_phase2(const DevicePlan &p, const double *ops, const double *work,
-                               double *sigma, double scale, cudaStream_t s);
+// CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
+template <typename T>
+cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const double *psi, T *work,
+                               cudaStream_t s);
+template <typename T>
+cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work, double *sigma,
+                               double scale, cudaStream_t s);
+cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t s);
 // compute-ceiling probe: TFLOP/s of a register-resident FP64 FMA loop
 cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops);
 
@@ -98,6 +101,7 @@ struct b2g_heff {
     b2g_context *ctx = nullptr;
     b2g::DevicePlan plan;
     double *ops = nullptr;
+    float *ops32 = nullptr;  // operators rounded to float (made on the first reduced-precision apply)
     double *work = nullptr;
     double *psi_stage = nullptr, *sigma_stage = nullptr; // device staging for the host entry
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;

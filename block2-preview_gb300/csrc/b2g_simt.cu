@@ -1,29 +1,34 @@
-// Plain FP64 form of H_eff*psi on sm_103a.
+// CUDA-core forms of H_eff*psi on sm_103a: plain FP64 (DFMA) and FP32 (FFMA).
 //
 // GB300 executes FP64 on CUDA-core DFMA units only (no FP64 tensor path), at
-// a small fraction of its tensor rate, so these kernels are DFMA-issue bound:
-// the design goal is that every issued DFMA lane does useful work (no padded
-// tiles) and that enough independent warps are resident to hide latency.
-// Operands are re-read through L1/L2 (the operator blocks of one H_eff are
-// reused by many pairs and stay L2-resident); see the phase comments below.
+// a small fraction of its tensor rate, so the FP64 kernels are DFMA-issue
+// bound: the design goal is that every issued DFMA lane does useful work (no
+// padded tiles) and that enough independent warps are resident to hide
+// latency.  Operands are re-read through L1/L2 (the operator blocks of one
+// H_eff are reused by many pairs and stay L2-resident).
+//
+// The FP32 instantiation (operators pre-rounded to float once per plan, W in
+// float, FP32 accumulation, sigma updated in FP64) is the CUDA-core
+// counterpart of the tensor-core mixed form and shares its error model.
 #include "b2g_internal.h"
 
 namespace b2g {
 
 namespace {
 
-constexpr int kLanesCols = 8;   // column chunks of 32 per warp (256 columns)
+constexpr int kLanesCols = 8;  // column chunks of 32 per warp (256 columns)
 
 // Phase 1: one warp per row r of a distinct product W_u (m0 x n0):
 //   W_u[r, c] = sum_k psi[a0 + r*lda0 + k] * B(k, c),
 //   B(k, c) = ops[b0 + k*ldb0 + c] (tb0 = 0) or ops[b0 + c*ldb0 + k] (tb0 = 1).
 // psi loads are warp-broadcast; B loads are coalesced for tb0 = 0 and
 // L1-served column walks for tb0 = 1.
-__global__ void __launch_bounds__(128) fp64_phase1(const WorkDesc *__restrict__ works,
+template <typename T>
+__global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ works,
                                                    const Task1 *__restrict__ tasks, int64_t n_tasks,
-                                                   const double *__restrict__ ops,
+                                                   const T *__restrict__ ops,
                                                    const double *__restrict__ psi,
-                                                   double *__restrict__ work) {
+                                                   T *__restrict__ work) {
     const int64_t t = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (t >= n_tasks)
@@ -31,18 +36,18 @@ __global__ void __launch_bounds__(128) fp64_phase1(const WorkDesc *__restrict__ 
     const Task1 tk = tasks[t];
     const WorkDesc wd = works[tk.u];
     const double *prow = psi + wd.a0 + (uint64_t)tk.r * wd.lda0;
-    const double *B = ops + wd.b0;
-    double *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
+    const T *B = ops + wd.b0;
+    T *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
     for (int cbase = 0; cbase < wd.n0; cbase += 32 * kLanesCols) {
-        double acc[kLanesCols];
+        T acc[kLanesCols];
 #pragma unroll
         for (int j = 0; j < kLanesCols; j++)
-            acc[j] = 0.0;
+            acc[j] = T(0);
         const int nj = min(kLanesCols, (wd.n0 - cbase + 31) >> 5);
         if (!wd.tb0) {
             for (int k = 0; k < wd.k0; k++) {
-                const double a = __ldg(prow + k);
-                const double *brow = B + (uint64_t)k * wd.ldb0 + cbase + lane;
+                const T a = (T)__ldg(prow + k);
+                const T *brow = B + (uint64_t)k * wd.ldb0 + cbase + lane;
 #pragma unroll
                 for (int j = 0; j < kLanesCols; j++)
                     if (j < nj && cbase + lane + 32 * j < wd.n0)
@@ -50,7 +55,7 @@ __global__ void __launch_bounds__(128) fp64_phase1(const WorkDesc *__restrict__ 
             }
         } else {
             for (int k = 0; k < wd.k0; k++) {
-                const double a = __ldg(prow + k);
+                const T a = (T)__ldg(prow + k);
 #pragma unroll
                 for (int j = 0; j < kLanesCols; j++) {
                     const int c = cbase + lane + 32 * j;
@@ -72,14 +77,16 @@ __global__ void __launch_bounds__(128) fp64_phase1(const WorkDesc *__restrict__ 
 // warp per row, lane -> columns lane + 32 j.  The task owns its cells: it
 // loops over its contribution list (pairs whose row window covers its rows)
 // and adds alpha * sum_k A(r - row0, k) * W_u(k, c - col0) in a fixed order,
-// then writes sigma += scale * acc once (no atomics, deterministic).
-__global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tasks,
+// then writes sigma += scale * acc once, only for cells some pair writes
+// (no atomics, deterministic).
+template <typename T>
+__global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tasks,
                                                    const int32_t *__restrict__ lists,
                                                    const Contrib *__restrict__ contribs,
                                                    const Region *__restrict__ regions,
                                                    const WorkDesc *__restrict__ works,
-                                                   const double *__restrict__ ops,
-                                                   const double *__restrict__ work,
+                                                   const T *__restrict__ ops,
+                                                   const T *__restrict__ work,
                                                    double *__restrict__ sigma, double scale) {
     const Task2 tk = tasks[blockIdx.x];
     const Region rg = regions[tk.g];
@@ -87,19 +94,18 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
     const int r = tk.rb * 4 + (threadIdx.x >> 5);
     if (r >= rg.rows)
         return;
-    double acc[kLanesCols];
+    T acc[kLanesCols];
     bool cov[kLanesCols];  // cell written by at least one pair (only those are stored)
 #pragma unroll
     for (int j = 0; j < kLanesCols; j++)
-        acc[j] = 0.0, cov[j] = false;
+        acc[j] = T(0), cov[j] = false;
     for (int64_t li = tk.lb; li < tk.le; li++) {
         const Contrib c = contribs[lists[li]];
         const int ar = r - c.row0;
         if (ar < 0 || ar >= c.m1)
             continue;  // warp-uniform
-        const double *A = ops + c.a1;
-        const double *W = work + works[c.u].woff;
-        // columns of this lane inside the contribution window
+        const T *A = ops + c.a1;
+        const T *W = work + works[c.u].woff;
         int cc[kLanesCols];
 #pragma unroll
         for (int j = 0; j < kLanesCols; j++) {
@@ -107,10 +113,11 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
             cc[j] = (col >= 0 && col < c.n1) ? col : -1;
             cov[j] = cov[j] || cc[j] >= 0;
         }
+        const T alpha = (T)c.alpha;
         for (int k = 0; k < c.k1; k++) {
-            const double a = c.alpha * __ldg(c.ta1 ? A + (uint64_t)k * c.lda1 + ar
-                                                    : A + (uint64_t)ar * c.lda1 + k);
-            const double *wrow = W + (uint64_t)k * c.n1;
+            const T a = alpha * __ldg(c.ta1 ? A + (uint64_t)k * c.lda1 + ar
+                                            : A + (uint64_t)ar * c.lda1 + k);
+            const T *wrow = W + (uint64_t)k * c.n1;
 #pragma unroll
             for (int j = 0; j < kLanesCols; j++)
                 if (cc[j] >= 0)
@@ -121,7 +128,7 @@ __global__ void __launch_bounds__(128) fp64_phase2(const Task2 *__restrict__ tas
 #pragma unroll
     for (int j = 0; j < kLanesCols; j++)
         if (cov[j])
-            srow[tk.col0 + lane + 32 * j] += scale * acc[j];
+            srow[tk.col0 + lane + 32 * j] += scale * (double)acc[j];
 }
 
 // FP64 ceiling probe: 8 independent FMA chains per thread, no memory traffic
@@ -140,6 +147,12 @@ __global__ void __launch_bounds__(256) fp64_fma_loop(double *out, int iters, dou
         s += a[j];
     if (s == 12345.678)  // never true: keeps the loop live
         out[0] = s;
+}
+
+__global__ void to_float(const double *__restrict__ x, float *__restrict__ y, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        y[i] = (float)x[i];
 }
 
 } // namespace
@@ -167,22 +180,41 @@ cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops) {
     return e;
 }
 
-cudaError_t launch_fp64_phase1(const DevicePlan &p, const double *ops, const double *psi,
-                               double *work, cudaStream_t s) {
-    if (p.n_t1 == 0)
+cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t s) {
+    if (n == 0)
         return cudaSuccess;
-    const int64_t blocks = (p.n_t1 + 3) / 4;
-    fp64_phase1<<<(unsigned)blocks, 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi, work);
+    const uint64_t b = (n + 255) / 256;
+    to_float<<<(unsigned)(b < 152 * 16 ? b : 152 * 16), 256, 0, s>>>(x, y, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fp64_phase2(const DevicePlan &p, const double *ops, const double *work,
-                               double *sigma, double scale, cudaStream_t s) {
-    if (p.n_t2 == 0)
+template <typename T>
+cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const double *psi, T *work,
+                               cudaStream_t s) {
+    if (p.n_t1 == 0)
         return cudaSuccess;
-    fp64_phase2<<<(unsigned)p.n_t2, 128, 0, s>>>(p.t2, p.lists, p.contribs, p.regions, p.works, ops,
-                                                 work, sigma, scale);
+    const int64_t blocks = (p.n_t1 + 3) / 4;
+    simt_phase1<T><<<(unsigned)blocks, 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi, work);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work, double *sigma,
+                               double scale, cudaStream_t s) {
+    if (p.n_t2 == 0)
+        return cudaSuccess;
+    simt_phase2<T><<<(unsigned)p.n_t2, 128, 0, s>>>(p.t2, p.lists, p.contribs, p.regions, p.works,
+                                                    ops, work, sigma, scale);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_simt_phase1<double>(const DevicePlan &, const double *, const double *,
+                                                double *, cudaStream_t);
+template cudaError_t launch_simt_phase1<float>(const DevicePlan &, const float *, const double *,
+                                               float *, cudaStream_t);
+template cudaError_t launch_simt_phase2<double>(const DevicePlan &, const double *, const double *,
+                                                double *, double, cudaStream_t);
+template cudaError_t launch_simt_phase2<float>(const DevicePlan &, const float *, const float *,
+                                               double *, double, cudaStream_t);
 
 } // namespace b2g

@@ -51,6 +51,7 @@ extern "C" {
 /* arithmetic forms of H_eff*psi */
 #define B2G_FP64 0             /* plain FP64 (CUDA-core DFMA) */
 #define B2G_TF32X3 1           /* split-TF32 x3 on tcgen05 tensor cores, FP32 accumulate */
+#define B2G_FP32 2             /* FP32 on CUDA cores (FFMA), FP32 accumulate */
 
 /*
  * The recorded GEMM-pair sequence of one H_eff*psi: BatchGEMMSeq::batch[0]
@@ -156,10 +157,14 @@ int b2g_probe_peak(b2g_context *ctx, int form, double *tflops);
  * Normal Davidson with Olsen preconditioning and thick restart to
  * def_min vectors when def_max is reached.  diag: diag(H_eff) (host),
  * psi: initial guess in, converged eigenvector out (host).  Convergence on
- * |r|^2 < conv_thrd.  form selects the arithmetic of the H_eff products; with
- * B2G_TF32X3 every residual is recomputed with an FP64 product (defect
- * correction).  Outputs: energy (eigenvalue, without const_e), iterations,
- * number of H_eff products by form.
+ * |r|^2 < conv_thrd.  form selects the arithmetic of the H_eff products that
+ * expand the basis; for a reduced-precision form (B2G_TF32X3, B2G_FP32)
+ * convergence is only ever declared on an FP64 residual: when the subspace
+ * residual is small, one FP64 product on the Ritz vector x gives the exact
+ * r = Hx - (x,Hx)x; if |r|^2 >= conv_thrd the basis restarts from x with its
+ * exact sigma and continues (defect correction).  The energy returned is
+ * the FP64 Rayleigh quotient.  Outputs: energy (eigenvalue, without
+ * const_e), iterations, number of H_eff products by form.
  */
 typedef struct {
     double energy;

@@ -84,6 +84,38 @@ def test_davidson_matches_reference(problems, heffs, name):
     assert ndav >= 1 and nflop > 0
 
 
+RTOL_FP32 = 2e-5    # reduced-precision products (FP32 rounding of operators, W, sums)
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+def test_apply_fp32_form_accuracy(problems, heffs, ctx, name):
+    p, h = problems[name], heffs[name]
+    psi = torch.from_numpy(p.psi).cuda()
+    sig = torch.zeros(p.sigma_size, dtype=torch.float64, device="cuda")
+    h(psi, sig, 1.0, b2g.FP32)
+    ctx.synchronize()
+    assert rel(sig.cpu().numpy(), p.sigma) <= RTOL_FP32
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+def test_davidson_fp32_with_fp64_defect_correction(problems, heffs, name):
+    """Basis expanded with FP32 products; convergence declared on FP64
+    residuals only; energy = FP64 Rayleigh quotient: within 1e-8 Ha."""
+    p, h = problems[name], heffs[name]
+    m = p.meta
+    psi = np.array(p.psi, copy=True)
+    e, ndav, nflop, tdav = h.eigs(p.diag, psi, conv_thrd=m["conv_thrd"], def_min=m["def_min"],
+                                  def_max=m["def_max"], form=b2g.FP32)
+    r = h.last_davidson
+    assert abs(e + m["const_e"] - m["davidson_energy"]) <= 1e-8
+    assert r.n_apply_fp64 >= 1 and r.n_apply_mixed >= 1
+    assert r.residual_norm2 < m["conv_thrd"]
+    # the returned vector's FP64 residual, checked independently on the host
+    hx = oracle.replay(p.seq(), p.ops, psi, p.sigma_size)
+    lam = psi @ hx / (psi @ psi)
+    assert np.sum((hx - lam * psi) ** 2) / (psi @ psi) < 10 * m["conv_thrd"]
+
+
 def test_size_mismatch_raises(problems, heffs):
     name = sorted(problems)[0]
     h = heffs[name]
