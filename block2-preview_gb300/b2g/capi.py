@@ -73,6 +73,7 @@ SIGNATURES = {
     "b2g_heff_create": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_int,
                                   C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
     "b2g_heff_destroy": (C.c_int, [C.c_void_p]),
+    "b2g_heff_status": (C.c_int, [C.c_void_p]),
     "b2g_heff_stats_get": (C.c_int, [C.c_void_p, C.POINTER(HeffStatsC)]),
     "b2g_plan_stats": (C.c_int, [C.POINTER(PairSeqC), C.c_uint64, C.c_uint64, C.c_uint64,
                                  C.POINTER(HeffStatsC)]),

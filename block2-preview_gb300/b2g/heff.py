@@ -101,6 +101,10 @@ class EffectiveHamiltonian:
             check(lib().b2g_heff_apply(self._h, _ptr(b), _ptr(c), scale, form))
         return c
 
+    def status(self):
+        """Synchronize and raise if a tensor-core kernel gave up a bounded wait."""
+        check(lib().b2g_heff_status(self._h))
+
     def apply_ptr(self, psi_ptr: int, sigma_ptr: int, scale: float = 1.0, form: int = FP64):
         """Raw device-pointer entry (asynchronous on the context stream)."""
         check(lib().b2g_heff_apply(self._h, psi_ptr, sigma_ptr, scale, form))

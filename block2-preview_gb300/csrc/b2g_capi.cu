@@ -33,6 +33,7 @@ template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaSt
 static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
+    cudaFree(p.tct), cudaFree(p.tcs);
     p = DevicePlan();
 }
 
@@ -108,7 +109,7 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     h->work_size = hp.work_size;
     auto bail = [&](int code) {
         free_plan(h->plan);
-        cudaFree(h->ops), cudaFree(h->work);
+        cudaFree(h->ops), cudaFree(h->work), cudaFree(h->err);
         delete h;
         return code;
     };
@@ -127,14 +128,22 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         h->work = nullptr;
         return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the work buffer"));
     }
+    if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) {
+        h->err = nullptr;
+        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the error flag"));
+    }
+    if (cudaMemsetAsync(h->err, 0, sizeof(int), s) != cudaSuccess)
+        return bail(fail(B2G_ERR_CUDA, "error flag reset failed"));
     DevicePlan &p = h->plan;
     if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
         (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
-        (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)))
+        (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
+        (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)))
         return bail(rc);
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
     p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
     p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
+    p.n_tct = (int64_t)hp.tct.size(), p.n_tcs = (int64_t)hp.tcs.size();
     if (cudaStreamSynchronize(s) != cudaSuccess)
         return bail(fail(B2G_ERR_CUDA, "plan upload failed"));
     b2g_heff_stats &st = h->stats;
@@ -148,9 +157,22 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     st.work_bytes = sizeof(double) * hp.work_size;
     st.plan_bytes = sizeof(WorkDesc) * hp.works.size() + sizeof(Contrib) * hp.contribs.size() +
                     sizeof(Region) * hp.regions.size() + sizeof(Task1) * hp.t1.size() +
-                    sizeof(Task2) * hp.t2.size() + sizeof(int32_t) * hp.lists.size();
+                    sizeof(Task2) * hp.t2.size() + sizeof(int32_t) * hp.lists.size() +
+                    sizeof(TcTask) * hp.tct.size() + sizeof(TcSeg) * hp.tcs.size();
     st.psi_size = psi_size, st.sigma_size = sigma_size;
     *out = h;
+    return B2G_OK;
+}
+
+int b2g_heff_status(b2g_heff *h) {
+    if (h == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_status: null handle");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+    int e = 0;
+    B2G_CUDA_TRY(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e != 0)
+        return fail(B2G_ERR_STATE, "b2g: a tensor-core kernel gave up a bounded wait; its sigma is incomplete");
     return B2G_OK;
 }
 
@@ -161,7 +183,7 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaStreamSynchronize(h->ctx->stream);
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->work);
-    cudaFree(h->psi_stage), cudaFree(h->sigma_stage);
+    cudaFree(h->psi_stage), cudaFree(h->sigma_stage), cudaFree(h->err);
     for (auto &e : h->ev)
         if (e)
             cudaEventDestroy(e);
@@ -251,7 +273,7 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;
     }
-    if (form == B2G_FP32) {
+    if (form == B2G_FP32 || form == B2G_TF32X3) {
         if (h->ops32 == nullptr && h->ops_size) {
             if (cudaMalloc(&h->ops32, sizeof(float) * h->ops_size) != cudaSuccess) {
                 h->ops32 = nullptr;
@@ -265,7 +287,10 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
         B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, psi, w32, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-        B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, scale, s));
+        if (form == B2G_TF32X3)
+            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops, w32, sigma, scale, h->err, s));
+        else
+            B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, scale, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;
@@ -297,6 +322,8 @@ int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double sc
         return rc;
     B2G_CUDA_TRY(cudaMemcpyAsync(sigma, h->sigma_stage, sizeof(double) * h->sigma_size,
                                  cudaMemcpyDeviceToHost, s));
+    if (form == B2G_TF32X3)
+        return b2g_heff_status(h);
     B2G_CUDA_TRY(cudaStreamSynchronize(s));
     return B2G_OK;
 }

@@ -438,6 +438,8 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
         res->residual_norm2 = qq;
         if (!converged)
             rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_davidson: max_iter reached");
+        if (form == B2G_TF32X3 && b2g_heff_status(h) != B2G_OK)
+            rc = B2G_ERR_STATE;
     }
 done:
 #undef DAV_TRY

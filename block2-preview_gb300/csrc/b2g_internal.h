@@ -44,6 +44,7 @@ struct Contrib {        // one GEMM1 contribution (one recorded pair)
 };
 struct Region {
     uint64_t base;      // sigma offset of (0, 0)
+    uint64_t lo, hi;    // merged write span [lo, hi): cells owned by this region
     int32_t ld, rows, cols, pad;
 };
 struct Task1 {          // phase 1: one row of one work product
@@ -54,6 +55,22 @@ struct Task2 {          // phase 2: rows [4*rb, 4*rb+4) x cols [col0, col0+256) 
     int64_t lb, le;     // contribution list range
 };
 
+// Tensor-core phase 2: one CTA per 128-row x N-column tile of a region; the
+// tile's contributions are cut into K segments packed into stages of
+// kTcStageK columns (zero-padded), one tcgen05 MMA group per stage.
+constexpr int kTcStageK = 16;
+struct TcTask {
+    int32_t g, row0, col0, n;   // region, tile origin, tile width (multiple of 16, <= 256)
+    int64_t sb, se;             // segment range
+    int32_t n_stages, pad;
+};
+struct TcSeg {
+    int32_t c;                  // contribution index
+    int16_t kb, kl;             // k range [kb, kb + kl) of the contribution
+    int32_t stage;              // stage index within the task
+    int32_t koff;               // column offset inside the stage
+};
+
 struct HostPlan {
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
@@ -61,6 +78,8 @@ struct HostPlan {
     std::vector<Task1> t1;
     std::vector<Task2> t2;
     std::vector<int32_t> lists;
+    std::vector<TcTask> tct;
+    std::vector<TcSeg> tcs;
     uint64_t work_size = 0;
     double mnk = 0, mnk_exec = 0;
 };
@@ -75,8 +94,16 @@ struct DevicePlan {
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;
     int32_t *lists = nullptr;
+    TcTask *tct = nullptr;
+    TcSeg *tcs = nullptr;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
+    int64_t n_tct = 0, n_tcs = 0;
 };
+
+// tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
+// bounded wait gives up
+cudaError_t launch_tc_phase2(const DevicePlan &p, const double *ops, const float *work,
+                             double *sigma, double scale, int *err, cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>
@@ -108,4 +135,5 @@ struct b2g_heff {
     b2g_heff_stats stats{};
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    int *err = nullptr;     // device flag: a bounded wait in a tensor-core kernel gave up
 };

@@ -149,6 +149,11 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             return fail(B2G_ERR_UNSUPPORTED, "no consistent column frame for a sigma region");
         Region rg;
         rg.ld = ld, rg.pad = 0;
+        rg.lo = UINT64_MAX, rg.hi = 0;
+        for (int64_t i : gp) {
+            rg.lo = std::min(rg.lo, s->c1[i]);
+            rg.hi = std::max(rg.hi, s->c1[i] + extent(false, s->m1[i], s->n1[i], s->ldc1[i]));
+        }
         uint64_t base = UINT64_MAX;
         std::vector<int64_t> colp(gp.size());
         for (size_t q = 0; q < gp.size(); q++) {
@@ -202,7 +207,39 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 t.le = (int64_t)plan.lists.size();
                 plan.t2.push_back(t);
             }
+        // tensor-core tiles: 128 rows x up to 256 columns, contributions packed
+        // along K into stages of kTcStageK columns
+        for (int32_t r0 = 0; r0 < rows; r0 += 128)
+            for (int32_t c0 = 0; c0 < cols; c0 += 256) {
+                const int32_t nt = std::min(256, ((cols - c0) + 15) / 16 * 16);
+                TcTask t;
+                t.g = g, t.row0 = r0, t.col0 = c0, t.n = nt, t.pad = 0;
+                t.sb = (int64_t)plan.tcs.size();
+                int32_t stage = 0, koff = 0;
+                for (size_t q = c_begin; q < plan.contribs.size(); q++) {
+                    const Contrib &c = plan.contribs[q];
+                    if (c.row0 >= r0 + 128 || c.row0 + c.m1 <= r0 || c.col0 >= c0 + nt ||
+                        c.col0 + c.n1 <= c0)
+                        continue;
+                    for (int32_t kb = 0; kb < c.k1;) {
+                        const int32_t take = std::min(c.k1 - kb, kTcStageK - koff);
+                        TcSeg sg;
+                        sg.c = (int32_t)q, sg.kb = (int16_t)kb, sg.kl = (int16_t)take;
+                        sg.stage = stage, sg.koff = koff;
+                        plan.tcs.push_back(sg);
+                        kb += take, koff += take;
+                        if (koff == kTcStageK)
+                            stage++, koff = 0;
+                    }
+                }
+                t.se = (int64_t)plan.tcs.size();
+                t.n_stages = stage + (koff > 0 ? 1 : 0);
+                if (t.se > t.sb)
+                    plan.tct.push_back(t);
+            }
     }
+    std::stable_sort(plan.tct.begin(), plan.tct.end(),
+                     [](const TcTask &a, const TcTask &b) { return a.n_stages > b.n_stages; });
     // heavy tasks first: shortens the tail of the phase-2 grid
     std::stable_sort(plan.t2.begin(), plan.t2.end(),
                      [](const Task2 &a, const Task2 &b) { return a.le - a.lb > b.le - b.lb; });

@@ -112,6 +112,10 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
                     uint64_t sigma_size, b2g_heff **out);
 int b2g_heff_destroy(b2g_heff *h);
 int b2g_heff_stats_get(const b2g_heff *h, b2g_heff_stats *out);
+/* Synchronizes the context stream and reports B2G_ERR_STATE if a
+ * tensor-core kernel of this H_eff gave up a bounded wait (its result is
+ * then incomplete).  b2g_heff_apply_host and b2g_davidson check this too. */
+int b2g_heff_status(b2g_heff *h);
 /* Host-only dry run of the plan builder (no device touched): validates the
  * sequence against the sizes and reports the schedule statistics. */
 int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size,

@@ -116,6 +116,36 @@ def test_davidson_fp32_with_fp64_defect_correction(problems, heffs, name):
     assert np.sum((hx - lam * psi) ** 2) / (psi @ psi) < 10 * m["conv_thrd"]
 
 
+RTOL_TF32X3 = 2e-5  # split-TF32 x3 on tensor cores, FP32 accumulation, FP32 work matrices
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+def test_apply_tf32x3_tensor_core_accuracy(problems, heffs, ctx, name):
+    p, h = problems[name], heffs[name]
+    psi = torch.from_numpy(p.psi).cuda()
+    sig = torch.zeros(p.sigma_size, dtype=torch.float64, device="cuda")
+    h(psi, sig, 1.0, b2g.TF32X3)
+    h.status()
+    assert rel(sig.cpu().numpy(), p.sigma) <= RTOL_TF32X3
+    # accumulate semantics and determinism (fixed summation order per tile)
+    s2 = sig.clone()
+    h(psi, s2, -1.0, b2g.TF32X3)
+    h.status()
+    assert float(torch.max(torch.abs(s2))) <= 1e-12 * float(torch.max(torch.abs(sig)))
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+def test_davidson_tf32x3_with_fp64_defect_correction(problems, heffs, name):
+    p, h = problems[name], heffs[name]
+    m = p.meta
+    psi = np.array(p.psi, copy=True)
+    e, ndav, nflop, tdav = h.eigs(p.diag, psi, conv_thrd=m["conv_thrd"], def_min=m["def_min"],
+                                  def_max=m["def_max"], form=b2g.TF32X3)
+    r = h.last_davidson
+    assert abs(e + m["const_e"] - m["davidson_energy"]) <= 1e-8
+    assert r.n_apply_mixed >= 1 and r.residual_norm2 < m["conv_thrd"]
+
+
 def test_size_mismatch_raises(problems, heffs):
     name = sorted(problems)[0]
     h = heffs[name]
