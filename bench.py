@@ -132,7 +132,14 @@ def cpu_replay_timing(prob, max_steps: int, budget_s: float, warmup: int = 1):
 
 
 # ----------------------------------------------------------------------------- our arm
+FORMS = {"fp64": 0, "tf32x3": 1, "fp32": 2}
+FORM_DTYPE = {"fp64": "f64", "tf32x3": "tf32x3 (split TF32 on tcgen05, f32 accumulate) -> f64 sigma",
+              "fp32": "f32 (CUDA cores) -> f64 sigma"}
+
+
 def run_ours(args, rank, local_rank, world, dist):
+    import ctypes as C
+
     import torch
 
     import b2g
@@ -141,11 +148,13 @@ def run_ours(args, rank, local_rank, world, dist):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     prob = load_workload(args.workload)
-    form = {"fp64": b2g.FP64}[args.form]
     ctx = b2g.Context(local_rank)
     heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
     st = heff.stats
     flop = 2.0 * st["mnk"]
+    a = prob.pairs
+    flop0 = 2.0 * float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]))
+    flop1 = 2.0 * float(np.sum(a["m1"].astype(np.float64) * a["n1"] * a["k1"]))
     stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
     psi = torch.from_numpy(prob.psi).to(dev)
     sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
@@ -155,64 +164,102 @@ def run_ours(args, rank, local_rank, world, dist):
         flush = torch.empty(4 * L2_BYTES, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
 
-    def step():
+    def do_flush():
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+
+    def step(form):
         with torch.cuda.stream(stream):
             sig.zero_()
         heff.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, form)
 
-    for _ in range(args.warmup):
-        step()
-    ctx.synchronize()
-    # ---- timed device leg: per-step CUDA events on the launching stream
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    clocks = ClockSampler(local_rank)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    t_wall = time.perf_counter()
-    for k in range(args.steps):
-        if flush is not None:
-            with torch.cuda.stream(stream):
-                flush.zero_()
-        evs[k][0].record(stream)
-        step()
-        evs[k][1].record(stream)
-    ctx.synchronize()
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall
-    ck = clocks.stop()
-    if dist is not None:
-        dist.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_s = sum(step_ms) / 1e3
-    # ---- per-kernel timing (dominant kernel) with events inside the library
-    capi.check(capi.lib().b2g_heff_set_timing(heff._h, 1))
-    ph = []
-    import ctypes as C
-    for _ in range(3):
-        if flush is not None:
-            with torch.cuda.stream(stream):
-                flush.zero_()
-        step()
-        ms = (C.c_float * 2)()
-        capi.check(capi.lib().b2g_heff_last_timing(heff._h, ms))
-        ph.append((ms[0], ms[1]))
-    capi.check(capi.lib().b2g_heff_set_timing(heff._h, 0))
-    p1 = statistics.median(x[0] for x in ph)
-    p2 = statistics.median(x[1] for x in ph)
-    pk = C.c_double()
-    capi.check(capi.lib().b2g_probe_peak(ctx.handle, b2g.FP64, C.byref(pk)))
-    a = prob.pairs
-    flop0 = 2.0 * float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]))
-    flop1 = 2.0 * float(np.sum(a["m1"].astype(np.float64) * a["n1"] * a["k1"]))
-    if p2 >= p1:
-        kname, kflop, kms = "fp64_phase2 (GEMM1: sigma += alpha op(L) W)", flop1, p2
+    def time_form(form, clocks=None):
+        for _ in range(args.warmup):
+            step(form)
+        heff.status()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if clocks is not None:
+            clocks.start()
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            do_flush()
+            evs[k][0].record(stream)
+            step(form)
+            evs[k][1].record(stream)
+        heff.status()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+        ck = clocks.stop() if clocks is not None else None
+        total = sum(x.elapsed_time(y) for x, y in evs) / 1e3
+        # per-kernel times (CUDA events recorded inside the library around each phase)
+        capi.check(capi.lib().b2g_heff_set_timing(heff._h, 1))
+        ph = []
+        for _ in range(3):
+            do_flush()
+            step(form)
+            ms = (C.c_float * 2)()
+            capi.check(capi.lib().b2g_heff_last_timing(heff._h, ms))
+            ph.append((ms[0], ms[1]))
+        capi.check(capi.lib().b2g_heff_set_timing(heff._h, 0))
+        p1 = statistics.median(x[0] for x in ph)
+        p2 = statistics.median(x[1] for x in ph)
+        return total, t_wall, p1, p2, ck, float(torch.linalg.norm(sig))
+
+    head = args.form
+    per_form = {}
+    head_res = None
+    for name in [head] + [f for f in FORMS if f != head]:
+        clocks = ClockSampler(local_rank) if name == head else None
+        total, t_wall, p1, p2, ck, nrm = time_form(FORMS[name], clocks)
+        tt = torch.tensor([total], dtype=torch.float64, device=dev)
+        if dist is not None:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total = float(tt[0])
+        per_form[name] = {"value": flop * args.steps * world / total / 1e12, "unit": "TFLOP/s",
+                          "ms_per_step": total / args.steps * 1e3,
+                          "phase_ms": {"gemm0": p1, "gemm1": p2}}
+        if name == head:
+            head_res = (total, t_wall, p1, p2, ck, nrm)
+    total, t_wall, p1, p2, ck, nrm = head_res
+    # sigma of each form against FP64 (relative 2-norm), same psi
+    ref = torch.zeros_like(sig)
+    heff.apply_ptr(psi.data_ptr(), ref.data_ptr(), 1.0, FORMS["fp64"])
+    for name in FORMS:
+        out = torch.zeros_like(sig)
+        heff.apply_ptr(psi.data_ptr(), out.data_ptr(), 1.0, FORMS[name])
+        heff.status()
+        per_form[name]["rel_err_vs_fp64"] = float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref))
+    # ---- roofline of the dominant kernel of the headline form
+    if head == "fp64":
+        pk = C.c_double()
+        capi.check(capi.lib().b2g_probe_peak(ctx.handle, FORMS["fp64"], C.byref(pk)))
+        peak, bound, unit = pk.value, "fp64-pipe", "TFLOP/s"
+        peak_src = ("measured in this run: register-resident FP64 FMA loop (b2g_probe_peak); GB300 has "
+                    "no FP64 tensor path and MEASURED_PEAKS.json holds no FP64 figure")
+        k2 = "simt_phase2<double> (GEMM1 sigma += alpha op(L) W)"
+        k1 = "simt_phase1<double> (GEMM0 W = psi op(R))"
     else:
-        kname, kflop, kms = "fp64_phase1 (GEMM0: W = psi op(R))", flop0, p1
+        pk_all = peaks()
+        peak = pk_all.get("bf16_tflops", 1900.0)
+        bound, unit = "tensor", "TFLOP/s"
+        peak_src = ("MEASURED_PEAKS.json bf16_tflops (burst) of measured; dense TF32 is nominally half of "
+                    "BF16 and split-TF32x3 issues 3 MMAs per useful product, so 1/6 of this is the "
+                    "useful-FLOP ceiling of this kernel")
+        k2 = ("tc_phase2_kernel (tcgen05.mma kind::tf32 x3, TMEM accumulator)" if head == "tf32x3"
+              else "simt_phase2<float>")
+        k1 = "simt_phase1<float> (GEMM0 W = psi op(R), FP32)"
+    if p2 >= p1:
+        kname, kflop, kms = k2, flop1, p2
+    else:
+        kname, kflop, kms = k1, flop0, p1
     achieved = kflop / (kms * 1e-3) / 1e12
-    # ---- e2e leg: host buffers through the C ABI host entry
+    # ---- e2e leg: host buffers through the C-ABI host entry
+    form = FORMS[head]
     psi_h = torch.from_numpy(prob.psi).pin_memory().numpy()
     sig_h = torch.zeros(prob.sigma_size, dtype=torch.float64).pin_memory().numpy()
     for _ in range(max(1, args.warmup)):
@@ -222,23 +269,18 @@ def run_ours(args, rank, local_rank, world, dist):
     if dist is not None:
         dist.barrier()
     for _ in range(args.steps):
-        if flush is not None:
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            ctx.synchronize()
+        do_flush()
+        ctx.synchronize()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         sig_h[:] = 0.0
         heff(psi_h, sig_h, 1.0, form)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_t)
-    check = float(np.linalg.norm(sig_h))
-    # ---- max over ranks
-    tot = torch.tensor([total_s, e2e_total], dtype=torch.float64, device=dev)
+    tt = torch.tensor([sum(e2e_t)], dtype=torch.float64, device=dev)
     if dist is not None:
-        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
-    total_s, e2e_total = float(tot[0]), float(tot[1])
-    value = flop * args.steps * world / total_s / 1e12
-    e2e_value = flop * args.steps * world / e2e_total / 1e12
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_total = float(tt[0])
+    value = flop * args.steps * world / total / 1e12
     result = {
         "metric": METRIC,
         "value": value,
@@ -246,16 +288,16 @@ def run_ours(args, rank, local_rank, world, dist):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": total_s / args.steps * 1e3,
+        "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": FORM_DTYPE[head],
         "data": prob.meta.get("data", "synthetic"),
         "config": {
             "workload": args.workload,
             "description": prob.meta.get("description", ""),
-            "form": args.form,
+            "form": head,
             "n_pairs": st["n_pairs"], "n_work_dedup": st["n_work"], "n_sigma_regions": st["n_regions"],
             "mnk": st["mnk"], "mnk_executed": st["mnk_executed"], "psi_size": prob.psi_size,
             "ops_bytes": st["ops_bytes"],
@@ -264,27 +306,21 @@ def run_ours(args, rank, local_rank, world, dist):
             "parallelism": f"replicas x{world}",
             "wall_s_timed_region": t_wall,
         },
+        "forms": per_form,
         "roofline": {
-            "bound": "fp64-pipe",
-            "kernel": kname,
-            "achieved": achieved,
-            "peak": pk.value,
-            "unit": "TFLOP/s",
-            "frac": achieved / pk.value if pk.value else None,
-            "peak_source": "measured in this run: register-resident FP64 FMA loop (b2g_probe_peak); "
-                           "GB300 has no FP64 tensor path, MEASURED_PEAKS.json holds no FP64 figure",
-            "phase_ms": {"gemm0": p1, "gemm1": p2},
-            "traffic": None,
+            "bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak if peak else None, "peak_source": peak_src,
+            "phase_ms": {"gemm0": p1, "gemm1": p2}, "traffic": None,
         },
         "e2e": {
-            "value": e2e_value, "unit": "TFLOP/s",
+            "value": flop * args.steps * world / e2e_total / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": 8 * (prob.psi_size + prob.sigma_size),
             "d2h_bytes_per_step": 8 * prob.sigma_size,
             "ms_per_step": e2e_total / args.steps * 1e3,
         },
         "gpu_launches": args.steps * 2,
         "clocks": ck,
-        "sigma_norm": check,
+        "sigma_norm": nrm,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, nth, blas = cpu_replay_timing(prob, max_steps=10, budget_s=20.0, warmup=1)
@@ -325,7 +361,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=None)
-    ap.add_argument("--form", default="fp64", choices=["fp64"])
+    ap.add_argument("--form", default="tf32x3", choices=sorted(FORMS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     from b2g import workloads
