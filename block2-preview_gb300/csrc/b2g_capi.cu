@@ -33,7 +33,7 @@ template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaSt
 static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
-    cudaFree(p.tct), cudaFree(p.tcs);
+    cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi), cudaFree(p.tc_part);
     p = DevicePlan();
 }
 
@@ -138,8 +138,14 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
         (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
         (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
-        (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)))
+        (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)) ||
+        (rc = upload(hp.tctile, &p.tctile, s)) || (rc = upload(hp.tc_multi, &p.tc_multi, s)))
         return bail(rc);
+    if (hp.tc_part_size && cudaMalloc(&p.tc_part, sizeof(float) * hp.tc_part_size) != cudaSuccess) {
+        p.tc_part = nullptr;
+        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the split-K partial tiles"));
+    }
+    p.n_tctile = (int64_t)hp.tctile.size(), p.n_tc_multi = (int64_t)hp.tc_multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
     p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
     p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();

@@ -55,19 +55,28 @@ struct Task2 {          // phase 2: rows [4*rb, 4*rb+4) x cols [col0, col0+256) 
     int64_t lb, le;     // contribution list range
 };
 
-// Tensor-core phase 2: one CTA per 128-row x N-column tile of a region; the
-// tile's contributions are cut into K segments packed into stages of
-// kTcStageK columns (zero-padded), one tcgen05 MMA group per stage.
+// Tensor-core phase 2: the contributions of a 128-row x N-column tile of a
+// region are cut into K segments packed into stages of kTcStageK columns
+// (zero-padded).  The stage list of a tile is split into chunks of at most
+// kTcChunkStages stages (split-K); one CTA per chunk.  A tile with one chunk
+// updates sigma directly; otherwise each chunk stores a partial tile and a
+// reduction kernel sums the partials in chunk order (deterministic).
 constexpr int kTcStageK = 16;
-struct TcTask {
+constexpr int kTcChunkStages = 64;
+struct TcTile {
     int32_t g, row0, col0, n;   // region, tile origin, tile width (multiple of 16, <= 256)
+    int32_t rows, n_chunks;     // valid rows (<= 128), chunks
+    int64_t part;               // offset (floats) of this tile's partials, -1 if single chunk
+};
+struct TcTask {                 // one chunk of one tile
+    int32_t tile, chunk;
     int64_t sb, se;             // segment range
-    int32_t n_stages, pad;
+    int32_t st0, n_stages;      // first stage index (tile numbering), stages in this chunk
 };
 struct TcSeg {
     int32_t c;                  // contribution index
     int16_t kb, kl;             // k range [kb, kb + kl) of the contribution
-    int32_t stage;              // stage index within the task
+    int32_t stage;              // stage index within the tile
     int32_t koff;               // column offset inside the stage
 };
 
@@ -80,6 +89,9 @@ struct HostPlan {
     std::vector<int32_t> lists;
     std::vector<TcTask> tct;
     std::vector<TcSeg> tcs;
+    std::vector<TcTile> tctile;
+    std::vector<int32_t> tc_multi;  // tiles with more than one chunk
+    uint64_t tc_part_size = 0;      // floats of partial tiles
     uint64_t work_size = 0;
     double mnk = 0, mnk_exec = 0;
 };
@@ -96,8 +108,11 @@ struct DevicePlan {
     int32_t *lists = nullptr;
     TcTask *tct = nullptr;
     TcSeg *tcs = nullptr;
+    TcTile *tctile = nullptr;
+    int32_t *tc_multi = nullptr;
+    float *tc_part = nullptr;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
-    int64_t n_tct = 0, n_tcs = 0;
+    int64_t n_tct = 0, n_tcs = 0, n_tctile = 0, n_tc_multi = 0;
 };
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a

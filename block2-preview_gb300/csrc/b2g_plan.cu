@@ -212,9 +212,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         for (int32_t r0 = 0; r0 < rows; r0 += 128)
             for (int32_t c0 = 0; c0 < cols; c0 += 256) {
                 const int32_t nt = std::min(256, ((cols - c0) + 15) / 16 * 16);
-                TcTask t;
-                t.g = g, t.row0 = r0, t.col0 = c0, t.n = nt, t.pad = 0;
-                t.sb = (int64_t)plan.tcs.size();
+                const int64_t sb = (int64_t)plan.tcs.size();
                 int32_t stage = 0, koff = 0;
                 for (size_t q = c_begin; q < plan.contribs.size(); q++) {
                     const Contrib &c = plan.contribs[q];
@@ -232,10 +230,34 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                             stage++, koff = 0;
                     }
                 }
-                t.se = (int64_t)plan.tcs.size();
-                t.n_stages = stage + (koff > 0 ? 1 : 0);
-                if (t.se > t.sb)
+                const int64_t se = (int64_t)plan.tcs.size();
+                const int32_t n_stages = stage + (koff > 0 ? 1 : 0);
+                if (se == sb)
+                    continue;
+                TcTile tl;
+                tl.g = g, tl.row0 = r0, tl.col0 = c0, tl.n = nt;
+                tl.rows = std::min(128, rows - r0);
+                tl.n_chunks = (n_stages + kTcChunkStages - 1) / kTcChunkStages;
+                tl.part = -1;
+                const int32_t tile = (int32_t)plan.tctile.size();
+                if (tl.n_chunks > 1) {
+                    tl.part = (int64_t)plan.tc_part_size;
+                    plan.tc_part_size += (uint64_t)tl.n_chunks * 128 * nt;
+                    plan.tc_multi.push_back(tile);
+                }
+                plan.tctile.push_back(tl);
+                int64_t s = sb;
+                for (int32_t ch = 0; ch < tl.n_chunks; ch++) {
+                    TcTask t;
+                    t.tile = tile, t.chunk = ch;
+                    t.st0 = ch * kTcChunkStages;
+                    t.n_stages = std::min(kTcChunkStages, n_stages - t.st0);
+                    t.sb = s;
+                    while (s < se && plan.tcs[s].stage < t.st0 + t.n_stages)
+                        s++;
+                    t.se = s;
                     plan.tct.push_back(t);
+                }
             }
     }
     std::stable_sort(plan.tct.begin(), plan.tct.end(),

@@ -135,19 +135,31 @@ __device__ __forceinline__ void split_tf32(double x, uint32_t &hi, uint32_t &lo)
     lo = to_tf32((float)(x - (double)__uint_as_float(hi)));
 }
 
+// per-stage copy of the segments and contribution fields staging needs
+struct StageSeg {
+    const double *A;  // operator block of the contribution
+    const float *W;   // work matrix of the contribution
+    double alpha;
+    int32_t row0, m1, lda1, ta1, col0, n1, kb, koff, kl, pad;
+};
+
 __global__ void __launch_bounds__(kThreads, 1)
-tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcSeg *__restrict__ segs,
-                 const Contrib *__restrict__ contribs, const Region *__restrict__ regions,
-                 const WorkDesc *__restrict__ works, const double *__restrict__ ops,
-                 const float *__restrict__ work, double *__restrict__ sigma, double scale, int *err) {
+tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ tiles,
+                 const TcSeg *__restrict__ segs, const Contrib *__restrict__ contribs,
+                 const Region *__restrict__ regions, const WorkDesc *__restrict__ works,
+                 const double *__restrict__ ops, const float *__restrict__ work,
+                 double *__restrict__ sigma, float *__restrict__ part, double scale, int *err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte aligned base for the operand buffers
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *mbar = (uint64_t *)(smem + 2 * kBufBytes);      // [0], [1]: stage buffers
     uint32_t *tmem_slot = (uint32_t *)(smem + 2 * kBufBytes + 64);
+    __shared__ StageSeg sseg[kTcStageK];
+    __shared__ int8_t col_seg[kTcStageK];   // stage column -> sseg index (-1: zero column)
+    __shared__ int8_t col_kk[kTcStageK];    // stage column -> k offset inside the segment
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const TcTask tk = tasks[blockIdx.x];
-    const Region rg = regions[tk.g];
+    const TcTile tl = tiles[tk.tile];
+    const Region rg = regions[tl.g];
 
     if (tid == 0) {
         mbar_init(smem_u32(&mbar[0]), 1);
@@ -163,96 +175,93 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcSeg *__restrict__ seg
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = make_idesc(tk.n);
-    bool ok = true;
+    const uint32_t idesc = make_idesc(tl.n);
     int issued = 0;      // stages whose MMAs were committed
     int64_t sp = tk.sb;  // segment cursor (segments are ordered by stage)
-    for (int st = 0; st < tk.n_stages; st++) {
-        const int b = st & 1;
+    for (int ls = 0; ls < tk.n_stages; ls++) {
+        const int st = tk.st0 + ls;
+        const int b = ls & 1;
         unsigned char *buf = smem + b * kBufBytes;
-        // buffer b was last read by the MMAs of stage st-2 (CTA-uniform outcome)
-        if (st >= 2) {
+        // buffer b was last read by the MMAs of local stage ls-2 (CTA-uniform outcome)
+        if (ls >= 2) {
             const int good = __syncthreads_and(
-                mbar_wait(smem_u32(&mbar[b]), (uint32_t)(((st >> 1) - 1) & 1)) ? 1 : 0);
+                mbar_wait(smem_u32(&mbar[b]), (uint32_t)(((ls >> 1) - 1) & 1)) ? 1 : 0);
             if (!good) {
-                ok = false;
                 if (tid == 0)
                     atomicExch(err, 1);
                 break;
             }
         }
+        // ---- this stage's segment table
+        if (tid < kTcStageK)
+            col_seg[tid] = -1;
+        __syncthreads();
+        const int64_t si = sp + tid;
+        const bool mine = tid < kTcStageK && si < tk.se && segs[si].stage == st;
+        if (mine) {
+            const TcSeg sg = segs[si];
+            const Contrib c = contribs[sg.c];
+            StageSeg x;
+            x.A = ops + c.a1;
+            x.W = work + works[c.u].woff;
+            x.alpha = c.alpha;
+            x.row0 = c.row0, x.m1 = c.m1, x.lda1 = c.lda1, x.ta1 = c.ta1;
+            x.col0 = c.col0, x.n1 = c.n1, x.kb = sg.kb, x.koff = sg.koff, x.kl = sg.kl;
+            sseg[tid] = x;
+            for (int kk = 0; kk < sg.kl; kk++)
+                col_seg[sg.koff + kk] = (int8_t)tid, col_kk[sg.koff + kk] = (int8_t)kk;
+        }
+        sp += __syncthreads_count(mine ? 1 : 0);
         // ---- stage the A slab: thread tid owns tile row tid
         {
-            uint32_t hi[kTcStageK], lo[kTcStageK];
-#pragma unroll
-            for (int k = 0; k < kTcStageK; k++)
-                hi[k] = 0u, lo[k] = 0u;
-            const int row = tk.row0 + tid;
-            for (int64_t s = sp; s < tk.se && segs[s].stage == st; s++) {
-                const TcSeg sg = segs[s];
-                const Contrib c = contribs[sg.c];
-                const int ar = row - c.row0;
-                if (ar < 0 || ar >= c.m1)
-                    continue;
-                const double *A = ops + c.a1;
-#pragma unroll 4
-                for (int kk = 0; kk < sg.kl; kk++) {
-                    const int k = sg.kb + kk;
-                    const double a = c.alpha * (c.ta1 ? A[(uint64_t)k * c.lda1 + ar]
-                                                      : A[(uint64_t)ar * c.lda1 + k]);
-                    uint32_t h, l;
-                    split_tf32(a, h, l);
-                    // koff + kk < kTcStageK by construction; select into registers
-#pragma unroll
-                    for (int q = 0; q < kTcStageK; q++)
-                        if (q == sg.koff + kk)
-                            hi[q] = h, lo[q] = l;
-                }
-            }
+            const int row = tl.row0 + tid;
 #pragma unroll
             for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
+                uint32_t h[4], l[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    h[j] = 0u, l[j] = 0u;
+                    const int q = 4 * k4 + j, si2 = col_seg[q];
+                    if (si2 >= 0) {
+                        const StageSeg &x = sseg[si2];
+                        const int ar = row - x.row0;
+                        if (ar >= 0 && ar < x.m1) {
+                            const int k = x.kb + col_kk[q];
+                            const double a = x.alpha * (x.ta1 ? x.A[(uint64_t)k * x.lda1 + ar]
+                                                              : x.A[(uint64_t)ar * x.lda1 + k]);
+                            split_tf32(a, h[j], l[j]);
+                        }
+                    }
+                }
                 const uint32_t off = kmajor_off(tid, 4 * k4);
-                *(uint4 *)(buf + off) = make_uint4(hi[4 * k4], hi[4 * k4 + 1], hi[4 * k4 + 2], hi[4 * k4 + 3]);
-                *(uint4 *)(buf + kABytes + off) =
-                    make_uint4(lo[4 * k4], lo[4 * k4 + 1], lo[4 * k4 + 2], lo[4 * k4 + 3]);
+                *(uint4 *)(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                *(uint4 *)(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
             }
         }
-        // ---- stage the B slab: B[n][k] = W(k, n), threads own columns tid, tid + 128
-        for (int nn = tid; nn < tk.n; nn += kThreads) {
-            uint32_t hi[kTcStageK], lo[kTcStageK];
-#pragma unroll
-            for (int k = 0; k < kTcStageK; k++)
-                hi[k] = 0u, lo[k] = 0u;
-            const int col = tk.col0 + nn;
-            for (int64_t s = sp; s < tk.se && segs[s].stage == st; s++) {
-                const TcSeg sg = segs[s];
-                const Contrib c = contribs[sg.c];
-                const int wc = col - c.col0;
-                if (wc < 0 || wc >= c.n1)
-                    continue;
-                const float *W = work + works[c.u].woff;
-#pragma unroll 4
-                for (int kk = 0; kk < sg.kl; kk++) {
-                    const float w = W[(uint64_t)(sg.kb + kk) * c.n1 + wc];
-                    uint32_t h, l;
-                    split_tf32((double)w, h, l);
-#pragma unroll
-                    for (int q = 0; q < kTcStageK; q++)
-                        if (q == sg.koff + kk)
-                            hi[q] = h, lo[q] = l;
-                }
-            }
+        // ---- stage the B slab: B[n][k] = W(k, n); threads own columns tid, tid + 128
+        for (int nn = tid; nn < tl.n; nn += kThreads) {
+            const int col = tl.col0 + nn;
 #pragma unroll
             for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
+                uint32_t h[4], l[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    h[j] = 0u, l[j] = 0u;
+                    const int q = 4 * k4 + j, si2 = col_seg[q];
+                    if (si2 >= 0) {
+                        const StageSeg &x = sseg[si2];
+                        const int wc = col - x.col0;
+                        if (wc >= 0 && wc < x.n1) {
+                            const float w = x.W[(uint64_t)(x.kb + col_kk[q]) * x.n1 + wc];
+                            split_tf32((double)w, h[j], l[j]);
+                        }
+                    }
+                }
                 const uint32_t off = kmajor_off(nn, 4 * k4);
-                *(uint4 *)(buf + 2 * kABytes + off) =
-                    make_uint4(hi[4 * k4], hi[4 * k4 + 1], hi[4 * k4 + 2], hi[4 * k4 + 3]);
-                *(uint4 *)(buf + 2 * kABytes + kBBytes + off) =
-                    make_uint4(lo[4 * k4], lo[4 * k4 + 1], lo[4 * k4 + 2], lo[4 * k4 + 3]);
+                *(uint4 *)(buf + 2 * kABytes + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                *(uint4 *)(buf + 2 * kABytes + kBBytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
             }
         }
-        while (sp < tk.se && segs[sp].stage == st)
-            sp++;
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -263,15 +272,14 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcSeg *__restrict__ seg
 #pragma unroll
             for (int h = 0; h < kTcStageK / 8; h++) {
                 const uint32_t ko = h * 2 * kLBO;  // K = 8 = two core matrices
-                const uint32_t acc0 = (st > 0 || h > 0) ? 1u : 0u;
+                const uint32_t acc0 = (ls > 0 || h > 0) ? 1u : 0u;
                 mma_tf32(tmem, make_desc(a_hi + ko), make_desc(b_hi + ko), idesc, acc0);
                 mma_tf32(tmem, make_desc(a_hi + ko), make_desc(b_lo + ko), idesc, 1u);
                 mma_tf32(tmem, make_desc(a_lo + ko), make_desc(b_hi + ko), idesc, 1u);
             }
             mma_commit(smem_u32(&mbar[b]));
         }
-        issued = st + 1;
-        __syncthreads();
+        issued = ls + 1;
     }
     // wait for the last issued stage's MMAs (its commit covers all earlier ones)
     const int last = issued - 1;
@@ -283,18 +291,24 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcSeg *__restrict__ seg
             atomicExch(err, 1);
     }
     tc_fence_after();
-    if (ok && done) {
+    if (done && issued == tk.n_stages) {
         // ---- epilogue: warp w holds TMEM lanes [32w, 32w + 32) = tile rows
-        const int row = tk.row0 + warp * 32 + lane;
+        const int trow = warp * 32 + lane;
+        const int row = tl.row0 + trow;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c16 = 0; c16 < tk.n; c16 += 16) {
+        float *prow = tl.part >= 0 ? part + tl.part + ((int64_t)tk.chunk * 128 + trow) * tl.n : nullptr;
+        for (int c16 = 0; c16 < tl.n; c16 += 16) {
             float v[16];
             tmem_ld16(tbase + (uint32_t)c16, v);
-            if (row < rg.rows) {
+            if (prow != nullptr) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 4)
+                    *(float4 *)(prow + c16 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            } else if (trow < tl.rows) {
                 const uint64_t rowaddr = rg.base + (uint64_t)row * rg.ld;
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
-                    const int col = tk.col0 + c16 + j;
+                    const int col = tl.col0 + c16 + j;
                     const uint64_t a = rowaddr + (uint64_t)col;
                     if (col < rg.cols && a >= rg.lo && a < rg.hi)
                         sigma[a] += scale * (double)v[j];
@@ -306,6 +320,29 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcSeg *__restrict__ seg
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kMaxN));
+}
+
+// split-K reduction: sigma += scale * sum over chunks (fixed order) of the partial tiles
+__global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restrict__ multi,
+                                                        const TcTile *__restrict__ tiles,
+                                                        const Region *__restrict__ regions,
+                                                        const float *__restrict__ part,
+                                                        double *__restrict__ sigma, double scale) {
+    const TcTile tl = tiles[multi[blockIdx.x]];
+    const Region rg = regions[tl.g];
+    const int64_t plane = (int64_t)128 * tl.n;
+    for (int e = threadIdx.x; e < tl.rows * tl.n; e += blockDim.x) {
+        const int r = e / tl.n, cc = e % tl.n;
+        const int col = tl.col0 + cc;
+        const uint64_t a = rg.base + (uint64_t)(tl.row0 + r) * rg.ld + (uint64_t)col;
+        if (col >= rg.cols || a < rg.lo || a >= rg.hi)
+            continue;
+        double s = 0.0;
+        const float *p = part + tl.part + (int64_t)r * tl.n + cc;
+        for (int ch = 0; ch < tl.n_chunks; ch++)
+            s += (double)p[ch * plane];
+        sigma[a] += scale * s;
+    }
 }
 
 } // namespace
@@ -323,7 +360,12 @@ cudaError_t launch_tc_phase2(const DevicePlan &p, const double *ops, const float
         attr_set = true;
     }
     tc_phase2_kernel<<<(unsigned)p.n_tct, kThreads, kSmemBytes, s>>>(
-        p.tct, p.tcs, p.contribs, p.regions, p.works, ops, work, sigma, scale, err);
+        p.tct, p.tctile, p.tcs, p.contribs, p.regions, p.works, ops, work, sigma, p.tc_part, scale, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || p.n_tc_multi == 0)
+        return e;
+    tc_reduce_kernel<<<(unsigned)p.n_tc_multi, 256, 0, s>>>(p.tc_multi, p.tctile, p.regions, p.tc_part,
+                                                            sigma, scale);
     return cudaGetLastError();
 }
 
