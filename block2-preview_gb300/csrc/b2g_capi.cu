@@ -34,6 +34,7 @@ static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
     cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi), cudaFree(p.tc_part);
+    cudaFree(p.t2multi), cudaFree(p.t2_part);
     p = DevicePlan();
 }
 
@@ -139,8 +140,15 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
         (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
         (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)) ||
-        (rc = upload(hp.tctile, &p.tctile, s)) || (rc = upload(hp.tc_multi, &p.tc_multi, s)))
+        (rc = upload(hp.tctile, &p.tctile, s)) || (rc = upload(hp.tc_multi, &p.tc_multi, s)) ||
+        (rc = upload(hp.t2multi, &p.t2multi, s)))
         return bail(rc);
+    p.n_t2multi = (int64_t)hp.t2multi.size();
+    if (hp.t2_part_tiles &&
+        cudaMalloc(&p.t2_part, sizeof(double) * 4 * 256 * hp.t2_part_tiles) != cudaSuccess) {
+        p.t2_part = nullptr;
+        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the phase-2 partial tiles"));
+    }
     if (hp.tc_part_size && cudaMalloc(&p.tc_part, sizeof(float) * hp.tc_part_size) != cudaSuccess) {
         p.tc_part = nullptr;
         return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the split-K partial tiles"));
@@ -188,7 +196,7 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaSetDevice(h->ctx->device);
     cudaStreamSynchronize(h->ctx->stream);
     free_plan(h->plan);
-    cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->work);
+    cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
     cudaFree(h->psi_stage), cudaFree(h->sigma_stage), cudaFree(h->err);
     for (auto &e : h->ev)
         if (e)
@@ -287,14 +295,22 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
             }
             B2G_CUDA_TRY(launch_to_float(h->ops, h->ops32, h->ops_size, s));
         }
+        if (h->psi32 == nullptr && h->psi_size) {
+            if (cudaMalloc(&h->psi32, sizeof(float) * h->psi_size) != cudaSuccess) {
+                h->psi32 = nullptr;
+                return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the float psi copy");
+            }
+        }
         float *w32 = (float *)h->work;
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-        B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, psi, w32, s));
+        // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
+        B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size, s));
+        B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
         if (form == B2G_TF32X3)
-            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops, w32, sigma, scale, h->err, s));
+            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops32, w32, sigma, scale, h->err, s));
         else
             B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, scale, s));
         if (h->timing)

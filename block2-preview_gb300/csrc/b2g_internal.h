@@ -50,9 +50,17 @@ struct Region {
 struct Task1 {          // phase 1: one row of one work product
     int32_t u, r;
 };
-struct Task2 {          // phase 2: rows [4*rb, 4*rb+4) x cols [col0, col0+256) of a region
-    int32_t g, rb, col0, pad;
-    int64_t lb, le;     // contribution list range
+// phase 2: rows [4*rb, 4*rb+4) x cols [col0, col0+256) of a region, one chunk of
+// its contribution list (split-K over chunks of at most kSimtChunkK k-steps)
+constexpr int kSimtChunkK = 768;
+struct Task2 {
+    int32_t g, rb, col0, chunk;
+    int64_t lb, le;     // contribution list range of this chunk
+    int64_t part;       // partial-tile slot (in 4 x 256 tiles) of chunk 0, -1: single chunk
+};
+struct Tile2 {          // a phase-2 tile split over several chunks (reduced after)
+    int32_t g, rb, col0, n_chunks;
+    int64_t part;
 };
 
 // Tensor-core phase 2: the contributions of a 128-row x N-column tile of a
@@ -86,6 +94,8 @@ struct HostPlan {
     std::vector<Region> regions;
     std::vector<Task1> t1;
     std::vector<Task2> t2;
+    std::vector<Tile2> t2multi;
+    uint64_t t2_part_tiles = 0;     // 4 x 256 partial tiles of split phase-2 tiles
     std::vector<int32_t> lists;
     std::vector<TcTask> tct;
     std::vector<TcSeg> tcs;
@@ -105,6 +115,9 @@ struct DevicePlan {
     Region *regions = nullptr;
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;
+    Tile2 *t2multi = nullptr;
+    void *t2_part = nullptr;        // partial tiles (double or float, sized for double)
+    int64_t n_t2multi = 0;
     int32_t *lists = nullptr;
     TcTask *tct = nullptr;
     TcSeg *tcs = nullptr;
@@ -117,12 +130,12 @@ struct DevicePlan {
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
 // bounded wait gives up
-cudaError_t launch_tc_phase2(const DevicePlan &p, const double *ops, const float *work,
+cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops32, const float *work,
                              double *sigma, double scale, int *err, cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>
-cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const double *psi, T *work,
+cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const T *psi, T *work,
                                cudaStream_t s);
 template <typename T>
 cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work, double *sigma,
@@ -144,6 +157,7 @@ struct b2g_heff {
     b2g::DevicePlan plan;
     double *ops = nullptr;
     float *ops32 = nullptr;  // operators rounded to float (made on the first reduced-precision apply)
+    float *psi32 = nullptr;  // psi rounded to float (per reduced-precision apply)
     double *work = nullptr;
     double *psi_stage = nullptr, *sigma_stage = nullptr; // device staging for the host entry
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;

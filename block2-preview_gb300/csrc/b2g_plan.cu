@@ -200,12 +200,33 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 auto &l = tl[(size_t)rb * ncs + cs];
                 if (l.empty())
                     continue;
-                Task2 t;
-                t.g = g, t.rb = rb, t.col0 = cs * kColsPerTask, t.pad = 0;
-                t.lb = (int64_t)plan.lists.size();
+                // split the list into chunks of at most kSimtChunkK k-steps
+                const int64_t lb = (int64_t)plan.lists.size();
                 plan.lists.insert(plan.lists.end(), l.begin(), l.end());
-                t.le = (int64_t)plan.lists.size();
-                plan.t2.push_back(t);
+                std::vector<int64_t> cuts{lb};
+                int64_t acc = 0;
+                for (size_t q = 0; q < l.size(); q++) {
+                    const int32_t k = plan.contribs[l[q]].k1;
+                    if (acc > 0 && acc + k > kSimtChunkK) {
+                        cuts.push_back(lb + (int64_t)q);
+                        acc = 0;
+                    }
+                    acc += k;
+                }
+                cuts.push_back(lb + (int64_t)l.size());
+                const int32_t nch = (int32_t)cuts.size() - 1;
+                int64_t part = -1;
+                if (nch > 1) {
+                    part = (int64_t)plan.t2_part_tiles;
+                    plan.t2_part_tiles += (uint64_t)nch;
+                    plan.t2multi.push_back(Tile2{g, rb, cs * kColsPerTask, nch, part});
+                }
+                for (int32_t ch = 0; ch < nch; ch++) {
+                    Task2 t;
+                    t.g = g, t.rb = rb, t.col0 = cs * kColsPerTask, t.chunk = ch;
+                    t.lb = cuts[ch], t.le = cuts[ch + 1], t.part = part;
+                    plan.t2.push_back(t);
+                }
             }
         // tensor-core tiles: 128 rows x up to 256 columns, contributions packed
         // along K into stages of kTcStageK columns

@@ -27,7 +27,7 @@ template <typename T>
 __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ works,
                                                    const Task1 *__restrict__ tasks, int64_t n_tasks,
                                                    const T *__restrict__ ops,
-                                                   const double *__restrict__ psi,
+                                                   const T *__restrict__ psi,
                                                    T *__restrict__ work) {
     const int64_t t = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
         return;
     const Task1 tk = tasks[t];
     const WorkDesc wd = works[tk.u];
-    const double *prow = psi + wd.a0 + (uint64_t)tk.r * wd.lda0;
+    const T *prow = psi + wd.a0 + (uint64_t)tk.r * wd.lda0;
     const T *B = ops + wd.b0;
     T *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
     for (int cbase = 0; cbase < wd.n0; cbase += 32 * kLanesCols) {
@@ -73,12 +73,14 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
     }
 }
 
-// Phase 2: one CTA per task (4 rows x 256 columns of one sigma region), one
-// warp per row, lane -> columns lane + 32 j.  The task owns its cells: it
-// loops over its contribution list (pairs whose row window covers its rows)
-// and adds alpha * sum_k A(r - row0, k) * W_u(k, c - col0) in a fixed order,
-// then writes sigma += scale * acc once, only for cells some pair writes
-// (no atomics, deterministic).
+// Phase 2: one CTA per task (4 rows x 256 columns of one sigma region, one
+// chunk of its contribution list), one warp per row, lane -> columns
+// lane + 32 j.  The task loops over its chunk (pairs whose row window covers
+// its rows) and adds alpha * sum_k A(r - row0, k) * W_u(k, c - col0) in a
+// fixed order.  A tile with a single chunk owns its cells and writes
+// sigma += scale * acc directly; otherwise the chunk stores its partial tile
+// and simt_reduce sums the chunks in order.  Only cells inside the region's
+// write span are stored (no atomics, deterministic).
 template <typename T>
 __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tasks,
                                                    const int32_t *__restrict__ lists,
@@ -87,18 +89,19 @@ __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tas
                                                    const WorkDesc *__restrict__ works,
                                                    const T *__restrict__ ops,
                                                    const T *__restrict__ work,
-                                                   double *__restrict__ sigma, double scale) {
+                                                   double *__restrict__ sigma, T *__restrict__ part,
+                                                   double scale) {
     const Task2 tk = tasks[blockIdx.x];
     const Region rg = regions[tk.g];
     const int lane = threadIdx.x & 31;
-    const int r = tk.rb * 4 + (threadIdx.x >> 5);
+    const int wr = threadIdx.x >> 5;
+    const int r = tk.rb * 4 + wr;
     if (r >= rg.rows)
         return;
     T acc[kLanesCols];
-    bool cov[kLanesCols];  // cell written by at least one pair (only those are stored)
 #pragma unroll
     for (int j = 0; j < kLanesCols; j++)
-        acc[j] = T(0), cov[j] = false;
+        acc[j] = T(0);
     for (int64_t li = tk.lb; li < tk.le; li++) {
         const Contrib c = contribs[lists[li]];
         const int ar = r - c.row0;
@@ -111,7 +114,6 @@ __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tas
         for (int j = 0; j < kLanesCols; j++) {
             const int col = tk.col0 + lane + 32 * j - c.col0;
             cc[j] = (col >= 0 && col < c.n1) ? col : -1;
-            cov[j] = cov[j] || cc[j] >= 0;
         }
         const T alpha = (T)c.alpha;
         for (int k = 0; k < c.k1; k++) {
@@ -124,11 +126,46 @@ __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tas
                     acc[j] = fma(a, __ldg(wrow + cc[j]), acc[j]);
         }
     }
-    double *srow = sigma + rg.base + (uint64_t)r * rg.ld;
+    if (tk.part >= 0) {
+        T *prow = part + ((tk.part + tk.chunk) * 4 + wr) * (int64_t)(32 * kLanesCols);
 #pragma unroll
-    for (int j = 0; j < kLanesCols; j++)
-        if (cov[j])
-            srow[tk.col0 + lane + 32 * j] += scale * (double)acc[j];
+        for (int j = 0; j < kLanesCols; j++)
+            prow[lane + 32 * j] = acc[j];
+        return;
+    }
+    const uint64_t rowaddr = rg.base + (uint64_t)r * rg.ld;
+#pragma unroll
+    for (int j = 0; j < kLanesCols; j++) {
+        const int col = tk.col0 + lane + 32 * j;
+        const uint64_t a = rowaddr + (uint64_t)col;
+        if (col < rg.cols && a >= rg.lo && a < rg.hi)
+            sigma[a] += scale * (double)acc[j];
+    }
+}
+
+// split-K reduction of phase 2: sigma += scale * sum over chunks (in order)
+template <typename T>
+__global__ void __launch_bounds__(128) simt_reduce(const Tile2 *__restrict__ tiles,
+                                                   const Region *__restrict__ regions,
+                                                   const T *__restrict__ part,
+                                                   double *__restrict__ sigma, double scale) {
+    const Tile2 tl = tiles[blockIdx.x];
+    const Region rg = regions[tl.g];
+    const int lane = threadIdx.x & 31, wr = threadIdx.x >> 5;
+    const int r = tl.rb * 4 + wr;
+    if (r >= rg.rows)
+        return;
+    const uint64_t rowaddr = rg.base + (uint64_t)r * rg.ld;
+    for (int j = 0; j < kLanesCols; j++) {
+        const int col = tl.col0 + lane + 32 * j;
+        const uint64_t a = rowaddr + (uint64_t)col;
+        if (col >= rg.cols || a < rg.lo || a >= rg.hi)
+            continue;
+        double s = 0.0;
+        for (int ch = 0; ch < tl.n_chunks; ch++)
+            s += (double)part[((tl.part + ch) * 4 + wr) * (int64_t)(32 * kLanesCols) + lane + 32 * j];
+        sigma[a] += scale * s;
+    }
 }
 
 // FP64 ceiling probe: 8 independent FMA chains per thread, no memory traffic
@@ -189,7 +226,7 @@ cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t 
 }
 
 template <typename T>
-cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const double *psi, T *work,
+cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const T *psi, T *work,
                                cudaStream_t s) {
     if (p.n_t1 == 0)
         return cudaSuccess;
@@ -203,14 +240,19 @@ cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work,
                                double scale, cudaStream_t s) {
     if (p.n_t2 == 0)
         return cudaSuccess;
+    T *part = (T *)p.t2_part;
     simt_phase2<T><<<(unsigned)p.n_t2, 128, 0, s>>>(p.t2, p.lists, p.contribs, p.regions, p.works,
-                                                    ops, work, sigma, scale);
+                                                    ops, work, sigma, part, scale);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || p.n_t2multi == 0)
+        return e;
+    simt_reduce<T><<<(unsigned)p.n_t2multi, 128, 0, s>>>(p.t2multi, p.regions, part, sigma, scale);
     return cudaGetLastError();
 }
 
 template cudaError_t launch_simt_phase1<double>(const DevicePlan &, const double *, const double *,
                                                 double *, cudaStream_t);
-template cudaError_t launch_simt_phase1<float>(const DevicePlan &, const float *, const double *,
+template cudaError_t launch_simt_phase1<float>(const DevicePlan &, const float *, const float *,
                                                float *, cudaStream_t);
 template cudaError_t launch_simt_phase2<double>(const DevicePlan &, const double *, const double *,
                                                 double *, double, cudaStream_t);

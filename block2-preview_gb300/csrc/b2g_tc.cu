@@ -5,8 +5,9 @@
 // (N <= 256, multiple of 16).  The tile's GEMM1 contributions
 // alpha * op(L) (rows x k1) * W (k1 x cols) are concatenated along K and
 // packed into stages of kTcStageK = 16 columns.  Per stage, all 128 threads
-// stage the A slab (128 x 16, alpha folded in, FP64 operators split into a
-// TF32 "hi" part and a TF32 "lo" remainder) and the B slab (N x 16 from W)
+// stage the A slab (128 x 16, alpha folded in, operators (FP32 copy) split
+// into a TF32 "hi" part and a TF32 "lo" remainder) and the B slab (N x 16
+// from W)
 // into shared memory in the canonical no-swizzle K-major layout (8-row x
 // 16-byte core matrices, LBO = 128 B along K, SBO = 512 B along M/N), then
 // one elected thread issues, per K = 8 half, the three products
@@ -129,25 +130,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
         v[i] = __uint_as_float(r[i]);
 }
 
-// split x into TF32 hi + TF32 lo (x - hi), stored as raw fp32 bit patterns
-__device__ __forceinline__ void split_tf32(double x, uint32_t &hi, uint32_t &lo) {
-    hi = to_tf32((float)x);
-    lo = to_tf32((float)(x - (double)__uint_as_float(hi)));
+// split x into TF32 hi + TF32 lo (x - hi, exact in FP32), raw fp32 bit patterns;
+// FP32 arithmetic only (FP64 work would run on GB300's narrow FP64 pipe)
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+    hi = to_tf32(x);
+    lo = to_tf32(x - __uint_as_float(hi));
 }
 
 // per-stage copy of the segments and contribution fields staging needs
 struct StageSeg {
-    const double *A;  // operator block of the contribution
+    const float *A;   // operator block of the contribution (FP32 copy of the blob)
     const float *W;   // work matrix of the contribution
-    double alpha;
-    int32_t row0, m1, lda1, ta1, col0, n1, kb, koff, kl, pad;
+    float alpha;
+    int32_t row0, m1, lda1, ta1, col0, n1, kb, koff, kl;
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
 tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ tiles,
                  const TcSeg *__restrict__ segs, const Contrib *__restrict__ contribs,
                  const Region *__restrict__ regions, const WorkDesc *__restrict__ works,
-                 const double *__restrict__ ops, const float *__restrict__ work,
+                 const float *__restrict__ ops, const float *__restrict__ work,
                  double *__restrict__ sigma, float *__restrict__ part, double scale, int *err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -204,7 +206,7 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
             StageSeg x;
             x.A = ops + c.a1;
             x.W = work + works[c.u].woff;
-            x.alpha = c.alpha;
+            x.alpha = (float)c.alpha;
             x.row0 = c.row0, x.m1 = c.m1, x.lda1 = c.lda1, x.ta1 = c.ta1;
             x.col0 = c.col0, x.n1 = c.n1, x.kb = sg.kb, x.koff = sg.koff, x.kl = sg.kl;
             sseg[tid] = x;
@@ -227,8 +229,8 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
                         const int ar = row - x.row0;
                         if (ar >= 0 && ar < x.m1) {
                             const int k = x.kb + col_kk[q];
-                            const double a = x.alpha * (x.ta1 ? x.A[(uint64_t)k * x.lda1 + ar]
-                                                              : x.A[(uint64_t)ar * x.lda1 + k]);
+                            const float a = x.alpha * (x.ta1 ? x.A[(uint64_t)k * x.lda1 + ar]
+                                                             : x.A[(uint64_t)ar * x.lda1 + k]);
                             split_tf32(a, h[j], l[j]);
                         }
                     }
@@ -253,7 +255,7 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
                         const int wc = col - x.col0;
                         if (wc >= 0 && wc < x.n1) {
                             const float w = x.W[(uint64_t)(x.kb + col_kk[q]) * x.n1 + wc];
-                            split_tf32((double)w, h[j], l[j]);
+                            split_tf32(w, h[j], l[j]);
                         }
                     }
                 }
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restric
 
 } // namespace
 
-cudaError_t launch_tc_phase2(const DevicePlan &p, const double *ops, const float *work,
+cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops, const float *work,
                              double *sigma, double scale, int *err, cudaStream_t s) {
     if (p.n_tct == 0)
         return cudaSuccess;
