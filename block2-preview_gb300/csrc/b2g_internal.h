@@ -65,12 +65,15 @@ struct Tile2 {          // a phase-2 tile split over several chunks (reduced aft
 
 // Tensor-core phase 2: the contributions of a 128-row x N-column tile of a
 // region are cut into K segments packed into stages of kTcStageK columns
-// (zero-padded).  The stage list of a tile is split into chunks of at most
-// kTcChunkStages stages (split-K); one CTA per chunk.  A tile with one chunk
-// updates sigma directly; otherwise each chunk stores a partial tile and a
-// reduction kernel sums the partials in chunk order (deterministic).
+// (zero-padded).  The stage list of a tile is split into chunks (split-K;
+// chunk length chosen so the whole product has about kTcTargetChunks
+// chunks, and at most kTcMaxSegs segments per chunk); one CTA per chunk.  A
+// tile with one chunk updates sigma directly; otherwise each chunk stores a
+// partial tile and a reduction kernel sums the partials in chunk order
+// (deterministic).
 constexpr int kTcStageK = 16;
-constexpr int kTcChunkStages = 64;
+constexpr int kTcMaxSegs = 384;
+constexpr int kTcTargetChunks = 8 * 152;
 struct TcTile {
     int32_t g, row0, col0, n;   // region, tile origin, tile width (multiple of 16, <= 256)
     int32_t rows, n_chunks;     // valid rows (<= 128), chunks
@@ -81,11 +84,16 @@ struct TcTask {                 // one chunk of one tile
     int64_t sb, se;             // segment range
     int32_t st0, n_stages;      // first stage index (tile numbering), stages in this chunk
 };
+// one K segment of one contribution, with everything staging needs (no
+// dependent lookups on the device)
 struct TcSeg {
-    int32_t c;                  // contribution index
+    uint64_t a;                 // offset of the left operator block (in the FP32 operator copy)
+    uint64_t w;                 // offset of the work matrix W_u (floats)
+    float alpha;                // alpha0 * alpha1
+    int32_t lda1, row0, m1, col0, n1;
     int16_t kb, kl;             // k range [kb, kb + kl) of the contribution
+    int8_t koff, ta1, pad0, pad1;
     int32_t stage;              // stage index within the tile
-    int32_t koff;               // column offset inside the stage
 };
 
 struct HostPlan {

@@ -243,8 +243,11 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                     for (int32_t kb = 0; kb < c.k1;) {
                         const int32_t take = std::min(c.k1 - kb, kTcStageK - koff);
                         TcSeg sg;
-                        sg.c = (int32_t)q, sg.kb = (int16_t)kb, sg.kl = (int16_t)take;
-                        sg.stage = stage, sg.koff = koff;
+                        sg.a = c.a1, sg.w = plan.works[c.u].woff, sg.alpha = (float)c.alpha;
+                        sg.lda1 = c.lda1, sg.row0 = c.row0, sg.m1 = c.m1, sg.col0 = c.col0, sg.n1 = c.n1;
+                        sg.kb = (int16_t)kb, sg.kl = (int16_t)take;
+                        sg.koff = (int8_t)koff, sg.ta1 = (int8_t)c.ta1, sg.pad0 = 0, sg.pad1 = 0;
+                        sg.stage = stage;
                         plan.tcs.push_back(sg);
                         kb += take, koff += take;
                         if (koff == kTcStageK)
@@ -258,28 +261,53 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 TcTile tl;
                 tl.g = g, tl.row0 = r0, tl.col0 = c0, tl.n = nt;
                 tl.rows = std::min(128, rows - r0);
-                tl.n_chunks = (n_stages + kTcChunkStages - 1) / kTcChunkStages;
-                tl.part = -1;
-                const int32_t tile = (int32_t)plan.tctile.size();
-                if (tl.n_chunks > 1) {
-                    tl.part = (int64_t)plan.tc_part_size;
-                    plan.tc_part_size += (uint64_t)tl.n_chunks * 128 * nt;
-                    plan.tc_multi.push_back(tile);
-                }
+                tl.n_chunks = n_stages;  // stage count until the chunking pass below
+                tl.part = sb;            // segment start until the chunking pass below
                 plan.tctile.push_back(tl);
-                int64_t s = sb;
-                for (int32_t ch = 0; ch < tl.n_chunks; ch++) {
-                    TcTask t;
-                    t.tile = tile, t.chunk = ch;
-                    t.st0 = ch * kTcChunkStages;
-                    t.n_stages = std::min(kTcChunkStages, n_stages - t.st0);
-                    t.sb = s;
-                    while (s < se && plan.tcs[s].stage < t.st0 + t.n_stages)
-                        s++;
-                    t.se = s;
-                    plan.tct.push_back(t);
-                }
             }
+    }
+    // ---- split-K chunking of the tensor-core tiles
+    {
+        int64_t total_stages = 0;
+        for (auto &tl : plan.tctile)
+            total_stages += tl.n_chunks;
+        const int32_t chunk_stages = (int32_t)std::min<int64_t>(
+            kTcMaxSegs, std::max<int64_t>(16, (total_stages + kTcTargetChunks - 1) / kTcTargetChunks));
+        for (int32_t tile = 0; tile < (int32_t)plan.tctile.size(); tile++) {
+            TcTile &tl = plan.tctile[tile];
+            const int32_t n_stages = tl.n_chunks;
+            const int64_t sb = tl.part;
+            const int64_t se = tile + 1 < (int32_t)plan.tctile.size() ? plan.tctile[tile + 1].part
+                                                                      : (int64_t)plan.tcs.size();
+            std::vector<TcTask> chunks;
+            int64_t s = sb;
+            int32_t st = 0;
+            while (st < n_stages) {
+                TcTask t;
+                t.tile = tile, t.chunk = (int32_t)chunks.size(), t.st0 = st, t.sb = s;
+                // up to chunk_stages stages and kTcMaxSegs segments, whole stages only
+                int32_t ns = 0;
+                while (st + ns < n_stages && ns < chunk_stages) {
+                    int64_t e = s;
+                    while (e < se && plan.tcs[e].stage == st + ns)
+                        e++;
+                    if (ns > 0 && e - t.sb > kTcMaxSegs)
+                        break;
+                    s = e, ns++;
+                }
+                t.n_stages = ns, t.se = s;
+                st += ns;
+                chunks.push_back(t);
+            }
+            tl.n_chunks = (int32_t)chunks.size();
+            tl.part = -1;
+            if (tl.n_chunks > 1) {
+                tl.part = (int64_t)plan.tc_part_size;
+                plan.tc_part_size += (uint64_t)tl.n_chunks * tl.rows * tl.n;
+                plan.tc_multi.push_back(tile);
+            }
+            plan.tct.insert(plan.tct.end(), chunks.begin(), chunks.end());
+        }
     }
     std::stable_sort(plan.tct.begin(), plan.tct.end(),
                      [](const TcTask &a, const TcTask &b) { return a.n_stages > b.n_stages; });

@@ -30,15 +30,18 @@ namespace b2g {
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;                          // 8 warps
+constexpr int kProducers = 7;                          // warps 0..6 stage operands
+constexpr int kMmaWarp = 7;                            // lane 0 of warp 7 issues the MMAs
 constexpr int kMaxN = 256;
-constexpr uint32_t kABytes = 128 * kTcStageK * 4;      // 8 KB per split part
-constexpr uint32_t kBBytes = kMaxN * kTcStageK * 4;    // 16 KB per split part
-constexpr uint32_t kBufBytes = 2 * kABytes + 2 * kBBytes;  // hi+lo of A and B: 48 KB
-constexpr uint32_t kSmemBytes = 2 * kBufBytes + 2048;  // two buffers + barriers + alignment slack
+constexpr int kMaxRing = 8;
+constexpr uint32_t kABytes = 128 * kTcStageK * 4;      // 8 KB per split part of A
+constexpr uint32_t kRingBytes = 192 * 1024;            // ring of stage slots
+constexpr uint32_t kSegBytes = kTcMaxSegs * sizeof(TcSeg);
+constexpr uint32_t kSmemBytes = kRingBytes + kSegBytes + 4 * (kTcMaxSegs + 2) + 256 + 1024;
 constexpr uint32_t kSBO = (kTcStageK / 4) * 128;       // bytes between 8-row groups
 constexpr uint32_t kLBO = 128;                         // bytes between K-adjacent core matrices
-constexpr long long kSpinLimit = 1ll << 22;  // an MMA group completes in microseconds
+constexpr long long kSpinLimit = 1ll << 24;            // bounded waits (a stage takes microseconds)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -137,35 +140,51 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) 
     lo = to_tf32(x - __uint_as_float(hi));
 }
 
-// per-stage copy of the segments and contribution fields staging needs
-struct StageSeg {
-    const float *A;   // operator block of the contribution (FP32 copy of the blob)
-    const float *W;   // work matrix of the contribution
-    float alpha;
-    int32_t row0, m1, lda1, ta1, col0, n1, kb, koff, kl;
-};
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
 
+// One CTA per chunk (a K range of one 128 x N tile).  Warps 0..6 are
+// producers: stage s is filled by warp s % 7 into ring slot s % R (A slab
+// 128 x 16 and B slab N x 16, TF32 hi/lo each), then released to the MMA
+// thread through full[slot].  Lane 0 of warp 7 waits on full[slot], issues
+// the 3 x 2 MMAs of the stage into the TMEM accumulator and commits them to
+// empty[slot], which frees the slot for stage s + R.  No CTA-wide barrier is
+// taken in the main loop, so several stages' global loads are in flight at
+// once.  All 8 warps drain TMEM at the end (warp w: lanes of quarter w % 4,
+// every other 16-column chunk).
 __global__ void __launch_bounds__(kThreads, 1)
 tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ tiles,
-                 const TcSeg *__restrict__ segs, const Contrib *__restrict__ contribs,
-                 const Region *__restrict__ regions, const WorkDesc *__restrict__ works,
+                 const TcSeg *__restrict__ segs, const Region *__restrict__ regions,
                  const float *__restrict__ ops, const float *__restrict__ work,
                  double *__restrict__ sigma, float *__restrict__ part, double scale, int *err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *mbar = (uint64_t *)(smem + 2 * kBufBytes);      // [0], [1]: stage buffers
-    uint32_t *tmem_slot = (uint32_t *)(smem + 2 * kBufBytes + 64);
-    __shared__ StageSeg sseg[kTcStageK];
-    __shared__ int8_t col_seg[kTcStageK];   // stage column -> sseg index (-1: zero column)
-    __shared__ int8_t col_kk[kTcStageK];    // stage column -> k offset inside the segment
+    TcSeg *sseg = (TcSeg *)(smem + kRingBytes);
+    int32_t *stage_start = (int32_t *)(smem + kRingBytes + kSegBytes);
+    uint64_t *full = (uint64_t *)(smem + kRingBytes + kSegBytes + 4 * (kTcMaxSegs + 2));
+    uint64_t *empty = full + kMaxRing;
+    uint64_t *done = empty + kMaxRing;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    int *abort_flag = (int *)(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const TcTask tk = tasks[blockIdx.x];
     const TcTile tl = tiles[tk.tile];
     const Region rg = regions[tl.g];
+    const int nseg = (int)(tk.se - tk.sb);
+    const uint32_t slot_bytes = (2 * kABytes + (uint32_t)tl.n * kTcStageK * 8 + 1023) & ~1023u;
+    const int R = min(kMaxRing, (int)(kRingBytes / slot_bytes));
 
+    // ---- setup: segment table, stage starts, barriers, TMEM
+    for (int i = tid; i < nseg; i += kThreads)
+        sseg[i] = segs[tk.sb + i];
     if (tid == 0) {
-        mbar_init(smem_u32(&mbar[0]), 1);
-        mbar_init(smem_u32(&mbar[1]), 1);
+        for (int i = 0; i < R; i++) {
+            mbar_init(smem_u32(&full[i]), 1);
+            mbar_init(smem_u32(&empty[i]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -173,104 +192,140 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
                      ::"r"(smem_u32(tmem_slot)), "r"(kMaxN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    __syncthreads();
+    // stage_start[j] = first local segment of stage st0 + j (segments ordered by stage)
+    for (int i = tid; i < nseg; i += kThreads) {
+        const int j = sseg[i].stage - tk.st0;
+        if (i == 0 || sseg[i - 1].stage != sseg[i].stage)
+            stage_start[j] = i;
+    }
+    if (tid == 0)
+        stage_start[tk.n_stages] = nseg;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = make_idesc(tl.n);
-    int issued = 0;      // stages whose MMAs were committed
-    int64_t sp = tk.sb;  // segment cursor (segments are ordered by stage)
-    for (int ls = 0; ls < tk.n_stages; ls++) {
-        const int st = tk.st0 + ls;
-        const int b = ls & 1;
-        unsigned char *buf = smem + b * kBufBytes;
-        // buffer b was last read by the MMAs of local stage ls-2 (CTA-uniform outcome)
-        if (ls >= 2) {
-            const int good = __syncthreads_and(
-                mbar_wait(smem_u32(&mbar[b]), (uint32_t)(((ls >> 1) - 1) & 1)) ? 1 : 0);
-            if (!good) {
-                if (tid == 0)
-                    atomicExch(err, 1);
+
+    if (warp < kProducers) {
+        // ---------------- producers
+        for (int ls = warp; ls < tk.n_stages; ls += kProducers) {
+            const int slot = ls % R, use = ls / R;
+            unsigned char *buf = smem + (uint32_t)slot * slot_bytes;
+            if (use >= 1) {
+                bool ok = false;
+                if (lane == 0)
+                    ok = mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1));
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok) {
+                    if (lane == 0) {
+                        atomicExch(err, 1);
+                        atomicExch(abort_flag, 1);
+                    }
+                    break;
+                }
+            }
+            // column map of this stage: lanes 0..15 find their column's segment
+            const int s0 = stage_start[ls], s1 = stage_start[ls + 1];
+            int my_seg = -1, my_kk = 0;
+            if (lane < kTcStageK)
+                for (int q = s0; q < s1; q++) {
+                    const int ko = sseg[q].koff;
+                    if (lane >= ko && lane < ko + sseg[q].kl) {
+                        my_seg = q, my_kk = lane - ko;
+                        break;
+                    }
+                }
+            // ---- A slab: lane owns rows lane + 32 i (i < 4), all 16 columns
+            float av[4][kTcStageK];
+#pragma unroll
+            for (int q = 0; q < kTcStageK; q++) {
+                const int sq = __shfl_sync(0xffffffffu, my_seg, q);
+                const int kk = __shfl_sync(0xffffffffu, my_kk, q);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    float v = 0.f;
+                    if (sq >= 0) {
+                        const TcSeg &x = sseg[sq];
+                        const int ar = tl.row0 + lane + 32 * i - x.row0;
+                        if (ar >= 0 && ar < x.m1) {
+                            const int k = x.kb + kk;
+                            v = x.alpha * __ldg(ops + x.a + (x.ta1 ? (uint64_t)k * x.lda1 + ar
+                                                                   : (uint64_t)ar * x.lda1 + k));
+                        }
+                    }
+                    av[i][q] = v;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int row = lane + 32 * i;
+#pragma unroll
+                for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
+                    uint32_t h[4], l[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        split_tf32(av[i][4 * k4 + j], h[j], l[j]);
+                    const uint32_t off = kmajor_off(row, 4 * k4);
+                    *(uint4 *)(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *(uint4 *)(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                }
+            }
+            // ---- B slab: lane owns tile columns lane + 32 j, all 16 k
+            const uint32_t b_hi = 2 * kABytes, b_lo = b_hi + (uint32_t)tl.n * kTcStageK * 4;
+            for (int jb = 0; jb < tl.n; jb += 128) {
+                float bv[4][kTcStageK];
+#pragma unroll
+                for (int q = 0; q < kTcStageK; q++) {
+                    const int sq = __shfl_sync(0xffffffffu, my_seg, q);
+                    const int kk = __shfl_sync(0xffffffffu, my_kk, q);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        float v = 0.f;
+                        const int nn = jb + lane + 32 * j;
+                        if (sq >= 0 && nn < tl.n) {
+                            const TcSeg &x = sseg[sq];
+                            const int wc = tl.col0 + nn - x.col0;
+                            if (wc >= 0 && wc < x.n1)
+                                v = __ldg(work + x.w + (uint64_t)(x.kb + kk) * x.n1 + wc);
+                        }
+                        bv[j][q] = v;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int nn = jb + lane + 32 * j;
+                    if (nn >= tl.n)
+                        continue;
+#pragma unroll
+                    for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
+                        uint32_t h[4], l[4];
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++)
+                            split_tf32(bv[j][4 * k4 + jj], h[jj], l[jj]);
+                        const uint32_t off = kmajor_off(nn, 4 * k4);
+                        *(uint4 *)(buf + b_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *(uint4 *)(buf + b_lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                    }
+                }
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(smem_u32(&full[slot]));
+        }
+    } else if (lane == 0) {
+        // ---------------- MMA issuer
+        const uint32_t idesc = make_idesc(tl.n);
+        for (int ls = 0; ls < tk.n_stages; ls++) {
+            const int slot = ls % R, use = ls / R;
+            if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(use & 1))) {
+                atomicExch(err, 1);
+                atomicExch(abort_flag, 1);
                 break;
             }
-        }
-        // ---- this stage's segment table
-        if (tid < kTcStageK)
-            col_seg[tid] = -1;
-        __syncthreads();
-        const int64_t si = sp + tid;
-        const bool mine = tid < kTcStageK && si < tk.se && segs[si].stage == st;
-        if (mine) {
-            const TcSeg sg = segs[si];
-            const Contrib c = contribs[sg.c];
-            StageSeg x;
-            x.A = ops + c.a1;
-            x.W = work + works[c.u].woff;
-            x.alpha = (float)c.alpha;
-            x.row0 = c.row0, x.m1 = c.m1, x.lda1 = c.lda1, x.ta1 = c.ta1;
-            x.col0 = c.col0, x.n1 = c.n1, x.kb = sg.kb, x.koff = sg.koff, x.kl = sg.kl;
-            sseg[tid] = x;
-            for (int kk = 0; kk < sg.kl; kk++)
-                col_seg[sg.koff + kk] = (int8_t)tid, col_kk[sg.koff + kk] = (int8_t)kk;
-        }
-        sp += __syncthreads_count(mine ? 1 : 0);
-        // ---- stage the A slab: thread tid owns tile row tid
-        {
-            const int row = tl.row0 + tid;
-#pragma unroll
-            for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
-                uint32_t h[4], l[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    h[j] = 0u, l[j] = 0u;
-                    const int q = 4 * k4 + j, si2 = col_seg[q];
-                    if (si2 >= 0) {
-                        const StageSeg &x = sseg[si2];
-                        const int ar = row - x.row0;
-                        if (ar >= 0 && ar < x.m1) {
-                            const int k = x.kb + col_kk[q];
-                            const float a = x.alpha * (x.ta1 ? x.A[(uint64_t)k * x.lda1 + ar]
-                                                             : x.A[(uint64_t)ar * x.lda1 + k]);
-                            split_tf32(a, h[j], l[j]);
-                        }
-                    }
-                }
-                const uint32_t off = kmajor_off(tid, 4 * k4);
-                *(uint4 *)(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                *(uint4 *)(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
-            }
-        }
-        // ---- stage the B slab: B[n][k] = W(k, n); threads own columns tid, tid + 128
-        for (int nn = tid; nn < tl.n; nn += kThreads) {
-            const int col = tl.col0 + nn;
-#pragma unroll
-            for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
-                uint32_t h[4], l[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    h[j] = 0u, l[j] = 0u;
-                    const int q = 4 * k4 + j, si2 = col_seg[q];
-                    if (si2 >= 0) {
-                        const StageSeg &x = sseg[si2];
-                        const int wc = col - x.col0;
-                        if (wc >= 0 && wc < x.n1) {
-                            const float w = x.W[(uint64_t)(x.kb + col_kk[q]) * x.n1 + wc];
-                            split_tf32(w, h[j], l[j]);
-                        }
-                    }
-                }
-                const uint32_t off = kmajor_off(nn, 4 * k4);
-                *(uint4 *)(buf + 2 * kABytes + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                *(uint4 *)(buf + 2 * kABytes + kBBytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
-            }
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == 0) {
-            const uint32_t a_hi = smem_u32(buf), a_lo = a_hi + kABytes;
-            const uint32_t b_hi = a_hi + 2 * kABytes, b_lo = b_hi + kBBytes;
+            tc_fence_after();
+            const uint32_t a_hi = smem_u32(smem + (uint32_t)slot * slot_bytes), a_lo = a_hi + kABytes;
+            const uint32_t b_hi = a_hi + 2 * kABytes, b_lo = b_hi + (uint32_t)tl.n * kTcStageK * 4;
 #pragma unroll
             for (int h = 0; h < kTcStageK / 8; h++) {
                 const uint32_t ko = h * 2 * kLBO;  // K = 8 = two core matrices
@@ -279,35 +334,32 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
                 mma_tf32(tmem, make_desc(a_hi + ko), make_desc(b_lo + ko), idesc, 1u);
                 mma_tf32(tmem, make_desc(a_lo + ko), make_desc(b_hi + ko), idesc, 1u);
             }
-            mma_commit(smem_u32(&mbar[b]));
+            mma_commit(smem_u32(&empty[slot]));
         }
-        issued = ls + 1;
+        mma_commit(smem_u32(done));  // tracks every MMA issued above
     }
-    // wait for the last issued stage's MMAs (its commit covers all earlier ones)
-    const int last = issued - 1;
-    bool done = false;
-    if (last >= 0) {
-        const int b = last & 1;
-        done = __syncthreads_and(mbar_wait(smem_u32(&mbar[b]), (uint32_t)((last >> 1) & 1)) ? 1 : 0) != 0;
-        if (!done && tid == 0)
-            atomicExch(err, 1);
-    }
+    // ---- epilogue
+    __syncwarp();
+    const int good = __syncthreads_and(mbar_wait(smem_u32(done), 0u) ? 1 : 0);
     tc_fence_after();
-    if (done && issued == tk.n_stages) {
-        // ---- epilogue: warp w holds TMEM lanes [32w, 32w + 32) = tile rows
-        const int trow = warp * 32 + lane;
-        const int row = tl.row0 + trow;
-        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-        float *prow = tl.part >= 0 ? part + tl.part + ((int64_t)tk.chunk * 128 + trow) * tl.n : nullptr;
-        for (int c16 = 0; c16 < tl.n; c16 += 16) {
+    if (!good && tid == 0)
+        atomicExch(err, 1);
+    if (good && *abort_flag == 0) {
+        const int q4 = warp & 3, half = warp >> 2;
+        const int trow = q4 * 32 + lane;
+        const uint32_t tbase = tmem + ((uint32_t)(q4 * 32) << 16);
+        for (int c16 = half * 16; c16 < tl.n; c16 += 32) {
             float v[16];
             tmem_ld16(tbase + (uint32_t)c16, v);
-            if (prow != nullptr) {
+            if (trow >= tl.rows)
+                continue;
+            if (tl.part >= 0) {
+                float *prow = part + tl.part + ((int64_t)tk.chunk * tl.rows + trow) * tl.n + c16;
 #pragma unroll
                 for (int j = 0; j < 16; j += 4)
-                    *(float4 *)(prow + c16 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-            } else if (trow < tl.rows) {
-                const uint64_t rowaddr = rg.base + (uint64_t)row * rg.ld;
+                    *(float4 *)(prow + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            } else {
+                const uint64_t rowaddr = rg.base + (uint64_t)(tl.row0 + trow) * rg.ld;
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const int col = tl.col0 + c16 + j;
@@ -324,7 +376,7 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kMaxN));
 }
 
-// split-K reduction: sigma += scale * sum over chunks (fixed order) of the partial tiles
+// split-K reduction: sigma += scale * sum over chunks (fixed order); block (tile, 8-row group)
 __global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restrict__ multi,
                                                         const TcTile *__restrict__ tiles,
                                                         const Region *__restrict__ regions,
@@ -332,9 +384,13 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restric
                                                         double *__restrict__ sigma, double scale) {
     const TcTile tl = tiles[multi[blockIdx.x]];
     const Region rg = regions[tl.g];
-    const int64_t plane = (int64_t)128 * tl.n;
-    for (int e = threadIdx.x; e < tl.rows * tl.n; e += blockDim.x) {
-        const int r = e / tl.n, cc = e % tl.n;
+    const int r0 = blockIdx.y * 8;
+    if (r0 >= tl.rows)
+        return;
+    const int nr = min(8, tl.rows - r0);
+    const int64_t plane = (int64_t)tl.rows * tl.n;
+    for (int e = threadIdx.x; e < nr * tl.n; e += blockDim.x) {
+        const int r = r0 + e / tl.n, cc = e % tl.n;
         const int col = tl.col0 + cc;
         const uint64_t a = rg.base + (uint64_t)(tl.row0 + r) * rg.ld + (uint64_t)col;
         if (col >= rg.cols || a < rg.lo || a >= rg.hi)
@@ -362,12 +418,12 @@ cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops, const float 
         attr_set = true;
     }
     tc_phase2_kernel<<<(unsigned)p.n_tct, kThreads, kSmemBytes, s>>>(
-        p.tct, p.tctile, p.tcs, p.contribs, p.regions, p.works, ops, work, sigma, p.tc_part, scale, err);
+        p.tct, p.tctile, p.tcs, p.regions, ops, work, sigma, p.tc_part, scale, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.n_tc_multi == 0)
         return e;
-    tc_reduce_kernel<<<(unsigned)p.n_tc_multi, 256, 0, s>>>(p.tc_multi, p.tctile, p.regions, p.tc_part,
-                                                            sigma, scale);
+    tc_reduce_kernel<<<dim3((unsigned)p.n_tc_multi, 16), 256, 0, s>>>(p.tc_multi, p.tctile, p.regions,
+                                                                      p.tc_part, sigma, scale);
     return cudaGetLastError();
 }
 
