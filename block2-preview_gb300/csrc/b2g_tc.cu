@@ -173,7 +173,11 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
     const Region rg = regions[tl.g];
     const int nseg = (int)(tk.se - tk.sb);
     const uint32_t slot_bytes = (2 * kABytes + (uint32_t)tl.n * kTcStageK * 8 + 1023) & ~1023u;
-    const int R = min(kMaxRing, (int)(kRingBytes / slot_bytes));
+    // P producer warps, each owning D ring slots (slot = p + P * (j % D) for its
+    // j-th stage): every slot is then filled by one warp in order, so no waiter
+    // is ever two mbarrier phases behind (parity waits would alias there)
+    const int Rmax = min(kMaxRing, (int)(kRingBytes / slot_bytes));
+    const int P = min(kProducers, Rmax), D = Rmax / P, R = P * D;
 
     // ---- setup: segment table, stage starts, barriers, TMEM
     for (int i = tid; i < nseg; i += kThreads)
@@ -206,10 +210,10 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp < kProducers) {
+    if (warp < P) {
         // ---------------- producers
-        for (int ls = warp; ls < tk.n_stages; ls += kProducers) {
-            const int slot = ls % R, use = ls / R;
+        for (int ls = warp, j = 0; ls < tk.n_stages; ls += P, j++) {
+            const int slot = warp + P * (j % D), use = j / D;
             unsigned char *buf = smem + (uint32_t)slot * slot_bytes;
             if (use >= 1) {
                 bool ok = false;
@@ -313,11 +317,11 @@ tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ ti
             if (lane == 0)
                 mbar_arrive(smem_u32(&full[slot]));
         }
-    } else if (lane == 0) {
+    } else if (warp == kMmaWarp && lane == 0) {
         // ---------------- MMA issuer
         const uint32_t idesc = make_idesc(tl.n);
         for (int ls = 0; ls < tk.n_stages; ls++) {
-            const int slot = ls % R, use = ls / R;
+            const int jj = ls / P, slot = ls % P + P * (jj % D), use = jj / D;
             if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(use & 1))) {
                 atomicExch(err, 1);
                 atomicExch(abort_flag, 1);
