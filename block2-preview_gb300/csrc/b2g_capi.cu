@@ -34,7 +34,7 @@ static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
     cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi), cudaFree(p.tc_part);
-    cudaFree(p.t2multi), cudaFree(p.t2_part);
+    cudaFree(p.t2multi), cudaFree(p.t2_part), cudaFree(p.tc1t), cudaFree(p.tc1r);
     p = DevicePlan();
 }
 
@@ -141,8 +141,10 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
         (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)) ||
         (rc = upload(hp.tctile, &p.tctile, s)) || (rc = upload(hp.tc_multi, &p.tc_multi, s)) ||
-        (rc = upload(hp.t2multi, &p.t2multi, s)))
+        (rc = upload(hp.t2multi, &p.t2multi, s)) || (rc = upload(hp.tc1t, &p.tc1t, s)) ||
+        (rc = upload(hp.tc1r, &p.tc1r, s)))
         return bail(rc);
+    p.n_tc1t = (int64_t)hp.tc1t.size();
     p.n_t2multi = (int64_t)hp.t2multi.size();
     if (hp.t2_part_tiles &&
         cudaMalloc(&p.t2_part, sizeof(double) * 4 * 256 * hp.t2_part_tiles) != cudaSuccess) {
@@ -306,7 +308,10 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
         // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
         B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size, s));
-        B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, s));
+        if (form == B2G_TF32X3)
+            B2G_CUDA_TRY(launch_tc_phase1(h->plan, h->ops32, h->psi32, w32, h->err, s));
+        else
+            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
         if (form == B2G_TF32X3)

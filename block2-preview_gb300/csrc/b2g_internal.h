@@ -74,6 +74,9 @@ struct Tile2 {          // a phase-2 tile split over several chunks (reduced aft
 constexpr int kTcStageK = 16;
 constexpr int kTcMaxSegs = 384;
 constexpr int kTcTargetChunks = 8 * 152;
+// FP32 accumulation in TMEM over very long K loses accuracy; chunks end after
+// at most this many stages (512 K) and the FP64 reduction sums the chunks
+constexpr int kTcMaxChunkStages = 32;
 struct TcTile {
     int32_t g, row0, col0, n;   // region, tile origin, tile width (multiple of 16, <= 256)
     int32_t rows, n_chunks;     // valid rows (<= 128), chunks
@@ -96,7 +99,25 @@ struct TcSeg {
     int32_t stage;              // stage index within the tile
 };
 
+// Tensor-core phase 1: the distinct products W_u = psi_sub * op(R) that share
+// one right-operator block R are stacked row-wise into tiles of <= 128 rows
+// (one CTA each, K = k0 in stages of kTcStageK, N <= 256 columns per tile).
+struct Tc1Tile {
+    uint64_t b0;                // right operator block offset
+    int32_t tb0, k0, n0, ldb0;  // its transpose flag, K, total columns, leading dimension
+    int32_t col0, n;            // column range [col0, col0 + n) of this tile (n multiple of 16)
+    int32_t rows;               // stacked rows (<= 128)
+    int32_t pad;
+    int64_t rb;                 // first entry in the row table
+};
+struct Tc1Row {
+    uint64_t psi;               // psi offset of the row (a0 + r * lda0)
+    uint64_t w;                 // work offset of the row (woff + r * n0)
+};
+
 struct HostPlan {
+    std::vector<Tc1Tile> tc1t;
+    std::vector<Tc1Row> tc1r;
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
     std::vector<Region> regions;
@@ -127,6 +148,9 @@ struct DevicePlan {
     void *t2_part = nullptr;        // partial tiles (double or float, sized for double)
     int64_t n_t2multi = 0;
     int32_t *lists = nullptr;
+    Tc1Tile *tc1t = nullptr;
+    Tc1Row *tc1r = nullptr;
+    int64_t n_tc1t = 0;
     TcTask *tct = nullptr;
     TcSeg *tcs = nullptr;
     TcTile *tctile = nullptr;
@@ -140,6 +164,8 @@ struct DevicePlan {
 // bounded wait gives up
 cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops32, const float *work,
                              double *sigma, double scale, int *err, cudaStream_t s);
+cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops32, const float *psi32,
+                             float *work, int *err, cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>

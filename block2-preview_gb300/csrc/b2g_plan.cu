@@ -272,7 +272,8 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         for (auto &tl : plan.tctile)
             total_stages += tl.n_chunks;
         const int32_t chunk_stages = (int32_t)std::min<int64_t>(
-            kTcMaxSegs, std::max<int64_t>(16, (total_stages + kTcTargetChunks - 1) / kTcTargetChunks));
+            kTcMaxChunkStages,
+            std::max<int64_t>(8, (total_stages + kTcTargetChunks - 1) / kTcTargetChunks));
         for (int32_t tile = 0; tile < (int32_t)plan.tctile.size(); tile++) {
             TcTile &tl = plan.tctile[tile];
             const int32_t n_stages = tl.n_chunks;
@@ -317,6 +318,54 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
     for (int32_t u = 0; u < (int32_t)plan.works.size(); u++)
         for (int32_t r = 0; r < plan.works[u].m0; r++)
             plan.t1.push_back(Task1{u, r});
+    // ---- tensor-core phase 1: stack rows of products sharing a right operator block
+    {
+        std::vector<int32_t> ord(plan.works.size());
+        for (size_t i = 0; i < ord.size(); i++)
+            ord[i] = (int32_t)i;
+        auto key_less = [&](int32_t x, int32_t y) {
+            const WorkDesc &a = plan.works[x], &b = plan.works[y];
+            if (a.b0 != b.b0) return a.b0 < b.b0;
+            if (a.tb0 != b.tb0) return a.tb0 < b.tb0;
+            if (a.k0 != b.k0) return a.k0 < b.k0;
+            if (a.n0 != b.n0) return a.n0 < b.n0;
+            if (a.ldb0 != b.ldb0) return a.ldb0 < b.ldb0;
+            return x < y;
+        };
+        std::sort(ord.begin(), ord.end(), key_less);
+        auto same_r = [&](int32_t x, int32_t y) {
+            const WorkDesc &a = plan.works[x], &b = plan.works[y];
+            return a.b0 == b.b0 && a.tb0 == b.tb0 && a.k0 == b.k0 && a.n0 == b.n0 && a.ldb0 == b.ldb0;
+        };
+        for (size_t gs = 0; gs < ord.size();) {
+            size_t ge = gs + 1;
+            while (ge < ord.size() && same_r(ord[gs], ord[ge]))
+                ge++;
+            const WorkDesc &w0 = plan.works[ord[gs]];
+            // rows of the group in order, cut into tiles of 128
+            std::vector<Tc1Row> rows;
+            for (size_t q = gs; q < ge; q++) {
+                const WorkDesc &w = plan.works[ord[q]];
+                for (int32_t r = 0; r < w.m0; r++)
+                    rows.push_back(Tc1Row{w.a0 + (uint64_t)r * w.lda0, w.woff + (uint64_t)r * w.n0});
+            }
+            for (size_t r0 = 0; r0 < rows.size(); r0 += 128) {
+                const int64_t rb = (int64_t)plan.tc1r.size();
+                const int32_t nr = (int32_t)std::min<size_t>(128, rows.size() - r0);
+                plan.tc1r.insert(plan.tc1r.end(), rows.begin() + r0, rows.begin() + r0 + nr);
+                for (int32_t c0 = 0; c0 < w0.n0; c0 += 256) {
+                    Tc1Tile t;
+                    t.b0 = w0.b0, t.tb0 = w0.tb0, t.k0 = w0.k0, t.n0 = w0.n0, t.ldb0 = w0.ldb0;
+                    t.col0 = c0, t.n = std::min(256, (w0.n0 - c0 + 15) / 16 * 16);
+                    t.rows = nr, t.pad = 0, t.rb = rb;
+                    plan.tc1t.push_back(t);
+                }
+            }
+            gs = ge;
+        }
+        std::stable_sort(plan.tc1t.begin(), plan.tc1t.end(),
+                         [](const Tc1Tile &a, const Tc1Tile &b) { return a.k0 * a.n > b.k0 * b.n; });
+    }
     return B2G_OK;
 }
 
