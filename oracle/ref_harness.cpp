@@ -270,13 +270,120 @@ template <typename S> struct Dumper : CallbackKernel {
         w.vec("psi", psi, "f8");
         w.man.flush();
     }
+    // the next operator rotation after a dumped site is recorded too
+    mutable bool want_rotation = false;
+    mutable string rot_dir;
     void compute(const string &name, int iprint) const override {
         if (d == nullptr || d->current_eff_ham == nullptr || !selected())
             return;
         if (name == "DMRG::sweep::iter.eff_ham")
             dump_pre(d->current_eff_ham);
-        else if (name == "DMRG::sweep::iter.eff_ham.end")
+        else if (name == "DMRG::sweep::iter.eff_ham.end") {
             dump_post(d->current_eff_ham);
+            want_rotation = true;
+            rot_dir = site_dir() + "/rotation";
+        }
+    }
+};
+
+// Operator rotation recorder: TensorFunctions::left_rotate / right_rotate
+// (src/core/tensor_functions.hpp:2365-2403) run unchanged; when a rotation is
+// requested, its per-block GEMM pairs are written in the same pair format as
+// H_eff*psi, restating the block loop of OperatorFunctions::tensor_rotate
+// (src/core/operator_functions.hpp:175-211) and the GEMM order of
+// GMatrixFunctions::rotate (src/core/matrix_functions.hpp:998-1009):
+//   work = a * op(ket);  c += scale * op(bra) * work.
+// "psi" is the packed input operator data, "ops" the MPS tensor (bra, ket),
+// "sigma" the packed rotated operators (the reference's result).
+template <typename S> struct RecordingTF : TensorFunctions<S, double> {
+    typedef TensorFunctions<S, double> TF;
+    const Dumper<S> *dumper = nullptr;
+    RecordingTF(const shared_ptr<OperatorFunctions<S, double>> &opf, const Dumper<S> *dp)
+        : TF(opf), dumper(dp) {}
+    shared_ptr<TF> copy() const override {
+        return make_shared<RecordingTF>(this->opf->copy(), dumper);
+    }
+    void left_rotate(const shared_ptr<OperatorTensor<S, double>> &a,
+                     const shared_ptr<SparseMatrix<S, double>> &bra,
+                     const shared_ptr<SparseMatrix<S, double>> &ket,
+                     shared_ptr<OperatorTensor<S, double>> &c) const override {
+        TF::left_rotate(a, bra, ket, c);
+        record(a->lmat, a, bra, ket, c, false);
+    }
+    void right_rotate(const shared_ptr<OperatorTensor<S, double>> &a,
+                      const shared_ptr<SparseMatrix<S, double>> &bra,
+                      const shared_ptr<SparseMatrix<S, double>> &ket,
+                      shared_ptr<OperatorTensor<S, double>> &c) const override {
+        TF::right_rotate(a, bra, ket, c);
+        record(a->rmat, a, bra, ket, c, true);
+    }
+    void record(const shared_ptr<Symbolic<S>> &mat, const shared_ptr<OperatorTensor<S, double>> &a,
+                const shared_ptr<SparseMatrix<S, double>> &bra,
+                const shared_ptr<SparseMatrix<S, double>> &ket,
+                const shared_ptr<OperatorTensor<S, double>> &c, bool trans) const {
+        if (dumper == nullptr || !dumper->want_rotation)
+            return;
+        dumper->want_rotation = false;
+        // packed blobs: input ops (psi role), rotated ops (sigma role), bra+ket (ops role)
+        map<const double *, size_t> in_off, out_off;
+        vector<double> in_blob, out_blob, mps_blob;
+        auto pack = [](map<const double *, size_t> &off, vector<double> &blob,
+                       const shared_ptr<SparseMatrix<S, double>> &m) {
+            auto it = off.find(m->data);
+            if (it != off.end())
+                return it->second;
+            size_t o = blob.size();
+            off[m->data] = o;
+            blob.insert(blob.end(), m->data, m->data + m->total_memory);
+            return o;
+        };
+        const size_t bra_off = 0;
+        mps_blob.insert(mps_blob.end(), bra->data, bra->data + bra->total_memory);
+        const size_t ket_off = bra == ket ? 0 : mps_blob.size();
+        if (bra != ket)
+            mps_blob.insert(mps_blob.end(), ket->data, ket->data + ket->total_memory);
+        vector<int32_t> tb0, m0, n0, k0, lda0, ldb0, ta1, m1, n1, k1, lda1, ldc1;
+        vector<double> al0, al1;
+        vector<uint64_t> a0, b0, a1, c1;
+        for (size_t i = 0; i < mat->data.size(); i++) {
+            if (mat->data[i]->get_type() == OpTypes::Zero)
+                continue;
+            auto pa = abs_value(mat->data[i]);
+            auto A = a->ops.at(pa), C = c->ops.at(pa);
+            const double scale = A->factor * bra->factor * ket->factor;
+            if (abs(scale) < TINY)
+                continue;
+            const size_t ao = pack(in_off, in_blob, A), co = pack(out_off, out_blob, C);
+            S cdq = C->info->delta_quantum;
+            for (int ic = 0, ia = 0; ic < C->info->n; ia++, ic++) {
+                while (A->info->quanta[ia] != C->info->quanta[ic])
+                    ia++;
+                S cq = C->info->quanta[ic].get_bra(cdq), cqp = C->info->quanta[ic].get_ket();
+                int ibra = bra->info->find_state(cq), iket = ket->info->find_state(cqp);
+                GMatrix<double> ma = (*A)[ia], mc = (*C)[ic], mb = (*bra)[ibra], mk = (*ket)[iket];
+                const int cb = trans ? 0 : 1, ck = trans ? 1 : 0;  // conj bits (!trans|2)&1, trans&1
+                tb0.push_back(ck), m0.push_back(ma.m), k0.push_back(ma.n), lda0.push_back(ma.n);
+                n0.push_back(ck ? mk.m : mk.n), ldb0.push_back(mk.n);
+                ta1.push_back(cb), m1.push_back(mc.m), k1.push_back(ma.m), lda1.push_back(mb.n);
+                n1.push_back(mc.n), ldc1.push_back(mc.n);
+                al0.push_back(1.0), al1.push_back(scale);
+                a0.push_back(ao + (ma.data - A->data)), b0.push_back(ket_off + (mk.data - ket->data));
+                a1.push_back(bra_off + (mb.data - bra->data)), c1.push_back(co + (mc.data - C->data));
+            }
+        }
+        Writer w(dumper->rot_dir);
+        w.scalar("n_pairs", (double)tb0.size());
+        w.scalar("psi_size", (double)in_blob.size());
+        w.scalar("sigma_size", (double)out_blob.size());
+        w.scalar("ops_size", (double)mps_blob.size());
+        w.scalar("trans", trans);
+        w.vec("tb0", tb0, "i4"), w.vec("m0", m0, "i4"), w.vec("n0", n0, "i4"), w.vec("k0", k0, "i4");
+        w.vec("lda0", lda0, "i4"), w.vec("ldb0", ldb0, "i4"), w.vec("ta1", ta1, "i4");
+        w.vec("m1", m1, "i4"), w.vec("n1", n1, "i4"), w.vec("k1", k1, "i4"), w.vec("lda1", lda1, "i4");
+        w.vec("ldc1", ldc1, "i4"), w.vec("alpha0", al0, "f8"), w.vec("alpha1", al1, "f8");
+        w.vec("a0", a0, "u8"), w.vec("b0", b0, "u8"), w.vec("a1", a1, "u8"), w.vec("c1", c1, "u8");
+        w.vec("psi", in_blob, "f8"), w.vec("ops", mps_blob, "f8"), w.vec("sigma", out_blob, "f8");
+        w.man.flush();
     }
 };
 
@@ -315,6 +422,9 @@ template <typename S> int run(const Opts &o) {
     mps->deallocate();
     mps_info->save_mutable();
     mps_info->deallocate_mutable();
+    auto dumper = make_shared<Dumper<S>>();
+    dumper->o = o;
+    mpo->tf = make_shared<RecordingTF<S>>(mpo->tf->opf, dumper.get());
     auto me = make_shared<MovingEnvironment<S, FL, FL>>(mpo, mps, mps, "DMRG");
     me->init_environments(false);
     me->delayed_contraction = OpNamesSet::normal_ops();
@@ -324,9 +434,7 @@ template <typename S> int run(const Opts &o) {
     dmrg->davidson_conv_thrds = o.dav_thrds;
     dmrg->noise_type = NoiseTypes::DensityMatrix;
     dmrg->iprint = 2;
-    auto dumper = make_shared<Dumper<S>>();
     dumper->d = dmrg.get();
-    dumper->o = o;
     callback_() = dumper;
     Timer t;
     t.get_time();

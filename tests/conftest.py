@@ -18,8 +18,18 @@ def fixture_paths():
     return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
 
 
-def fixture_ids():
+def all_ids():
     return [os.path.basename(p)[:-4] for p in fixture_paths()]
+
+
+def fixture_ids():
+    """Effective-Hamiltonian problems (H_eff*psi and Davidson)."""
+    return [n for n in all_ids() if not n.endswith("_rot")]
+
+
+def rotation_ids():
+    """Operator-rotation problems (same pair format, no Davidson)."""
+    return [n for n in all_ids() if n.endswith("_rot")]
 
 
 @pytest.fixture(scope="session")

@@ -118,6 +118,21 @@ def run_case(name, args, desc):
     print(f"{name}: pairs={meta['n_pairs']} ops={prob.ops.size} psi={prob.psi_size} "
           f"E_dav={meta['davidson_energy']:.12f} E_final={meta['final_energy']:.12f} "
           f"-> {os.path.getsize(path)} bytes")
+    # the operator rotation that followed this site (same pair format)
+    rdir = os.path.join(out, site_dirs[0], "rotation")
+    if os.path.isdir(rdir):
+        ra, rs = read_dump(rdir)
+        rmeta = {"name": name + "_rot", "kind": "rotation",
+                 "description": "operator rotation after the site of " + name + " ("
+                                + ("right" if rs["trans"] else "left") + "_rotate)",
+                 "n_pairs": int(rs["n_pairs"]), "trans": int(rs["trans"])}
+        rot = HeffProblem(pairs={k: ra[k] for k in PAIR_FIELDS}, ops=ra["ops"],
+                          psi_size=int(rs["psi_size"]), sigma_size=int(rs["sigma_size"]),
+                          psi=ra["psi"], sigma=ra["sigma"], meta=rmeta)
+        rpath = os.path.join(HERE, name + "_rot.npz")
+        rot.save(rpath)
+        print(f"{name}_rot: pairs={rmeta['n_pairs']} in={rot.psi_size} out={rot.sigma_size} "
+              f"-> {os.path.getsize(rpath)} bytes")
 
 
 def main():
