@@ -79,6 +79,8 @@ SIGNATURES = {
                                  C.POINTER(HeffStatsC)]),
     "b2g_heff_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
     "b2g_heff_apply_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+    "b2g_heff_apply_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                       C.c_int]),
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),
     "b2g_heff_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
@@ -86,6 +88,8 @@ SIGNATURES = {
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,
                                C.c_int, C.c_int, C.POINTER(DavidsonResultC)]),
+    "b2g_davidson_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
+                                     C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(DavidsonResultC)]),
 }
 
 _lib = None

@@ -101,6 +101,18 @@ class EffectiveHamiltonian:
             check(lib().b2g_heff_apply(self._h, _ptr(b), _ptr(c), scale, form))
         return c
 
+    def apply_batch(self, b, c, scale: float = 1.0, form: int = FP64):
+        """c[r] += scale * H_eff * b[r] for every row r of the (nroots, size)
+        CUDA tensors b and c, in one launch per kernel."""
+        if b.dim() != 2 or c.dim() != 2 or b.shape[0] != c.shape[0]:
+            raise ValueError("b and c must be (nroots, size) tensors with equal nroots")
+        if b.shape[1] != self.psi_size or c.shape[1] != self.sigma_size:
+            raise ValueError("wavefunction sizes do not match the effective Hamiltonian")
+        if not (b.is_cuda and c.is_cuda and b.is_contiguous() and c.is_contiguous()):
+            raise TypeError("device buffers must be contiguous CUDA tensors")
+        check(lib().b2g_heff_apply_batch(self._h, _ptr(b), _ptr(c), int(b.shape[0]), scale, form))
+        return c
+
     def status(self):
         """Synchronize and raise if a tensor-core kernel gave up a bounded wait."""
         check(lib().b2g_heff_status(self._h))
@@ -126,6 +138,26 @@ class EffectiveHamiltonian:
         self.last_davidson = res
         nflop = self.nflop * (res.n_apply_fp64 + res.n_apply_mixed)
         return res.energy, res.n_iter, nflop, tdav
+
+    # EffectiveHamiltonian<S, FL, MultiMPS>::eigs (effective_hamiltonian.hpp:1711-1797)
+    def eigs_multi(self, diag, psis, conv_thrd: float = 5e-6, max_iter: int = 5000,
+                   def_min: int = 2, def_max: int = 50, form: int = FP64):
+        """k lowest eigenpairs; psis (k, n) host float64 guesses, overwritten with
+        the eigenvectors.  Returns (energies[k], ndav, nflop, tdav)."""
+        diag = np.ascontiguousarray(diag, dtype=np.float64)
+        if psis.dtype != np.float64 or not psis.flags.c_contiguous or psis.ndim != 2:
+            raise TypeError("psis must be a contiguous (k, n) float64 array")
+        k = psis.shape[0]
+        energies = np.zeros(k)
+        res = capi.DavidsonResultC()
+        t0 = time.perf_counter()
+        rc = lib().b2g_davidson_multi(self._h, diag.ctypes.data, psis.ctypes.data, k, conv_thrd,
+                                      max_iter, def_min, def_max, form, energies.ctypes.data,
+                                      C.byref(res))
+        tdav = time.perf_counter() - t0
+        check(rc)
+        self.last_davidson = res
+        return energies, res.n_iter, self.nflop * (res.n_apply_fp64 + res.n_apply_mixed), tdav
 
     def close(self):
         if self._h:

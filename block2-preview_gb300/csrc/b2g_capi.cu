@@ -33,9 +33,32 @@ template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaSt
 static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
-    cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi), cudaFree(p.tc_part);
-    cudaFree(p.t2multi), cudaFree(p.t2_part), cudaFree(p.tc1t), cudaFree(p.tc1r);
+    cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi);
+    cudaFree(p.t2multi), cudaFree(p.tc1t), cudaFree(p.tc1r);
     p = DevicePlan();
+}
+
+// per-root buffers (work matrices, split-K partials, float psi) for nroots roots
+static int ensure_roots(b2g_heff *h, int nroots) {
+    if (nroots <= h->cap_roots)
+        return B2G_OK;
+    B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+    cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
+    h->work = nullptr, h->simt_part = nullptr, h->tc_part = nullptr, h->psi32 = nullptr;
+    h->cap_roots = 0;
+    const size_t R = (size_t)nroots;
+    if ((h->work_size && cudaMalloc(&h->work, sizeof(double) * h->work_size * R) != cudaSuccess) ||
+        (h->simt_part_size &&
+         cudaMalloc(&h->simt_part, sizeof(double) * h->simt_part_size * R) != cudaSuccess) ||
+        (h->tc_part_size && cudaMalloc(&h->tc_part, sizeof(float) * h->tc_part_size * R) != cudaSuccess) ||
+        (h->psi_size && cudaMalloc(&h->psi32, sizeof(float) * h->psi_size * R) != cudaSuccess)) {
+        cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
+        h->work = nullptr, h->simt_part = nullptr, h->tc_part = nullptr, h->psi32 = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the per-root work buffers of " +
+                                       std::to_string(nroots) + " roots");
+    }
+    h->cap_roots = nroots;
+    return B2G_OK;
 }
 
 } // namespace b2g
@@ -111,6 +134,7 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     auto bail = [&](int code) {
         free_plan(h->plan);
         cudaFree(h->ops), cudaFree(h->work), cudaFree(h->err);
+        cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
         delete h;
         return code;
     };
@@ -125,10 +149,10 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
                             s) != cudaSuccess)
             return bail(fail(B2G_ERR_CUDA, "operator blob upload failed"));
     }
-    if (hp.work_size && cudaMalloc(&h->work, sizeof(double) * hp.work_size) != cudaSuccess) {
-        h->work = nullptr;
-        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the work buffer"));
-    }
+    h->simt_part_size = (uint64_t)4 * 256 * hp.t2_part_tiles;
+    h->tc_part_size = hp.tc_part_size;
+    if ((rc = ensure_roots(h, 1)) != B2G_OK)
+        return bail(rc);
     if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) {
         h->err = nullptr;
         return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the error flag"));
@@ -146,15 +170,6 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         return bail(rc);
     p.n_tc1t = (int64_t)hp.tc1t.size();
     p.n_t2multi = (int64_t)hp.t2multi.size();
-    if (hp.t2_part_tiles &&
-        cudaMalloc(&p.t2_part, sizeof(double) * 4 * 256 * hp.t2_part_tiles) != cudaSuccess) {
-        p.t2_part = nullptr;
-        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the phase-2 partial tiles"));
-    }
-    if (hp.tc_part_size && cudaMalloc(&p.tc_part, sizeof(float) * hp.tc_part_size) != cudaSuccess) {
-        p.tc_part = nullptr;
-        return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the split-K partial tiles"));
-    }
     p.n_tctile = (int64_t)hp.tctile.size(), p.n_tc_multi = (int64_t)hp.tc_multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
     p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
@@ -199,6 +214,7 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaStreamSynchronize(h->ctx->stream);
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
+    cudaFree(h->simt_part), cudaFree(h->tc_part);
     cudaFree(h->psi_stage), cudaFree(h->sigma_stage), cudaFree(h->err);
     for (auto &e : h->ev)
         if (e)
@@ -273,18 +289,29 @@ int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size
     return B2G_OK;
 }
 
-int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {
-    if (h == nullptr || (h->psi_size && psi == nullptr) || (h->sigma_size && sigma == nullptr))
-        return fail(B2G_ERR_ARG, "b2g_heff_apply: null argument");
+int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
+                         int form) {
+    if (h == nullptr || nroots < 1 || (h->psi_size && psi == nullptr) ||
+        (h->sigma_size && sigma == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_apply: null argument or nroots < 1");
+    if (nroots > 65535)
+        return fail(B2G_ERR_ARG, "b2g_heff_apply: too many roots");
     B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
     cudaStream_t s = h->ctx->stream;
+    int rc = ensure_roots(h, nroots);
+    if (rc != B2G_OK)
+        return rc;
+    RootStrides rs;
+    rs.nroots = nroots, rs.psi = h->psi_size, rs.sigma = h->sigma_size;
     if (form == B2G_FP64) {
+        rs.work = h->work_size, rs.part = h->simt_part_size;
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-        B2G_CUDA_TRY(launch_simt_phase1<double>(h->plan, h->ops, psi, h->work, s));
+        B2G_CUDA_TRY(launch_simt_phase1<double>(h->plan, h->ops, psi, h->work, rs, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-        B2G_CUDA_TRY(launch_simt_phase2<double>(h->plan, h->ops, h->work, sigma, scale, s));
+        B2G_CUDA_TRY(launch_simt_phase2<double>(h->plan, h->ops, h->work, sigma, (double *)h->simt_part,
+                                                scale, rs, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;
@@ -297,32 +324,35 @@ int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, 
             }
             B2G_CUDA_TRY(launch_to_float(h->ops, h->ops32, h->ops_size, s));
         }
-        if (h->psi32 == nullptr && h->psi_size) {
-            if (cudaMalloc(&h->psi32, sizeof(float) * h->psi_size) != cudaSuccess) {
-                h->psi32 = nullptr;
-                return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the float psi copy");
-            }
-        }
         float *w32 = (float *)h->work;
+        rs.work = 2 * h->work_size;  // floats per root in a buffer sized in doubles
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
         // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
-        B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size, s));
+        B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
         if (form == B2G_TF32X3)
-            B2G_CUDA_TRY(launch_tc_phase1(h->plan, h->ops32, h->psi32, w32, h->err, s));
+            B2G_CUDA_TRY(launch_tc_phase1(h->plan, h->ops32, h->psi32, w32, h->err, rs, s));
         else
-            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, s));
+            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-        if (form == B2G_TF32X3)
-            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops32, w32, sigma, scale, h->err, s));
-        else
-            B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, scale, s));
+        if (form == B2G_TF32X3) {
+            rs.part = h->tc_part_size;
+            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops32, w32, sigma, h->tc_part, scale, h->err, rs, s));
+        } else {
+            rs.part = 2 * h->simt_part_size;
+            B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, (float *)h->simt_part,
+                                                   scale, rs, s));
+        }
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;
     }
     return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_apply: unknown form " + std::to_string(form));
+}
+
+int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {
+    return b2g_heff_apply_batch(h, psi, sigma, 1, scale, form);
 }
 
 int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {

@@ -18,6 +18,7 @@
 // All vectors live in HBM; per iteration only (lambda, |r|^2) come back to
 // the host for the convergence decision.  Reductions are two-stage
 // (per-block partials, then a fixed-order sum): results are bit-reproducible.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -276,36 +277,39 @@ int grid_for(uint64_t n) {
 
 using namespace b2g;
 
-extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double conv_thrd,
-                            int max_iter, int def_min, int def_max, int form,
-                            b2g_davidson_result *res) {
-    if (h == nullptr || diag == nullptr || psi == nullptr || res == nullptr)
-        return fail(B2G_ERR_ARG, "b2g_davidson: null argument");
+// Block Davidson for the k lowest eigenpairs.  k = 1 is the reference's
+// one-root Davidson; for k > 1 every unconverged root contributes its Olsen
+// correction each iteration and all new basis vectors go through one batched
+// H_eff product (the reference converges state-averaged roots one correction
+// at a time, iterative_matrix_functions.hpp:1010-1160; the converged
+// eigenpairs are the same).
+static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, double conv_thrd,
+                         int max_iter, int def_min, int def_max, int form, double *energies,
+                         b2g_davidson_result *res) {
+    if (h == nullptr || diag == nullptr || psi == nullptr || res == nullptr || k < 1)
+        return fail(B2G_ERR_ARG, "b2g_davidson: null argument or k < 1");
     if (h->psi_size != h->sigma_size)
         return fail(B2G_ERR_ARG, "b2g_davidson: H_eff is not square (bra != ket size)");
-    if (def_min < 1)
-        def_min = 1;
-    if (def_max < def_min + 1)
-        def_max = def_min + 1;
-    if (def_max > kMaxSub)
-        return fail(B2G_ERR_ARG, "b2g_davidson: def_max above 64");
     if (form != B2G_FP64 && form != B2G_FP32 && form != B2G_TF32X3)
         return fail(B2G_ERR_UNSUPPORTED, "b2g_davidson: unknown form");
+    def_min = std::max(def_min, k);
+    def_max = std::max(def_max, def_min + k);
+    if (def_max > kMaxSub)
+        return fail(B2G_ERR_ARG, "b2g_davidson: def_max above 64");
     B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
     cudaStream_t st = h->ctx->stream;
     const uint64_t n = h->psi_size;
     const int g = grid_for(n);
-    // device workspace: B, S (def_max vectors each), x, s, q, t, tmp (def_min vectors), diag
-    double *B = nullptr, *S = nullptr, *x = nullptr, *s = nullptr, *q = nullptr, *t = nullptr,
+    double *B = nullptr, *S = nullptr, *X = nullptr, *SX = nullptr, *Q = nullptr, *t = nullptr,
            *R = nullptr, *D = nullptr, *small = nullptr, *partial = nullptr;
-    const size_t nsmall = (size_t)kMaxSub * kMaxSub * 2 + 4 * kMaxSub + 16;
+    const size_t nsmall = (size_t)kMaxSub * kMaxSub * 2 + 6 * kMaxSub + 16;
     auto cleanup = [&]() {
-        cudaFree(B), cudaFree(S), cudaFree(x), cudaFree(s), cudaFree(q), cudaFree(t), cudaFree(R);
+        cudaFree(B), cudaFree(S), cudaFree(X), cudaFree(SX), cudaFree(Q), cudaFree(t), cudaFree(R);
         cudaFree(D), cudaFree(small), cudaFree(partial);
     };
     if (cudaMalloc(&B, sizeof(double) * n * def_max) || cudaMalloc(&S, sizeof(double) * n * def_max) ||
-        cudaMalloc(&x, sizeof(double) * n) || cudaMalloc(&s, sizeof(double) * n) ||
-        cudaMalloc(&q, sizeof(double) * n) || cudaMalloc(&t, sizeof(double) * n) ||
+        cudaMalloc(&X, sizeof(double) * n * k) || cudaMalloc(&SX, sizeof(double) * n * k) ||
+        cudaMalloc(&Q, sizeof(double) * n * k) || cudaMalloc(&t, sizeof(double) * n) ||
         cudaMalloc(&R, sizeof(double) * n * def_min) || cudaMalloc(&D, sizeof(double) * n) ||
         cudaMalloc(&small, sizeof(double) * nsmall) ||
         cudaMalloc(&partial, sizeof(double) * kRedBlocks * kMaxSub)) {
@@ -314,136 +318,192 @@ extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double
     }
     double *A = small;                          // kMaxSub x kMaxSub subspace matrix
     double *V = A + kMaxSub * kMaxSub;          // eigenvectors (columns), ld kMaxSub
-    double *w = V + kMaxSub * kMaxSub;          // eigenvalues
+    double *w = V + kMaxSub * kMaxSub;          // eigenvalues (ascending)
     double *dots = w + kMaxSub;                 // kMaxSub dot results
-    double *sc = dots + kMaxSub;                // scalars: [0] lambda, [1] |q|^2, [2..3] olsen
+    double *qqd = dots + kMaxSub;               // kMaxSub residual norms
+    double *sc = qqd + kMaxSub;                 // scratch scalars
     double *coef = sc + 16;                     // kMaxSub coefficients
-    auto dot_many = [&](const double *X, int nv, const double *y, double *out) {
-        multidot_partial<<<kRedBlocks, kRedThreads, 0, st>>>(X, n, nv, y, n, partial);
+    auto dot_many = [&](const double *Xv, int nv, const double *y, double *out) {
+        multidot_partial<<<kRedBlocks, kRedThreads, 0, st>>>(Xv, n, nv, y, n, partial);
         multidot_final<<<(nv + 7) / 8, 256, 0, st>>>(partial, kRedBlocks, nv, out);
     };
+    std::vector<double> lam(kMaxSub), qq(kMaxSub);
     int rc = B2G_OK;
-#define DAV_TRY(expr)                                                                       \
-    do {                                                                                    \
-        cudaError_t _e = (expr);                                                            \
-        if (_e != cudaSuccess) {                                                            \
-            rc = fail(B2G_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));    \
-            goto done;                                                                      \
-        }                                                                                   \
-    } while (0)
-    {
-        DAV_TRY(cudaMemcpyAsync(D, diag, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-        DAV_TRY(cudaMemcpyAsync(q, psi, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-        DAV_TRY(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st));
+    int m = 0, msig = 0, xiter = 0, n_fp64 = 0, n_mixed = 0, n_refine = 0, since_refine = 0;
+    bool converged = false, have_exact = false;
+    // host-side helpers; each returns false after recording an error in rc
+    auto cuda_ok = [&](cudaError_t e, const char *what) {
+        if (e == cudaSuccess)
+            return true;
+        rc = fail(B2G_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+        return false;
+    };
+    // orthogonalise Q_row (device vector q) against B[0..m) twice, append if not degenerate
+    auto append = [&](double *q) -> int {
+        for (int pass = 0; pass < 2; pass++) {
+            dot_many(B, m, q, coef);
+            combine<<<g, 256, 0, st>>>(q, 1.0, B, n, m, coef, -1.0, n);
+        }
         dot_many(q, 1, q, sc + 1);
-        normalize_into<<<g, 256, 0, st>>>(B, q, sc + 1, n);
-        int m = 1, msig = 0, xiter = 0, n_fp64 = 0, n_mixed = 0, n_refine = 0, since_refine = 0;
-        double lam = 0.0, qq = 0.0;
-        bool converged = false, have_exact = false;
-        while (xiter < max_iter) {
-            xiter++;
-            since_refine++;
-            for (int i = msig; i < m; i++, msig++) {
-                double *si = S + (uint64_t)i * n;
-                DAV_TRY(cudaMemsetAsync(si, 0, sizeof(double) * n, st));
-                rc = b2g_heff_apply(h, B + (uint64_t)i * n, si, 1.0, form);
-                if (rc != B2G_OK)
-                    goto done;
-                (form == B2G_FP64 ? n_fp64 : n_mixed)++;
-                // A(i, j) = <b_i | sigma_j>, j <= i
-                dot_many(S, i + 1, B + (uint64_t)i * n, dots);
-                set_sub_row<<<1, kMaxSub, 0, st>>>(A, kMaxSub, i, dots);
+        double nrm2 = 0;
+        if (!cuda_ok(cudaMemcpyAsync(&nrm2, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st), "norm") ||
+            !cuda_ok(cudaStreamSynchronize(st), "sync"))
+            return -1;
+        if (!(nrm2 > 1e-28))
+            return 0;
+        normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)m * n, q, sc + 1, n);
+        m++;
+        return 1;
+    };
+    // sigma of the new basis vectors [msig, m) in one batched product, subspace rows
+    auto expand = [&](int pform) -> bool {
+        const int nn = m - msig;
+        if (nn <= 0)
+            return true;
+        if (!cuda_ok(cudaMemsetAsync(S + (uint64_t)msig * n, 0, sizeof(double) * n * nn, st), "memset"))
+            return false;
+        rc = b2g_heff_apply_batch(h, B + (uint64_t)msig * n, S + (uint64_t)msig * n, nn, 1.0, pform);
+        if (rc != B2G_OK)
+            return false;
+        (pform == B2G_FP64 ? n_fp64 : n_mixed) += nn;
+        for (int i = msig; i < m; i++) {
+            dot_many(S, i + 1, B + (uint64_t)i * n, dots);
+            set_sub_row<<<1, kMaxSub, 0, st>>>(A, kMaxSub, i, dots);
+        }
+        msig = m;
+        return true;
+    };
+    // Rayleigh-Ritz: X, SX = the k lowest Ritz vectors and their images, residual norms
+    auto ritz = [&]() -> bool {
+        jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
+        rotate_basis<<<g, 256, 0, st>>>(X, B, n, m, k, V, kMaxSub, n);
+        rotate_basis<<<g, 256, 0, st>>>(SX, S, n, m, k, V, kMaxSub, n);
+        for (int i = 0; i < k; i++) {
+            residual_olsen<<<g, 256, 0, st>>>(Q + (uint64_t)i * n, t, SX + (uint64_t)i * n,
+                                              X + (uint64_t)i * n, D, w + i, n, 0);
+            dot_many(Q + (uint64_t)i * n, 1, Q + (uint64_t)i * n, qqd + i);
+        }
+        return cuda_ok(cudaMemcpyAsync(lam.data(), w, sizeof(double) * m, cudaMemcpyDeviceToHost, st), "w") &&
+               cuda_ok(cudaMemcpyAsync(qq.data(), qqd, sizeof(double) * k, cudaMemcpyDeviceToHost, st), "qq") &&
+               cuda_ok(cudaStreamSynchronize(st), "sync");
+    };
+    auto all_below = [&](bool loose) {
+        for (int i = 0; i < k; i++) {
+            const double thr = loose ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i]) : conv_thrd;
+            if (!(qq[i] < thr))
+                return false;
+        }
+        return true;
+    };
+    // ---- initial basis: the k guesses, orthonormalised
+    if (!cuda_ok(cudaMemcpyAsync(D, diag, sizeof(double) * n, cudaMemcpyHostToDevice, st), "diag") ||
+        !cuda_ok(cudaMemcpyAsync(Q, psi, sizeof(double) * n * k, cudaMemcpyHostToDevice, st), "psi") ||
+        !cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A"))
+        goto done;
+    for (int i = 0; i < k; i++) {
+        const int r = append(Q + (uint64_t)i * n);
+        if (r < 0)
+            goto done;
+        if (r == 0) {
+            rc = fail(B2G_ERR_ARG, "b2g_davidson: initial guesses are linearly dependent");
+            goto done;
+        }
+    }
+    while (xiter < max_iter) {
+        xiter++;
+        since_refine++;
+        if (!expand(form) || !ritz())
+            goto done;
+        const bool reduced = form != B2G_FP64;
+        if (all_below(reduced && !have_exact) || (reduced && since_refine >= 40)) {
+            if (!reduced) {
+                converged = true;
+                break;
             }
-            jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
-            // x = B v0, s = S v0 (v0 = column 0 of V, stride kMaxSub)
-            rotate_basis<<<g, 256, 0, st>>>(x, B, n, m, 1, V, kMaxSub, n);
-            rotate_basis<<<g, 256, 0, st>>>(s, S, n, m, 1, V, kMaxSub, n);
-            residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 0);
-            dot_many(q, 1, q, sc + 1);
-            DAV_TRY(cudaMemcpyAsync(&lam, w, sizeof(double), cudaMemcpyDeviceToHost, st));
-            DAV_TRY(cudaMemcpyAsync(&qq, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
-            DAV_TRY(cudaStreamSynchronize(st));
-            // reduced-precision forms: before any exact product is in the basis,
-            // the subspace residual cannot fall below the product's rounding
-            // level, so the first pass stops at max(conv_thrd, (1e-6 lambda)^2)
-            const double thr = (form != B2G_FP64 && !have_exact)
-                                   ? std::max(conv_thrd, 1e-12 * lam * lam) : conv_thrd;
-            if (qq < thr || (form != B2G_FP64 && since_refine >= 40)) {
-                if (form == B2G_FP64) {
-                    converged = true;
-                    break;
-                }
-                // Defect correction: one FP64 product on the Ritz vector gives
-                // the exact residual r = H x - (x,Hx) x.  Converged when |r|^2 is
-                // below conv_thrd; otherwise the basis restarts from x with its
-                // exact sigma, and the correction built from r continues in the
-                // reduced-precision form (its rounding now only enters through
-                // the small correction coefficients).
-                dot_many(x, 1, x, sc + 1);
-                normalize_into<<<g, 256, 0, st>>>(B, x, sc + 1, n);
-                DAV_TRY(cudaMemcpyAsync(x, B, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-                DAV_TRY(cudaMemsetAsync(s, 0, sizeof(double) * n, st));
-                rc = b2g_heff_apply(h, x, s, 1.0, B2G_FP64);
-                if (rc != B2G_OK)
-                    goto done;
-                n_fp64++;
-                dot_many(x, 1, s, w);
-                residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 0);
-                dot_many(q, 1, q, sc + 1);
-                DAV_TRY(cudaMemcpyAsync(&lam, w, sizeof(double), cudaMemcpyDeviceToHost, st));
-                DAV_TRY(cudaMemcpyAsync(&qq, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
-                DAV_TRY(cudaStreamSynchronize(st));
-                if (qq < conv_thrd) {
-                    converged = true;
-                    break;
-                }
-                if (++n_refine > 30)
-                    break;
-                DAV_TRY(cudaMemcpyAsync(S, s, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-                set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, 1, w);
-                m = msig = 1;
-                have_exact = true;
-                since_refine = 0;
+            // Defect correction: FP64 products of the k Ritz vectors; Rayleigh-Ritz
+            // in their span with exact sigmas; converged when every exact residual
+            // is below conv_thrd, otherwise continue from this exact basis.
+            if (!cuda_ok(cudaMemcpyAsync(B, X, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st), "X"))
+                goto done;
+            m = k, msig = 0;
+            if (!cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A") ||
+                !expand(B2G_FP64) || !ritz())
+                goto done;
+            if (all_below(false)) {
+                converged = true;
+                break;
             }
-            // Olsen correction: q = K^-1 r - (x,K^-1 r)/(x,K^-1 x) K^-1 x
-            residual_olsen<<<g, 256, 0, st>>>(q, t, s, x, D, w, n, 1);
+            if (++n_refine > 30)
+                break;
+            have_exact = true;
+            since_refine = 0;
+        }
+        // ---- restart when the new corrections would not fit
+        int n_unconv = 0;
+        for (int i = 0; i < k; i++)
+            n_unconv += qq[i] >= (reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i])
+                                                          : conv_thrd);
+        if (m + n_unconv > def_max) {
+            rotate_basis<<<g, 256, 0, st>>>(R, B, n, m, def_min, V, kMaxSub, n);
+            if (!cuda_ok(cudaMemcpyAsync(B, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st), "B"))
+                goto done;
+            rotate_basis<<<g, 256, 0, st>>>(R, S, n, m, def_min, V, kMaxSub, n);
+            if (!cuda_ok(cudaMemcpyAsync(S, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st), "S"))
+                goto done;
+            set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, def_min, w);
+            m = msig = def_min;
+        }
+        // ---- Olsen corrections of the unconverged roots
+        int added = 0;
+        for (int i = 0; i < k; i++) {
+            const double thr = reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i]) : conv_thrd;
+            if (qq[i] < thr || m >= def_max)
+                continue;
+            double *q = Q + (uint64_t)i * n, *x = X + (uint64_t)i * n;
+            residual_olsen<<<g, 256, 0, st>>>(q, t, SX + (uint64_t)i * n, x, D, w + i, n, 1);
             dot_many(q, 1, x, sc + 2);
             dot_many(t, 1, x, sc + 3);
             olsen_update<<<g, 256, 0, st>>>(q, t, sc + 2, n);
-            if (m >= def_max) {
-                // restart with the def_min lowest Ritz vectors
-                rotate_basis<<<g, 256, 0, st>>>(R, B, n, m, def_min, V, kMaxSub, n);
-                DAV_TRY(cudaMemcpyAsync(B, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st));
-                rotate_basis<<<g, 256, 0, st>>>(R, S, n, m, def_min, V, kMaxSub, n);
-                DAV_TRY(cudaMemcpyAsync(S, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st));
-                set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, def_min, w);
-                m = msig = def_min;
-            }
-            // classical Gram-Schmidt, twice
-            for (int pass = 0; pass < 2; pass++) {
-                dot_many(B, m, q, coef);
-                combine<<<g, 256, 0, st>>>(q, 1.0, B, n, m, coef, -1.0, n);
-            }
-            dot_many(q, 1, q, sc + 1);
-            normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)m * n, q, sc + 1, n);
-            m++;
+            const int r = append(q);
+            if (r < 0)
+                goto done;
+            added += r;
         }
-        DAV_TRY(cudaGetLastError());
-        DAV_TRY(cudaMemcpyAsync(psi, x, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        DAV_TRY(cudaStreamSynchronize(st));
-        res->energy = lam;
-        res->n_iter = xiter;
-        res->n_apply_fp64 = n_fp64;
-        res->n_apply_mixed = n_mixed;
-        res->residual_norm2 = qq;
-        if (!converged)
-            rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_davidson: max_iter reached");
-        if (form == B2G_TF32X3 && b2g_heff_status(h) != B2G_OK)
-            rc = B2G_ERR_STATE;
+        if (added == 0 && msig == m)
+            break;  // no new direction: stagnated
     }
+    if (!cuda_ok(cudaGetLastError(), "kernels") ||
+        !cuda_ok(cudaMemcpyAsync(psi, X, sizeof(double) * n * k, cudaMemcpyDeviceToHost, st), "psi out") ||
+        !cuda_ok(cudaStreamSynchronize(st), "sync"))
+        goto done;
+    for (int i = 0; i < k; i++)
+        energies[i] = lam[i];
+    res->energy = lam[0];
+    res->n_iter = xiter;
+    res->n_apply_fp64 = n_fp64;
+    res->n_apply_mixed = n_mixed;
+    res->residual_norm2 = *std::max_element(qq.begin(), qq.begin() + k);
+    if (!converged)
+        rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_davidson: not converged within max_iter");
+    if (form == B2G_TF32X3 && b2g_heff_status(h) != B2G_OK)
+        rc = B2G_ERR_STATE;
 done:
-#undef DAV_TRY
     cudaStreamSynchronize(st);
     cleanup();
     return rc;
+}
+
+extern "C" int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double conv_thrd,
+                            int max_iter, int def_min, int def_max, int form,
+                            b2g_davidson_result *res) {
+    double e = 0.0;
+    return davidson_impl(h, diag, psi, 1, conv_thrd, max_iter, def_min, def_max, form, &e, res);
+}
+
+extern "C" int b2g_davidson_multi(b2g_heff *h, const double *diag, double *psi, int k,
+                                  double conv_thrd, int max_iter, int def_min, int def_max,
+                                  int form, double *energies, b2g_davidson_result *res) {
+    if (energies == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_davidson_multi: null energies");
+    return davidson_impl(h, diag, psi, k, conv_thrd, max_iter, def_min, def_max, form, energies, res);
 }

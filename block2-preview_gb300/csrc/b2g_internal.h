@@ -145,7 +145,6 @@ struct DevicePlan {
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;
     Tile2 *t2multi = nullptr;
-    void *t2_part = nullptr;        // partial tiles (double or float, sized for double)
     int64_t n_t2multi = 0;
     int32_t *lists = nullptr;
     Tc1Tile *tc1t = nullptr;
@@ -155,25 +154,33 @@ struct DevicePlan {
     TcSeg *tcs = nullptr;
     TcTile *tctile = nullptr;
     int32_t *tc_multi = nullptr;
-    float *tc_part = nullptr;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
     int64_t n_tct = 0, n_tcs = 0, n_tctile = 0, n_tc_multi = 0;
+};
+
+// Several right-hand sides (roots) in one launch: root r (blockIdx.y) reads
+// psi + r * psi, writes sigma + r * sigma, and uses its own slice of the work
+// and split-K partial buffers (strides in elements of the buffer's type).
+struct RootStrides {
+    int nroots = 1;
+    uint64_t psi = 0, sigma = 0, work = 0, part = 0;
 };
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
 // bounded wait gives up
 cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops32, const float *work,
-                             double *sigma, double scale, int *err, cudaStream_t s);
+                             double *sigma, float *part, double scale, int *err,
+                             const RootStrides &rs, cudaStream_t s);
 cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops32, const float *psi32,
-                             float *work, int *err, cudaStream_t s);
+                             float *work, int *err, const RootStrides &rs, cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>
 cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const T *psi, T *work,
-                               cudaStream_t s);
+                               const RootStrides &rs, cudaStream_t s);
 template <typename T>
 cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work, double *sigma,
-                               double scale, cudaStream_t s);
+                               T *part, double scale, const RootStrides &rs, cudaStream_t s);
 cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t s);
 // compute-ceiling probe: TFLOP/s of a register-resident FP64 FMA loop
 cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops);
@@ -192,9 +199,14 @@ struct b2g_heff {
     double *ops = nullptr;
     float *ops32 = nullptr;  // operators rounded to float (made on the first reduced-precision apply)
     float *psi32 = nullptr;  // psi rounded to float (per reduced-precision apply)
-    double *work = nullptr;
+    double *work = nullptr;  // cap_roots x work_size doubles (FP32 forms use it as floats)
     double *psi_stage = nullptr, *sigma_stage = nullptr; // device staging for the host entry
+    void *simt_part = nullptr;   // cap_roots x phase-2 partial tiles (doubles)
+    float *tc_part = nullptr;    // cap_roots x tensor-core partial tiles
+    int cap_roots = 0;           // roots the per-root buffers are sized for
+    int stage_roots = 0;         // roots the host staging buffers are sized for
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;
+    uint64_t simt_part_size = 0, tc_part_size = 0;  // per root, in elements
     b2g_heff_stats stats{};
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

@@ -28,11 +28,13 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
                                                    const Task1 *__restrict__ tasks, int64_t n_tasks,
                                                    const T *__restrict__ ops,
                                                    const T *__restrict__ psi,
-                                                   T *__restrict__ work) {
+                                                   T *__restrict__ work, RootStrides rs) {
     const int64_t t = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (t >= n_tasks)
         return;
+    psi += blockIdx.y * rs.psi;
+    work += blockIdx.y * rs.work;
     const Task1 tk = tasks[t];
     const WorkDesc wd = works[tk.u];
     const T *prow = psi + wd.a0 + (uint64_t)tk.r * wd.lda0;
@@ -90,8 +92,11 @@ __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tas
                                                    const T *__restrict__ ops,
                                                    const T *__restrict__ work,
                                                    double *__restrict__ sigma, T *__restrict__ part,
-                                                   double scale) {
+                                                   double scale, RootStrides rs) {
     const Task2 tk = tasks[blockIdx.x];
+    work += blockIdx.y * rs.work;
+    sigma += blockIdx.y * rs.sigma;
+    part += blockIdx.y * rs.part;
     const Region rg = regions[tk.g];
     const int lane = threadIdx.x & 31;
     const int wr = threadIdx.x >> 5;
@@ -148,8 +153,11 @@ template <typename T>
 __global__ void __launch_bounds__(128) simt_reduce(const Tile2 *__restrict__ tiles,
                                                    const Region *__restrict__ regions,
                                                    const T *__restrict__ part,
-                                                   double *__restrict__ sigma, double scale) {
+                                                   double *__restrict__ sigma, double scale,
+                                                   RootStrides rs) {
     const Tile2 tl = tiles[blockIdx.x];
+    part += blockIdx.y * rs.part;
+    sigma += blockIdx.y * rs.sigma;
     const Region rg = regions[tl.g];
     const int lane = threadIdx.x & 31, wr = threadIdx.x >> 5;
     const int r = tl.rb * 4 + wr;
@@ -227,36 +235,39 @@ cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t 
 
 template <typename T>
 cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const T *psi, T *work,
-                               cudaStream_t s) {
+                               const RootStrides &rs, cudaStream_t s) {
     if (p.n_t1 == 0)
         return cudaSuccess;
     const int64_t blocks = (p.n_t1 + 3) / 4;
-    simt_phase1<T><<<(unsigned)blocks, 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi, work);
+    simt_phase1<T><<<dim3((unsigned)blocks, rs.nroots), 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi,
+                                                                     work, rs);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work, double *sigma,
-                               double scale, cudaStream_t s) {
+                               T *part, double scale, const RootStrides &rs, cudaStream_t s) {
     if (p.n_t2 == 0)
         return cudaSuccess;
-    T *part = (T *)p.t2_part;
-    simt_phase2<T><<<(unsigned)p.n_t2, 128, 0, s>>>(p.t2, p.lists, p.contribs, p.regions, p.works,
-                                                    ops, work, sigma, part, scale);
+    simt_phase2<T><<<dim3((unsigned)p.n_t2, rs.nroots), 128, 0, s>>>(
+        p.t2, p.lists, p.contribs, p.regions, p.works, ops, work, sigma, part, scale, rs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.n_t2multi == 0)
         return e;
-    simt_reduce<T><<<(unsigned)p.n_t2multi, 128, 0, s>>>(p.t2multi, p.regions, part, sigma, scale);
+    simt_reduce<T><<<dim3((unsigned)p.n_t2multi, rs.nroots), 128, 0, s>>>(p.t2multi, p.regions, part,
+                                                                          sigma, scale, rs);
     return cudaGetLastError();
 }
 
 template cudaError_t launch_simt_phase1<double>(const DevicePlan &, const double *, const double *,
-                                                double *, cudaStream_t);
+                                                double *, const RootStrides &, cudaStream_t);
 template cudaError_t launch_simt_phase1<float>(const DevicePlan &, const float *, const float *,
-                                               float *, cudaStream_t);
+                                               float *, const RootStrides &, cudaStream_t);
 template cudaError_t launch_simt_phase2<double>(const DevicePlan &, const double *, const double *,
-                                                double *, double, cudaStream_t);
+                                                double *, double *, double, const RootStrides &,
+                                                cudaStream_t);
 template cudaError_t launch_simt_phase2<float>(const DevicePlan &, const float *, const float *,
-                                               double *, double, cudaStream_t);
+                                               double *, float *, double, const RootStrides &,
+                                               cudaStream_t);
 
 } // namespace b2g

@@ -157,8 +157,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_phase2_kernel(const TcTask *__restrict__ tasks, const TcTile *__restrict__ tiles,
                  const TcSeg *__restrict__ segs, const Region *__restrict__ regions,
                  const float *__restrict__ ops, const float *__restrict__ work,
-                 double *__restrict__ sigma, float *__restrict__ part, double scale, int *err) {
+                 double *__restrict__ sigma, float *__restrict__ part, double scale, int *err,
+                 RootStrides rs) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
+    work += blockIdx.y * rs.work;
+    sigma += blockIdx.y * rs.sigma;
+    part += blockIdx.y * rs.part;
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcSeg *sseg = (TcSeg *)(smem + kRingBytes);
     int32_t *stage_start = (int32_t *)(smem + kRingBytes + kSegBytes);
@@ -391,8 +395,10 @@ constexpr uint32_t kSmem1Bytes = kRing1Bytes + 128 * sizeof(Tc1Row) + 256 + 1024
 __global__ void __launch_bounds__(kThreads, 1)
 tc_phase1_kernel(const Tc1Tile *__restrict__ tiles, const Tc1Row *__restrict__ rowtab,
                  const float *__restrict__ ops, const float *__restrict__ psi,
-                 float *__restrict__ work, int *err) {
+                 float *__restrict__ work, int *err, RootStrides rs) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
+    psi += blockIdx.y * rs.psi;
+    work += blockIdx.y * rs.work;
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     Tc1Row *srow = (Tc1Row *)(smem + kRing1Bytes);
     uint64_t *full = (uint64_t *)(smem + kRing1Bytes + 128 * sizeof(Tc1Row));
@@ -553,8 +559,11 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restric
                                                         const TcTile *__restrict__ tiles,
                                                         const Region *__restrict__ regions,
                                                         const float *__restrict__ part,
-                                                        double *__restrict__ sigma, double scale) {
+                                                        double *__restrict__ sigma, double scale,
+                                                        RootStrides rs) {
     const TcTile tl = tiles[multi[blockIdx.x]];
+    part += blockIdx.z * rs.part;
+    sigma += blockIdx.z * rs.sigma;
     const Region rg = regions[tl.g];
     const int r0 = blockIdx.y * 8;
     if (r0 >= tl.rows)
@@ -578,7 +587,8 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const int32_t *__restric
 } // namespace
 
 cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops, const float *work,
-                             double *sigma, double scale, int *err, cudaStream_t s) {
+                             double *sigma, float *part, double scale, int *err,
+                             const RootStrides &rs, cudaStream_t s) {
     if (p.n_tct == 0)
         return cudaSuccess;
     static bool attr_set = false;
@@ -589,13 +599,13 @@ cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops, const float 
             return e;
         attr_set = true;
     }
-    tc_phase2_kernel<<<(unsigned)p.n_tct, kThreads, kSmemBytes, s>>>(
-        p.tct, p.tctile, p.tcs, p.regions, ops, work, sigma, p.tc_part, scale, err);
+    tc_phase2_kernel<<<dim3((unsigned)p.n_tct, rs.nroots), kThreads, kSmemBytes, s>>>(
+        p.tct, p.tctile, p.tcs, p.regions, ops, work, sigma, part, scale, err, rs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.n_tc_multi == 0)
         return e;
-    tc_reduce_kernel<<<dim3((unsigned)p.n_tc_multi, 16), 256, 0, s>>>(p.tc_multi, p.tctile, p.regions,
-                                                                      p.tc_part, sigma, scale);
+    tc_reduce_kernel<<<dim3((unsigned)p.n_tc_multi, 16, rs.nroots), 256, 0, s>>>(
+        p.tc_multi, p.tctile, p.regions, part, sigma, scale, rs);
     return cudaGetLastError();
 }
 
@@ -604,7 +614,7 @@ cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops, const float 
 namespace b2g {
 
 cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops, const float *psi, float *work,
-                             int *err, cudaStream_t s) {
+                             int *err, const RootStrides &rs, cudaStream_t s) {
     if (p.n_tc1t == 0)
         return cudaSuccess;
     static bool attr_set = false;
@@ -615,7 +625,8 @@ cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops, const float 
             return e;
         attr_set = true;
     }
-    tc_phase1_kernel<<<(unsigned)p.n_tc1t, kThreads, kSmem1Bytes, s>>>(p.tc1t, p.tc1r, ops, psi, work, err);
+    tc_phase1_kernel<<<dim3((unsigned)p.n_tc1t, rs.nroots), kThreads, kSmem1Bytes, s>>>(
+        p.tc1t, p.tc1r, ops, psi, work, err, rs);
     return cudaGetLastError();
 }
 

@@ -126,6 +126,14 @@ int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size
 int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form);
 /* same with HOST psi/sigma: copies psi in, applies, copies sigma out, synchronizes. */
 int b2g_heff_apply_host(b2g_heff *h, const double *psi, double *sigma, double scale, int form);
+/* sigma_r += scale * H_eff * psi_r for nroots right-hand sides stored one after
+ * another (psi: nroots * psi_size, sigma: nroots * sigma_size, DEVICE pointers),
+ * in one launch per kernel.  Replaces the one-vector-at-a-time application of
+ * state-averaged effective Hamiltonians (EffectiveHamiltonian<..., MultiMPS>
+ * ::operator(), src/dmrg/effective_hamiltonian.hpp:1690, and
+ * TensorFunctions::tensor_product_multi_multiply, src/core/tensor_functions.hpp:806-870). */
+int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
+                         int form);
 
 /*
  * sigma += scale * H_eff * psi in plain FP64 without allocating anything.
@@ -181,6 +189,20 @@ typedef struct {
 int b2g_davidson(b2g_heff *h, const double *diag, double *psi, double conv_thrd,
                  int max_iter, int def_min, int def_max, int form,
                  b2g_davidson_result *res);
+
+/*
+ * The k lowest eigenpairs (state-averaged roots; the reference's davidson
+ * with k = vs.size() > 1, src/core/iterative_matrix_functions.hpp:864-1173, as
+ * used by EffectiveHamiltonian<..., MultiMPS>::eigs,
+ * src/dmrg/effective_hamiltonian.hpp:1711-1797).  psi: k guesses in, k
+ * eigenvectors out (host, k * psi_size); energies: k eigenvalues.  Block
+ * variant: each iteration adds the Olsen corrections of all unconverged roots
+ * and computes their H_eff products in one b2g_heff_apply_batch call; the
+ * reduced-precision forms certify every root on FP64 residuals.
+ */
+int b2g_davidson_multi(b2g_heff *h, const double *diag, double *psi, int k, double conv_thrd,
+                       int max_iter, int def_min, int def_max, int form, double *energies,
+                       b2g_davidson_result *res);
 
 #ifdef __cplusplus
 }
