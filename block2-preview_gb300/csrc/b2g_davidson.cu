@@ -340,7 +340,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     };
     // orthogonalise Q_row (device vector q) against B[0..m) twice, append if not degenerate
     auto append = [&](double *q) -> int {
-        for (int pass = 0; pass < 2; pass++) {
+        for (int pass = 0; pass < 2 && m > 0; pass++) {
             dot_many(B, m, q, coef);
             combine<<<g, 256, 0, st>>>(q, 1.0, B, n, m, coef, -1.0, n);
         }
