@@ -234,6 +234,29 @@ def run_ours(args, rank, local_rank, world, dist):
         heff.apply_ptr(psi.data_ptr(), out.data_ptr(), 1.0, FORMS[name])
         heff.status()
         per_form[name]["rel_err_vs_fp64"] = float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref))
+    # ---- batched roots (state-averaged form): 8 right-hand sides per launch
+    nb = 8
+    xb = torch.randn((nb, prob.psi_size), dtype=torch.float64, device=dev)
+    yb = torch.zeros((nb, prob.sigma_size), dtype=torch.float64, device=dev)
+    for name in ("tf32x3", "fp64"):
+        form = FORMS[name]
+        for _ in range(2):
+            heff.apply_batch(xb, yb, 1.0, form)
+        heff.status()
+        reps = max(1, args.steps // 4)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            do_flush()
+            with torch.cuda.stream(stream):
+                yb.zero_()
+            heff.apply_batch(xb, yb, 1.0, form)
+        e1.record(stream)
+        heff.status()
+        ms = e0.elapsed_time(e1) / reps
+        per_form[name + "_batch8"] = {"value": flop * nb / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                                      "ms_per_step": ms, "roots": nb}
+    del xb, yb
     # ---- roofline of the dominant kernel of the headline form
     if head == "fp64":
         pk = C.c_double()
@@ -322,6 +345,25 @@ def run_ours(args, rank, local_rank, world, dist):
         "clocks": ck,
         "sigma_norm": nrm,
     }
+    # ---- Davidson on a real reference H_eff (Hubbard L=16 U=4 M=250 middle site):
+    # plain FP64 vs TF32x3 with FP64 defect correction, energy vs the reference's
+    from b2g import workloads
+    dprob = workloads.get("heff_hub16_su2_M250")
+    dh = b2g.EffectiveHamiltonian(ctx, dprob.seq(), dprob.ops, dprob.psi_size, dprob.sigma_size)
+    dav = {"workload": "heff_hub16_su2_M250", "reference_energy": dprob.meta["davidson_energy"],
+           "conv_thrd": dprob.meta["conv_thrd"]}
+    for name in ("fp64", "tf32x3"):
+        x = np.array(dprob.psi, copy=True)
+        e, ndav, nfl, tdav = dh.eigs(dprob.diag, x, conv_thrd=dprob.meta["conv_thrd"],
+                                     def_min=dprob.meta["def_min"], def_max=dprob.meta["def_max"],
+                                     form=FORMS[name])
+        r = dh.last_davidson
+        dav[name] = {"energy": e, "abs_err_vs_reference": abs(e + dprob.meta["const_e"]
+                                                               - dprob.meta["davidson_energy"]),
+                     "iterations": ndav, "fp64_products": r.n_apply_fp64,
+                     "reduced_products": r.n_apply_mixed, "seconds": tdav}
+    dh.close()
+    result["davidson"] = dav
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, nth, blas = cpu_replay_timing(prob, max_steps=10, budget_s=20.0, warmup=1)
         result["cpu_baseline"] = {
