@@ -62,6 +62,18 @@ class DavidsonResultC(C.Structure):
     ]
 
 
+class DmLayoutC(C.Structure):
+    _fields_ = [
+        ("trace_right", C.c_int32), ("n_psi_blocks", C.c_int32), ("psi_dm", C.c_void_p),
+        ("psi_rows", C.c_void_p), ("psi_cols", C.c_void_p), ("psi_off", C.c_void_p),
+        ("n_dm_blocks", C.c_int32), ("dm_dim", C.c_void_p),
+    ]
+
+
+class DmResultC(C.Structure):
+    _fields_ = [("error", C.c_double), ("n_kept", C.c_int32)]
+
+
 # every symbol declared in include/b2g.h, with its ctypes signature
 SIGNATURES = {
     "b2g_version": (C.c_int, []),
@@ -90,6 +102,9 @@ SIGNATURES = {
                                C.c_int, C.c_int, C.POINTER(DavidsonResultC)]),
     "b2g_davidson_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(DavidsonResultC)]),
+    "b2g_dm_truncate": (C.c_int, [C.c_void_p, C.POINTER(DmLayoutC), C.c_void_p, C.c_int, C.c_double,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.POINTER(DmResultC)]),
 }
 
 _lib = None

@@ -204,6 +204,58 @@ int b2g_davidson_multi(b2g_heff *h, const double *diag, double *psi, int k, doub
                        int max_iter, int def_min, int def_max, int form, double *energies,
                        b2g_davidson_result *res);
 
+/*
+ * Block layout of a two-site wavefunction and of its reduced density matrix.
+ * psi block a is psi_rows[a] x psi_cols[a], row-major at psi_off[a]; it
+ * contributes to density-matrix block psi_dm[a] (-1: none), which is square
+ * of size dm_dim[b].  trace_right != 0 traces out the right index (forward
+ * sweep: rho_b = sum_a psi_a psi_a^T over row quanta), else the left index
+ * (rho_b = sum_a psi_a^T psi_a over column quanta).  This is the mapping
+ * OperatorFunctions::trans_product applies, src/core/operator_functions.hpp:
+ * 777-838.
+ */
+typedef struct {
+    int32_t trace_right;
+    int32_t n_psi_blocks;
+    const int32_t *psi_dm;
+    const int32_t *psi_rows;
+    const int32_t *psi_cols;
+    const uint64_t *psi_off;
+    int32_t n_dm_blocks;
+    const int32_t *dm_dim;
+} b2g_dm_layout;
+
+typedef struct {
+    double error;   /* discarded weight: sum of the positive discarded eigenvalues */
+    int32_t n_kept; /* states kept over all blocks */
+} b2g_dm_result;
+
+/*
+ * Density-matrix truncation of one two-site step, FP64:
+ * MovingEnvironment::density_matrix (without noise) + split_density_matrix
+ * with TruncationTypes::Physical (src/dmrg/moving_environment.hpp:3554-3580,
+ * 3715-3843, 4250-4345).  rho is formed and diagonalised on the device;
+ * the k largest eigenvalues are kept (k = -1 keeps all), then trailing kept
+ * states below cutoff are dropped while more than one remains.
+ * Host buffers:
+ *   psi       the wavefunction (layout above)
+ *   eigvals   out, sum(dm_dim): each block's eigenvalues, ascending
+ *   kept      out, n_dm_blocks: states kept per block
+ *   rotation  out, room for sum(dm_dim^2): per block with kept[b] > 0, in
+ *             block order, the kept eigenvectors in ascending eigenvalue
+ *             order -- trace_right: dm_dim x kept (vectors as columns, the
+ *             left MPS tensor); else kept x dm_dim (vectors as rows, the
+ *             right MPS tensor)
+ *   wfn       out, room for the psi length: per psi block whose dm block
+ *             keeps states, in psi block order -- trace_right: rot^T psi_a
+ *             (kept x psi_cols); else psi_a rot^T (psi_rows x kept) -- the
+ *             whole scaled to unit norm (the reference's normalize = true)
+ * Returns B2G_ERR_UNSUPPORTED for a density-matrix block above 2048 states.
+ */
+int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *layout, const double *psi, int k,
+                    double cutoff, double *eigvals, int32_t *kept, double *rotation,
+                    double *wfn, b2g_dm_result *res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,3 +99,69 @@ def davidson(seq: PairSeq, ops, diag, psi0, conv_thrd, max_iter=500, def_min=2, 
                                    psi.size, conv_thrd, max_iter, def_min, def_max, nthreads,
                                    C.byref(e), C.byref(it))
     return e.value, it.value, psi, rc
+
+
+def dm_truncate(trace_right, psi_dm, psi_rows, psi_cols, psi_off, dm_dim, psi, k, cutoff):
+    """Density-matrix truncation restated in numpy (the checker of b2g_dm_truncate).
+
+    rho: OperatorFunctions::trans_product without noise
+    (src/core/operator_functions.hpp:777-838); selection:
+    MovingEnvironment::truncate_density_matrix, Physical
+    (src/dmrg/moving_environment.hpp:3715-3843); split: split_density_matrix
+    (moving_environment.hpp:4250-4345) with normalize = True.
+    Returns (eigenvalues per block ascending, kept per block, rotation blocks,
+    wavefunction blocks per psi block, discarded weight)."""
+    nb = len(dm_dim)
+    rho = [np.zeros((int(n), int(n))) for n in dm_dim]
+    blocks = []
+    for a in range(len(psi_dm)):
+        r, c, o = int(psi_rows[a]), int(psi_cols[a]), int(psi_off[a])
+        P = np.asarray(psi[o:o + r * c]).reshape(r, c)
+        blocks.append(P)
+        b = int(psi_dm[a])
+        if b >= 0:
+            rho[b] += P @ P.T if trace_right else P.T @ P
+    eigs, vecs = [], []
+    for b in range(nb):
+        w, v = np.linalg.eigh(rho[b]) if dm_dim[b] else (np.zeros(0), np.zeros((0, 0)))
+        eigs.append(w)
+        vecs.append(v)           # columns = eigenvectors, ascending
+    ss = [(b, j) for b in range(nb) for j in range(int(dm_dim[b]))]
+    k_total, error = len(ss), 0.0
+    if k != -1:
+        ss.sort(key=lambda p: -eigs[p[0]][p[1]])
+        for i in range(k, k_total):
+            x = eigs[ss[i][0]][ss[i][1]]
+            if x > 0:
+                error += x
+        kk = min(k, k_total)
+        while kk > 1 and eigs[ss[kk - 1][0]][ss[kk - 1][1]] < cutoff:
+            x = eigs[ss[kk - 1][0]][ss[kk - 1][1]]
+            if x > 0:
+                error += x
+            kk -= 1
+        ss = sorted(ss[:kk])
+    kept = np.zeros(nb, dtype=np.int32)
+    sel = [[] for _ in range(nb)]
+    for b, j in ss:
+        kept[b] += 1
+        sel[b].append(j)
+    rots = []
+    for b in range(nb):
+        if kept[b] == 0:
+            rots.append(None)
+            continue
+        V = vecs[b][:, sel[b]]                     # dm_dim x kept
+        rots.append(V.copy() if trace_right else V.T.copy())
+    wfns = []
+    for a in range(len(psi_dm)):
+        b = int(psi_dm[a])
+        if b < 0 or kept[b] == 0:
+            wfns.append(None)
+        elif trace_right:
+            wfns.append(rots[b].T @ blocks[a])
+        else:
+            wfns.append(blocks[a] @ rots[b].T)
+    nrm = np.sqrt(sum(float((x * x).sum()) for x in wfns if x is not None))
+    wfns = [None if x is None else x / nrm for x in wfns]
+    return eigs, kept, rots, wfns, error

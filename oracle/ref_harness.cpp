@@ -269,6 +269,81 @@ template <typename S> struct Dumper : CallbackKernel {
         w.scalar("norm2", nn);
         w.vec("psi", psi, "f8");
         w.man.flush();
+        dump_truncation(h);
+    }
+    // Density matrix of the converged psi, its spectrum, and the reference's
+    // truncation/split (MovingEnvironment::density_matrix / split_density_matrix,
+    // src/dmrg/moving_environment.hpp:3554-3580, 4250-4345) on copies.
+    void dump_truncation(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        Writer w(site_dir() + "/truncation");
+        const bool trace_right = d->isweep % 2 == 0;  // solve() starts forward and alternates
+        auto vmem = make_shared<VectorAllocator<double>>();
+        auto psi = make_shared<SparseMatrix<S, double>>(vmem);
+        psi->allocate(h->ket->info);
+        memcpy(psi->data, h->ket->data, sizeof(double) * psi->total_memory);
+        const S vacuum = d->me->ket->info->vacuum;
+        auto dm = MovingEnvironment<S, double, double>::density_matrix(vacuum, psi, trace_right, 0.0,
+                                                                       NoiseTypes::None);
+        // psi block -> dm block (the mapping trans_product uses)
+        vector<int32_t> psi_dm(psi->info->n), psi_rows(psi->info->n), psi_cols(psi->info->n);
+        vector<uint64_t> psi_off(psi->info->n);
+        for (int ia = 0; ia < psi->info->n; ia++) {
+            S q = trace_right ? psi->info->quanta[ia].get_bra(psi->info->delta_quantum)
+                              : -psi->info->quanta[ia].get_ket();
+            psi_dm[ia] = dm->info->find_state(q);
+            psi_rows[ia] = psi->info->n_states_bra[ia], psi_cols[ia] = psi->info->n_states_ket[ia];
+            psi_off[ia] = psi->info->block_shifts[ia];
+        }
+        vector<int32_t> dm_dim(dm->info->n);
+        vector<uint64_t> dm_off(dm->info->n);
+        vector<double> eig;
+        for (int ib = 0; ib < dm->info->n; ib++) {
+            dm_dim[ib] = dm->info->n_states_bra[ib], dm_off[ib] = dm->info->block_shifts[ib];
+            GMatrix<double> blk = (*dm)[ib];
+            vector<double> a(blk.data, blk.data + (size_t)blk.m * blk.n), ww(blk.m);
+            GMatrixFunctions<double>::eigs(GMatrix<double>(a.data(), blk.m, blk.n),
+                                           GDiagonalMatrix<double>(ww.data(), blk.m));
+            eig.insert(eig.end(), ww.begin(), ww.end());
+        }
+        vector<double> rho(dm->data, dm->data + dm->total_memory);
+        shared_ptr<SparseMatrix<S, double>> left, right;
+        vector<double> spectra;
+        const int M = (int)d->bond_dims[min((size_t)d->isweep, d->bond_dims.size() - 1)];
+        double err = MovingEnvironment<S, double, double>::split_density_matrix(
+            dm, psi, M, trace_right, true, left, right, d->cutoff, false, spectra, d->trunc_type);
+        auto blocks = [&](const shared_ptr<SparseMatrix<S, double>> &m, const char *tag, bool is_left) {
+            vector<int32_t> rows(m->info->n), cols(m->info->n), link(m->info->n);
+            vector<uint64_t> off(m->info->n);
+            for (int i = 0; i < m->info->n; i++) {
+                rows[i] = m->info->n_states_bra[i], cols[i] = m->info->n_states_ket[i];
+                off[i] = m->info->block_shifts[i];
+                // link: dm block (rotation side) or psi block (wavefunction side)
+                // (rotation blocks carry their dm block's quantum,
+                // rotation_matrix_info_from_density_matrix)
+                if (is_left == trace_right)
+                    link[i] = dm->info->find_state(m->info->quanta[i]);
+                else
+                    link[i] = psi->info->find_state(m->info->quanta[i]);
+            }
+            string t(tag);
+            w.vec(t + "_rows", rows, "i4"), w.vec(t + "_cols", cols, "i4");
+            w.vec(t + "_off", off, "u8"), w.vec(t + "_link", link, "i4");
+            w.arr(t + "_data", m->data, m->total_memory, "f8");
+        };
+        w.scalar("trace_right", trace_right);
+        w.scalar("bond_dim", M);
+        w.scalar("cutoff", d->cutoff);
+        w.scalar("error", err);
+        w.vec("psi_dm", psi_dm, "i4"), w.vec("psi_rows", psi_rows, "i4"), w.vec("psi_cols", psi_cols, "i4");
+        w.vec("psi_off", psi_off, "u8");
+        w.vec("dm_dim", dm_dim, "i4"), w.vec("dm_off", dm_off, "u8");
+        w.vec("dm_eig", eig, "f8"), w.vec("rho", rho, "f8");
+        blocks(left, "left", true);
+        blocks(right, "right", false);
+        w.man.flush();
+        right->deallocate(), left->deallocate(), dm->deallocate();  // stack order
+        right->info->deallocate(), left->info->deallocate(), dm->info->deallocate();
+        psi->deallocate();
     }
     // the next operator rotation after a dumped site is recorded too
     mutable bool want_rotation = false;

@@ -133,6 +133,20 @@ def run_case(name, args, desc):
         rot.save(rpath)
         print(f"{name}_rot: pairs={rmeta['n_pairs']} in={rot.psi_size} out={rot.sigma_size} "
               f"-> {os.path.getsize(rpath)} bytes")
+    # density matrix of the converged psi and the reference's truncation/split
+    tdir = os.path.join(out, site_dirs[0], "truncation")
+    if os.path.isdir(tdir):
+        ta, ts = read_dump(tdir)
+        tpath = os.path.join(HERE, name + "_dm.npz")
+        np.savez_compressed(
+            tpath, psi=post_a["psi"], trace_right=np.int32(ts["trace_right"]),
+            bond_dim=np.int32(ts["bond_dim"]), cutoff=np.float64(ts["cutoff"]),
+            error=np.float64(ts["error"]), **{k: v for k, v in ta.items()},
+            meta=np.array(json.dumps({"name": name + "_dm", "kind": "truncation",
+                                      "description": "density-matrix truncation after the site of "
+                                                     + name})))
+        print(f"{name}_dm: dm blocks={ta['dm_dim'].size} states={int(ta['dm_dim'].sum())} "
+              f"M={int(ts['bond_dim'])} error={ts['error']:.3e} -> {os.path.getsize(tpath)} bytes")
 
 
 def main():
