@@ -11,9 +11,8 @@
 //
 // Device work: rho blocks (batched SYRK, one thread per lower-triangle
 // element), the symmetric eigen-decomposition of every rho block (one CTA
-// per block, parallel cyclic Jacobi with round-robin pairing, matrix and
-// eigenvectors in global memory so blocks of any size fit), and the split
-// GEMMs.  The selection of the kept states (a sort of at most a few thousand
+// per block: Householder tridiagonalisation + implicit QL, matrices in
+// global memory, vectors in shared memory), and the split GEMMs.  The selection of the kept states (a sort of at most a few thousand
 // eigenvalues) runs on the host, in the reference's order.
 #include <algorithm>
 #include <cmath>
@@ -59,146 +58,301 @@ __global__ void rho_kernel(const double *__restrict__ psi, const int32_t *__rest
     rho[rho_off[b] + (int64_t)j * n + i] = s;
 }
 
-// One CTA per block: cyclic Jacobi, round-robin pairs (index 0 fixed).
-// A (n x n, symmetric, destroyed) -> eigenvalues w (ascending), eigenvectors
-// as ROWS of V (row j = eigenvector of w[j], the storage LAPACK leaves in a
-// row-major matrix).  Vt holds the accumulated rotation (columns = vectors).
-constexpr int kJacThreads = 256;
-constexpr int kJacMaxHalf = 1024;  // blocks up to 2048 states
-constexpr int kJacMaxSweeps = 60;
-__global__ void __launch_bounds__(kJacThreads) jacobi_block(double *__restrict__ Aall,
-                                                            double *__restrict__ Vtall,
-                                                            double *__restrict__ Vall,
-                                                            const int32_t *__restrict__ dim,
-                                                            const uint64_t *__restrict__ off,
-                                                            double *__restrict__ wall,
-                                                            const uint64_t *__restrict__ woff,
-                                                            int *__restrict__ perm_all,
-                                                            int *err) {
-    __shared__ double cs[kJacMaxHalf], sn[kJacMaxHalf];
-    __shared__ int pp[kJacMaxHalf], qq[kJacMaxHalf];
-    __shared__ double red[kJacThreads / 32];
-    __shared__ double thr_s;
-    __shared__ int rotated_s;
+// Block-wide sum over kThreads threads (all threads get the result).
+constexpr int kEigThreads = 256;
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();  // red may still be read by a previous call
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int k = 0; k < kEigThreads / 32; k++)
+        s += red[k];
+    return s;
+}
+
+// Symmetric eigen-decomposition of one density-matrix block per CTA, FP64:
+// Householder reduction to tridiagonal form, explicit accumulation of the
+// orthogonal factor, then the implicit QL iteration with Wilkinson shifts on
+// the tridiagonal (the published Bowdler-Martin-Reinsch-Wilkinson method, the
+// same reduction + QL family LAPACK's dsyev uses).  The FP64 pipe of an SM is
+// narrow, so the work is kept near the 9 n^3 flops of this method (a cyclic
+// Jacobi needs ~60 n^3).  Parallel structure: the reflector steps are
+// block-wide matrix-vector products and rank-2 updates; each QL iteration's
+// rotation chase is a short scalar recurrence (one thread) whose rotations
+// are then applied to all n rows of the eigenvector matrix in parallel.
+//
+// A: the block (n x n row-major, symmetric; overwritten by the reflectors).
+// Z: scratch n x n, holds Z^T (row i = eigenvector i before sorting).
+// V: out, row j = eigenvector of the j-th smallest eigenvalue (the storage
+//    LAPACK leaves in a row-major matrix).  w: out, eigenvalues ascending.
+// Dynamic shared memory: 7 n doubles (d, e, beta, v, p, rotation c, s;
+// the QL phase reuses beta..s as two rotation slots).
+constexpr int kQlMaxIter = 60;
+constexpr int kConsumerWarps = kEigThreads / 32 - kEigThreads / 128;  // warps with (warp & 3) != 0
+
+// The next QL iteration of the tridiagonal (d, e) (e[i] couples i and i+1):
+// finds the unreduced block [l, m] (|e| <= tol splits), applies one implicit
+// QL step with the Wilkinson shift from its top and records its plane
+// rotations (c, s) in rc/rs in the order they are generated (pair m-1-t,
+// m-t for rotation t).  state = {l, iterations spent on l}.  Returns false
+// when every eigenvalue has converged.  Rotations use one rsqrt instead of a
+// hypot and two divisions (|rho| stays far from the FP64 range limits).
+__device__ __forceinline__ bool ql_next(double *d, double *e, int n, double tol, int *state, double *rc,
+                        double *rs, int &m_out, int &cnt_out, int *err) {
+    int l = state[0], iter = state[1];
+    bool produced = false;
+    while (l < n && !produced) {
+        int m = l;
+        for (; m < n - 1; m++)
+            if (fabs(e[m]) <= tol)
+                break;
+        if (m == l) {
+            l++, iter = 0;
+            continue;
+        }
+        if (iter >= kQlMaxIter) {  // no convergence: flag it and leave this eigenvalue
+            atomicExch(err, 2);
+            l++, iter = 0;
+            continue;
+        }
+        iter++;
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        const double rr = hypot(g, 1.0);
+        g = d[m] - d[l] + e[l] / (g + (g >= 0 ? rr : -rr));
+        double s = 1.0, c = 1.0, pp = 0.0;
+        int cnt = 0;
+        bool underflow = false;
+        for (int i = m - 1; i >= l; i--) {
+            const double f = s * e[i], bb = c * e[i];
+            const double h = fma(f, f, g * g);
+            if (h == 0.0) {
+                e[i + 1] = 0.0;
+                d[i + 1] -= pp;
+                e[m] = 0.0;
+                underflow = true;
+                break;
+            }
+            const double inv = rsqrt(h);
+            e[i + 1] = h * inv;
+            s = f * inv, c = g * inv;
+            g = d[i + 1] - pp;
+            const double r = (d[i] - g) * s + 2.0 * c * bb;
+            pp = s * r;
+            d[i + 1] = g + pp;
+            g = c * r - bb;
+            rc[cnt] = c, rs[cnt] = s, cnt++;
+        }
+        if (!underflow) {
+            d[l] -= pp;
+            e[l] = g;
+            e[m] = 0.0;
+        }
+        if (cnt > 0) {
+            m_out = m, cnt_out = cnt;
+            produced = true;
+        }
+    }
+    state[0] = l, state[1] = iter;
+    return produced;
+}
+constexpr int kDmMaxDim = 4000;  // 7 n doubles of shared memory stay below 227 KB
+__global__ void __launch_bounds__(kEigThreads) eig_block(double *__restrict__ Aall,
+                                                         double *__restrict__ Zall,
+                                                         double *__restrict__ Vall,
+                                                         const int32_t *__restrict__ dim,
+                                                         const uint64_t *__restrict__ off,
+                                                         double *__restrict__ wall,
+                                                         const uint64_t *__restrict__ woff,
+                                                         int *__restrict__ perm_all, int *err) {
+    extern __shared__ double sm[];
+    __shared__ double red[kEigThreads / 32];
+    __shared__ int item_m[2], item_cnt[2], ql_state[2];
+    __shared__ double ql_tol;
     const int b = blockIdx.x;
     const int n = dim[b];
     if (n == 0)
         return;
-    double *A = Aall + off[b], *Vt = Vtall + off[b], *V = Vall + off[b], *w = wall + woff[b];
-    int *perm = perm_all + woff[b] + b;  // n + 1 slots per block
-    const int tid = threadIdx.x;
-    const int mm = n + (n & 1), half = mm / 2;
-    if (half > kJacMaxHalf) {
+    double *A = Aall + off[b], *Z = Zall + off[b], *V = Vall + off[b], *w = wall + woff[b];
+    int *perm = perm_all + woff[b] + b;
+    double *d = sm, *e = sm + n, *beta = sm + 2 * n, *v = sm + 3 * n, *p = sm + 4 * n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int nwarps = kEigThreads / 32;
+
+    // ---- 1. Householder reduction: step k zeroes A[k+2.., k]
+    for (int k = 0; k + 2 < n; k++) {
+        const int len = n - k - 1;
+        const double *xk = A + (int64_t)k * n + k + 1;  // row k right of the diagonal
+        double ss = 0.0;
+        for (int i = tid; i < len; i += kEigThreads)
+            ss += xk[i] * xk[i];
+        const double sigma = block_sum(ss, red);
+        const double x0 = xk[0];
+        const double tail = sigma - x0 * x0;
         if (tid == 0)
-            atomicExch(err, 1);
-        return;
+            d[k] = A[(int64_t)k * n + k];
+        if (tail <= 0.0) {  // already tridiagonal in this column
+            if (tid == 0)
+                e[k] = x0, beta[k] = 0.0;
+            __syncthreads();
+            continue;
+        }
+        const double alpha = x0 >= 0 ? -sqrt(sigma) : sqrt(sigma);
+        const double bt = 1.0 / (sigma - x0 * alpha);
+        for (int i = tid; i < len; i += kEigThreads)
+            v[i] = i == 0 ? x0 - alpha : xk[i];
+        __syncthreads();
+        // p = beta * B v,  B = A[k+1.., k+1..]  (one warp per row)
+        for (int i = warp; i < len; i += nwarps) {
+            const double *Bi = A + (int64_t)(k + 1 + i) * n + k + 1;
+            double acc = 0.0;
+            for (int j = lane; j < len; j += 32)
+                acc = fma(Bi[j], v[j], acc);
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0)
+                p[i] = bt * acc;
+        }
+        __syncthreads();
+        double vp = 0.0;
+        for (int i = tid; i < len; i += kEigThreads)
+            vp += v[i] * p[i];
+        const double K = 0.5 * bt * block_sum(vp, red);
+        for (int i = tid; i < len; i += kEigThreads)
+            p[i] -= K * v[i];  // p <- w
+        __syncthreads();
+        // B <- B - v w^T - w v^T
+        for (int i = warp; i < len; i += nwarps) {
+            double *Bi = A + (int64_t)(k + 1 + i) * n + k + 1;
+            const double vi = v[i], wi = p[i];
+            for (int j = lane; j < len; j += 32)
+                Bi[j] -= vi * p[j] + wi * v[j];
+        }
+        // keep the reflector in row k for the accumulation
+        for (int i = tid; i < len; i += kEigThreads)
+            A[(int64_t)k * n + k + 1 + i] = v[i];
+        if (tid == 0)
+            e[k] = alpha, beta[k] = bt;
+        __syncthreads();
     }
-    for (int64_t e = tid; e < (int64_t)n * n; e += kJacThreads)
-        Vt[e] = (e / n == e % n) ? 1.0 : 0.0;
-    for (int i = tid; i < mm; i += kJacThreads)
-        perm[i] = i;
+    if (tid == 0) {
+        if (n >= 2) {
+            d[n - 2] = A[(int64_t)(n - 2) * n + n - 2];
+            e[n - 2] = A[(int64_t)(n - 2) * n + n - 1];
+        }
+        d[n - 1] = A[(int64_t)(n - 1) * n + n - 1];
+        e[n - 1] = 0.0;
+    }
+    // ---- 2. Q = H_0 H_1 ... H_{n-3}, built backwards, stored transposed in Z
+    for (int64_t q = tid; q < (int64_t)n * n; q += kEigThreads)
+        Z[q] = (q / n == q % n) ? 1.0 : 0.0;
     __syncthreads();
-    // rotation threshold: 1e-18 of the Frobenius norm, far below the
-    // eps * |A| absolute accuracy LAPACK's dsyev gives
-    {
-        double st = 0.0;
-        for (int64_t e = tid; e < (int64_t)n * n; e += kJacThreads)
-            st += A[e] * A[e];
-        for (int o = 16; o > 0; o >>= 1)
-            st += __shfl_down_sync(0xffffffffu, st, o);
-        if ((tid & 31) == 0)
-            red[tid >> 5] = st;
+    for (int k = n - 3; k >= 0; k--) {
+        const double bt = beta[k];
+        if (bt == 0.0)
+            continue;
+        const int len = n - k - 1;
+        for (int i = tid; i < len; i += kEigThreads)
+            v[i] = A[(int64_t)k * n + k + 1 + i];
         __syncthreads();
-        if (tid == 0) {
-            double t = 0.0;
-            for (int k = 0; k < kJacThreads / 32; k++)
-                t += red[k];
-            thr_s = 1e-18 * sqrt(t);
+        // y_i = sum_r v_r Q[r][i] = (row i of Z) . v ; then Z[i][r] -= beta y_i v_r
+        for (int i = warp; i < len; i += nwarps) {
+            const double *Zi = Z + (int64_t)(k + 1 + i) * n + k + 1;
+            double acc = 0.0;
+            for (int j = lane; j < len; j += 32)
+                acc = fma(Zi[j], v[j], acc);
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0)
+                p[i] = bt * acc;
+        }
+        __syncthreads();
+        for (int i = warp; i < len; i += nwarps) {
+            double *Zi = Z + (int64_t)(k + 1 + i) * n + k + 1;
+            const double yi = p[i];
+            for (int j = lane; j < len; j += 32)
+                Zi[j] -= yi * v[j];
         }
         __syncthreads();
     }
-    const double thr = thr_s;
-    for (int sweep = 0; sweep < kJacMaxSweeps; sweep++) {
-        if (tid == 0)
-            rotated_s = 0;
-        __syncthreads();
-        for (int step = 0; step < mm - 1; step++) {
-            for (int k = tid; k < half; k += kJacThreads) {
-                int p = perm[k], q = perm[mm - 1 - k];
-                if (p > q) {
-                    const int t = p;
-                    p = q, q = t;
-                }
-                pp[k] = p, qq[k] = q;
-                double c = 1.0, s = 0.0;
-                if (q < n) {
-                    const double apq = A[(int64_t)p * n + q];
-                    if (fabs(apq) > thr) {
-                        rotated_s = 1;
-                        const double th = (A[(int64_t)q * n + q] - A[(int64_t)p * n + p]) / (2.0 * apq);
-                        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-                        c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                    }
-                }
-                cs[k] = c, sn[k] = s;
-            }
-            __syncthreads();
-            // columns: A <- A J, Vt <- Vt J
-            for (int64_t e = tid; e < (int64_t)half * n; e += kJacThreads) {
-                const int k = (int)(e / n), r = (int)(e % n), p = pp[k], q = qq[k];
-                if (q >= n || sn[k] == 0.0)
-                    continue;
-                const double c = cs[k], s = sn[k];
-                double *Ar = A + (int64_t)r * n, *Vr = Vt + (int64_t)r * n;
-                const double arp = Ar[p], arq = Ar[q];
-                Ar[p] = c * arp - s * arq, Ar[q] = s * arp + c * arq;
-                const double vrp = Vr[p], vrq = Vr[q];
-                Vr[p] = c * vrp - s * vrq, Vr[q] = s * vrp + c * vrq;
-            }
-            __syncthreads();
-            // rows: A <- J^T A
-            for (int64_t e = tid; e < (int64_t)half * n; e += kJacThreads) {
-                const int k = (int)(e / n), cidx = (int)(e % n), p = pp[k], q = qq[k];
-                if (q >= n || sn[k] == 0.0)
-                    continue;
-                const double c = cs[k], s = sn[k];
-                const double apc = A[(int64_t)p * n + cidx], aqc = A[(int64_t)q * n + cidx];
-                // the eliminated pair is set to zero exactly
-                A[(int64_t)p * n + cidx] = cidx == q ? 0.0 : c * apc - s * aqc;
-                A[(int64_t)q * n + cidx] = cidx == p ? 0.0 : s * apc + c * aqc;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                const int last = perm[mm - 1];
-                for (int k = mm - 1; k > 1; k--)
-                    perm[k] = perm[k - 1];
-                perm[1] = last;
-            }
-            __syncthreads();
-        }
-        if (rotated_s == 0)
+    // ---- 3. implicit QL with Wilkinson shifts on (d, e), two-stage pipeline:
+    // thread 0 chases QL iteration t+1 (a scalar recurrence producing its
+    // plane rotations) while warps 1.. apply the rotations of iteration t to
+    // the rows of Z; one barrier per iteration.  Rotation slots reuse the
+    // reflector scratch: slot s holds c at sm + (2 + 2s) n and s at + n.
+    if (tid == 0) {
+        // Deflation is tested against the norm of the whole tridiagonal
+        // (absolute accuracy eps * |rho|, as LAPACK's): a local test never
+        // deflates the numerically-zero tail of a rank-deficient rho.
+        double anorm = 0.0;
+        for (int i = 0; i < n; i++)
+            anorm = fmax(anorm, fabs(d[i]) + fabs(e[i]));
+        ql_state[0] = 0, ql_state[1] = 0;
+        ql_tol = 2.220446049250313e-16 * anorm;
+        int m = -1, cnt = 0;
+        if (!ql_next(d, e, n, ql_tol, ql_state, sm + 2 * n, sm + 3 * n, m, cnt, err))
+            m = -1;
+        item_m[0] = m, item_cnt[0] = cnt;
+    }
+    __syncthreads();
+    for (int t = 0;; t++) {  // at most kQlMaxIter * n items
+        const int cur = t & 1;
+        const int m = item_m[cur], cnt = item_cnt[cur];
+        if (m < 0)
             break;
+        if (tid == 0) {
+            const int nx = cur ^ 1;
+            int m2 = -1, cnt2 = 0;
+            if (!ql_next(d, e, n, ql_tol, ql_state, sm + (2 + 2 * nx) * n, sm + (3 + 2 * nx) * n, m2,
+                         cnt2, err))
+                m2 = -1;
+            item_m[nx] = m2, item_cnt[nx] = cnt2;
+        } else if ((warp & 3) != 0) {
+            // The consumers are the warps off thread 0's SM sub-partition, so
+            // the chase keeps that sub-partition's FP64 pipe to itself.
+            // Rotation t2 acts on eigenvector pair (m-1-t2, m-t2).
+            const double *cs = sm + (2 + 2 * cur) * n, *sn = cs + n;
+            const int cw = warp - 1 - (warp >> 2);  // 0 .. kConsumerWarps-1
+            for (int r = cw * 32 + lane; r < n; r += kConsumerWarps * 32) {
+                double carry = Z[(int64_t)m * n + r];
+                double zn = Z[(int64_t)(m - 1) * n + r];
+                for (int t2 = 0; t2 < cnt; t2++) {
+                    const int i = m - 1 - t2;
+                    const double zi = zn;
+                    if (t2 + 1 < cnt)
+                        zn = Z[(int64_t)(i - 1) * n + r];
+                    const double c = cs[t2], sv = sn[t2];
+                    Z[(int64_t)(i + 1) * n + r] = sv * zi + c * carry;
+                    carry = c * zi - sv * carry;
+                }
+                Z[(int64_t)(m - cnt) * n + r] = carry;
+            }
+        }
         __syncthreads();
     }
-    // sort ascending (selection sort by one thread; n is at most a few hundred)
+    // ---- 4. ascending order (a stable selection on one thread; n is small)
     if (tid == 0) {
         for (int i = 0; i < n; i++)
             perm[i] = i;
         for (int i = 0; i < n; i++) {
             int bi = i;
             for (int j = i + 1; j < n; j++)
-                if (A[(int64_t)perm[j] * n + perm[j]] < A[(int64_t)perm[bi] * n + perm[bi]])
+                if (d[perm[j]] < d[perm[bi]])
                     bi = j;
-            const int t = perm[i];
-            perm[i] = perm[bi], perm[bi] = t;
+            const int t = perm[bi];
+            for (int j = bi; j > i; j--)
+                perm[j] = perm[j - 1];
+            perm[i] = t;
         }
         for (int i = 0; i < n; i++)
-            w[i] = A[(int64_t)perm[i] * n + perm[i]];
+            w[i] = d[perm[i]];
     }
     __syncthreads();
-    for (int64_t e = tid; e < (int64_t)n * n; e += kJacThreads) {
-        const int j = (int)(e / n), r = (int)(e % n);  // V row j = column perm[j] of Vt
-        V[e] = Vt[(int64_t)r * n + perm[j]];
+    for (int64_t q = tid; q < (int64_t)n * n; q += kEigThreads) {
+        const int j = (int)(q / n), r = (int)(q % n);
+        V[q] = Z[(int64_t)perm[j] * n + r];
     }
 }
 
@@ -237,6 +391,9 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
         return fail(B2G_ERR_ARG, "b2g_dm_truncate: k must be -1 (keep all) or non-negative");
     if (nb > 65535)
         return fail(B2G_ERR_UNSUPPORTED, "b2g_dm_truncate: more than 65535 density-matrix blocks");
+    for (int b = 0; b < nb; b++)
+        if (lay->dm_dim[b] > kDmMaxDim)
+            return fail(B2G_ERR_UNSUPPORTED, "b2g_dm_truncate: density-matrix block above 4000 states");
     const bool tr = lay->trace_right != 0;
     // ---- host-side layout checks and tables
     uint64_t psi_size = 0, psi_sum = 0;
@@ -338,7 +495,9 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
             rho_kernel<<<dim3((unsigned)((cells + 255) / 256), nb), 256, 0, s>>>(
                 d_psi, d_lptr, d_list, d_prow, d_pcol, d_poff, d_dim, d_roff, d_rho, tr ? 1 : 0);
             DM_TRY(cudaGetLastError());
-            jacobi_block<<<nb, kJacThreads, 0, s>>>(d_rho, d_vt, d_v, d_dim, d_roff, d_w, d_woff, d_perm, d_err);
+            const size_t smem = sizeof(double) * 7 * (size_t)maxdim;
+            DM_TRY(cudaFuncSetAttribute(eig_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            eig_block<<<nb, kEigThreads, smem, s>>>(d_rho, d_vt, d_v, d_dim, d_roff, d_w, d_woff, d_perm, d_err);
             DM_TRY(cudaGetLastError());
         }
         std::vector<double> w(wtot);
@@ -347,7 +506,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
         DM_TRY(cudaMemcpyAsync(&errflag, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
         DM_TRY(cudaStreamSynchronize(s));
         if (errflag) {
-            rc = fail(B2G_ERR_UNSUPPORTED, "b2g_dm_truncate: density-matrix block above 2048 states");
+            rc = fail(B2G_ERR_NOT_CONVERGED, "b2g_dm_truncate: QL iteration did not converge");
             goto done;
         }
         memcpy(eigvals, w.data(), sizeof(double) * wtot);

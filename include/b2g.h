@@ -250,7 +250,8 @@ typedef struct {
  *             keeps states, in psi block order -- trace_right: rot^T psi_a
  *             (kept x psi_cols); else psi_a rot^T (psi_rows x kept) -- the
  *             whole scaled to unit norm (the reference's normalize = true)
- * Returns B2G_ERR_UNSUPPORTED for a density-matrix block above 2048 states.
+ * Returns B2G_ERR_UNSUPPORTED for a density-matrix block above 4000 states,
+ * B2G_ERR_NOT_CONVERGED if a QL iteration needs more than 60 steps.
  */
 int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *layout, const double *psi, int k,
                     double cutoff, double *eigvals, int32_t *kept, double *rotation,
