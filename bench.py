@@ -226,18 +226,26 @@ def run_ours(args, rank, local_rank, world, dist):
         if name == head:
             head_res = (total, t_wall, p1, p2, ck, nrm)
     total, t_wall, p1, p2, ck, nrm = head_res
-    # sigma of each form against FP64 (relative 2-norm), same psi
-    ref = torch.zeros_like(sig)
+    # sigma of each form against FP64 (relative 2-norm), same psi; every tensor op
+    # on the library's stream, synchronized before reading
+    with torch.cuda.stream(stream):
+        ref = torch.zeros_like(sig)
     heff.apply_ptr(psi.data_ptr(), ref.data_ptr(), 1.0, FORMS["fp64"])
+    heff.status()
     for name in FORMS:
-        out = torch.zeros_like(sig)
+        with torch.cuda.stream(stream):
+            out = torch.zeros_like(sig)
         heff.apply_ptr(psi.data_ptr(), out.data_ptr(), 1.0, FORMS[name])
         heff.status()
-        per_form[name]["rel_err_vs_fp64"] = float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref))
+        with torch.cuda.stream(stream):
+            rel = torch.linalg.norm(out - ref) / torch.linalg.norm(ref)
+        stream.synchronize()
+        per_form[name]["rel_err_vs_fp64"] = float(rel)
     # ---- batched roots (state-averaged form): 8 right-hand sides per launch
     nb = 8
     xb = torch.randn((nb, prob.psi_size), dtype=torch.float64, device=dev)
     yb = torch.zeros((nb, prob.sigma_size), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()  # made on torch's stream, used on the library's
     for name in ("tf32x3", "fp64"):
         form = FORMS[name]
         for _ in range(2):
@@ -273,9 +281,13 @@ def run_ours(args, rank, local_rank, world, dist):
         peak_src = ("MEASURED_PEAKS.json bf16_tflops (burst) of measured; dense TF32 is nominally half of "
                     "BF16 and split-TF32x3 issues 3 MMAs per useful product, so 1/6 of this is the "
                     "useful-FLOP ceiling of this kernel")
-        k2 = ("tc_phase2_kernel (tcgen05.mma kind::tf32 x3, TMEM accumulator)" if head == "tf32x3"
-              else "simt_phase2<float>")
-        k1 = "simt_phase1<float> (GEMM0 W = psi op(R), FP32)"
+        if head == "tf32x3":
+            k2 = ("g1_build_w + g1_kernel + g1_reduce (GEMM1 sigma += alpha op(L) W: bulk-copied "
+                  "TF32 hi/lo operand images, tcgen05.mma kind::tf32 x3, TMEM accumulator)")
+            k1 = "tc_phase1_kernel (GEMM0 W = psi op(R), tcgen05.mma kind::tf32 x3)"
+        else:
+            k2 = "simt_phase2<float> (GEMM1, FP32)"
+            k1 = "simt_phase1<float> (GEMM0 W = psi op(R), FP32)"
     if p2 >= p1:
         kname, kflop, kms = k2, flop1, p2
     else:

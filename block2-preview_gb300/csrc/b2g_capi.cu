@@ -33,8 +33,9 @@ template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaSt
 static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
-    cudaFree(p.tct), cudaFree(p.tcs), cudaFree(p.tctile), cudaFree(p.tc_multi);
     cudaFree(p.t2multi), cudaFree(p.tc1t), cudaFree(p.tc1r);
+    cudaFree(p.g1tile), cudaFree(p.g1stage), cudaFree(p.g1task), cudaFree(p.g1aimg);
+    cudaFree(p.g1wimg), cudaFree(p.g1red), cudaFree(p.g1cover);
     p = DevicePlan();
 }
 
@@ -43,21 +44,48 @@ static int ensure_roots(b2g_heff *h, int nroots) {
     if (nroots <= h->cap_roots)
         return B2G_OK;
     B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
-    cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
-    h->work = nullptr, h->simt_part = nullptr, h->tc_part = nullptr, h->psi32 = nullptr;
+    cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->psi32);
+    h->work = nullptr, h->simt_part = nullptr, h->psi32 = nullptr;
     h->cap_roots = 0;
     const size_t R = (size_t)nroots;
     if ((h->work_size && cudaMalloc(&h->work, sizeof(double) * h->work_size * R) != cudaSuccess) ||
         (h->simt_part_size &&
          cudaMalloc(&h->simt_part, sizeof(double) * h->simt_part_size * R) != cudaSuccess) ||
-        (h->tc_part_size && cudaMalloc(&h->tc_part, sizeof(float) * h->tc_part_size * R) != cudaSuccess) ||
         (h->psi_size && cudaMalloc(&h->psi32, sizeof(float) * h->psi_size * R) != cudaSuccess)) {
-        cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
-        h->work = nullptr, h->simt_part = nullptr, h->tc_part = nullptr, h->psi32 = nullptr;
+        cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->psi32);
+        h->work = nullptr, h->simt_part = nullptr, h->psi32 = nullptr;
         return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the per-root work buffers of " +
                                        std::to_string(nroots) + " roots");
     }
     h->cap_roots = nroots;
+    return B2G_OK;
+}
+
+// buffers of the image-fed tensor-core GEMM1 (TF32x3 form only, made on its
+// first use): A images once, W images and partial tiles per root
+static int ensure_g1(b2g_heff *h, int nroots) {
+    const DevicePlan &p = h->plan;
+    if (h->g1_aimg == nullptr && p.g1_abytes) {
+        if (cudaMalloc(&h->g1_aimg, p.g1_abytes) != cudaSuccess) {
+            h->g1_aimg = nullptr;
+            return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the GEMM1 operator images");
+        }
+        B2G_CUDA_TRY(launch_g1_build_a(p, h->ops32, h->g1_aimg, h->ctx->stream));
+    }
+    if (nroots <= h->g1_roots)
+        return B2G_OK;
+    B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+    cudaFree(h->g1_wimg), cudaFree(h->g1_part);
+    h->g1_wimg = nullptr, h->g1_part = nullptr, h->g1_roots = 0;
+    const size_t R = (size_t)nroots;
+    if ((p.g1_wbytes && cudaMalloc(&h->g1_wimg, p.g1_wbytes * R) != cudaSuccess) ||
+        (p.g1_part && cudaMalloc(&h->g1_part, sizeof(float) * p.g1_part * R) != cudaSuccess)) {
+        cudaFree(h->g1_wimg), cudaFree(h->g1_part);
+        h->g1_wimg = nullptr, h->g1_part = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the GEMM1 work images of " +
+                                       std::to_string(nroots) + " roots");
+    }
+    h->g1_roots = nroots;
     return B2G_OK;
 }
 
@@ -134,7 +162,8 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     auto bail = [&](int code) {
         free_plan(h->plan);
         cudaFree(h->ops), cudaFree(h->work), cudaFree(h->err);
-        cudaFree(h->simt_part), cudaFree(h->tc_part), cudaFree(h->psi32);
+        cudaFree(h->simt_part), cudaFree(h->psi32);
+        cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part);
         delete h;
         return code;
     };
@@ -150,7 +179,6 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
             return bail(fail(B2G_ERR_CUDA, "operator blob upload failed"));
     }
     h->simt_part_size = (uint64_t)4 * 256 * hp.t2_part_tiles;
-    h->tc_part_size = hp.tc_part_size;
     if ((rc = ensure_roots(h, 1)) != B2G_OK)
         return bail(rc);
     if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) {
@@ -163,18 +191,20 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
         (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
         (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
-        (rc = upload(hp.tct, &p.tct, s)) || (rc = upload(hp.tcs, &p.tcs, s)) ||
-        (rc = upload(hp.tctile, &p.tctile, s)) || (rc = upload(hp.tc_multi, &p.tc_multi, s)) ||
         (rc = upload(hp.t2multi, &p.t2multi, s)) || (rc = upload(hp.tc1t, &p.tc1t, s)) ||
-        (rc = upload(hp.tc1r, &p.tc1r, s)))
+        (rc = upload(hp.tc1r, &p.tc1r, s)) || (rc = upload(hp.g1tile, &p.g1tile, s)) ||
+        (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
+        (rc = upload(hp.g1aimg, &p.g1aimg, s)) || (rc = upload(hp.g1wimg, &p.g1wimg, s)) ||
+        (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)))
         return bail(rc);
+    p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
+    p.n_g1wimg = (int64_t)hp.g1wimg.size(), p.n_g1red = (int64_t)hp.g1red.size();
+    p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
     p.n_tc1t = (int64_t)hp.tc1t.size();
     p.n_t2multi = (int64_t)hp.t2multi.size();
-    p.n_tctile = (int64_t)hp.tctile.size(), p.n_tc_multi = (int64_t)hp.tc_multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
     p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
     p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
-    p.n_tct = (int64_t)hp.tct.size(), p.n_tcs = (int64_t)hp.tcs.size();
     if (cudaStreamSynchronize(s) != cudaSuccess)
         return bail(fail(B2G_ERR_CUDA, "plan upload failed"));
     b2g_heff_stats &st = h->stats;
@@ -189,7 +219,9 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     st.plan_bytes = sizeof(WorkDesc) * hp.works.size() + sizeof(Contrib) * hp.contribs.size() +
                     sizeof(Region) * hp.regions.size() + sizeof(Task1) * hp.t1.size() +
                     sizeof(Task2) * hp.t2.size() + sizeof(int32_t) * hp.lists.size() +
-                    sizeof(TcTask) * hp.tct.size() + sizeof(TcSeg) * hp.tcs.size();
+                    sizeof(G1Tile) * hp.g1tile.size() + sizeof(G1Stage) * hp.g1stage.size() +
+                    sizeof(G1Task) * hp.g1task.size() + sizeof(G1AImg) * hp.g1aimg.size() +
+                    sizeof(G1WImg) * hp.g1wimg.size() + sizeof(G1Red) * hp.g1red.size();
     st.psi_size = psi_size, st.sigma_size = sigma_size;
     *out = h;
     return B2G_OK;
@@ -214,7 +246,8 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaStreamSynchronize(h->ctx->stream);
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
-    cudaFree(h->simt_part), cudaFree(h->tc_part);
+    cudaFree(h->simt_part);
+    cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part);
     cudaFree(h->psi_stage), cudaFree(h->sigma_stage), cudaFree(h->err);
     for (auto &e : h->ev)
         if (e)
@@ -337,8 +370,11 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
         if (form == B2G_TF32X3) {
-            rs.part = h->tc_part_size;
-            B2G_CUDA_TRY(launch_tc_phase2(h->plan, h->ops32, w32, sigma, h->tc_part, scale, h->err, rs, s));
+            if ((rc = ensure_g1(h, nroots)) != B2G_OK)
+                return rc;
+            rs.wimg = h->plan.g1_wbytes, rs.part = h->plan.g1_part;
+            B2G_CUDA_TRY(launch_g1_build_w(h->plan, w32, h->g1_wimg, rs, s));
+            B2G_CUDA_TRY(launch_g1(h->plan, h->g1_aimg, h->g1_wimg, h->g1_part, sigma, scale, h->err, rs, s));
         } else {
             rs.part = 2 * h->simt_part_size;
             B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, (float *)h->simt_part,

@@ -63,41 +63,12 @@ struct Tile2 {          // a phase-2 tile split over several chunks (reduced aft
     int64_t part;
 };
 
-// Tensor-core phase 2: the contributions of a 128-row x N-column tile of a
-// region are cut into K segments packed into stages of kTcStageK columns
-// (zero-padded).  The stage list of a tile is split into chunks (split-K;
-// chunk length chosen so the whole product has about kTcTargetChunks
-// chunks, and at most kTcMaxSegs segments per chunk); one CTA per chunk.  A
-// tile with one chunk updates sigma directly; otherwise each chunk stores a
-// partial tile and a reduction kernel sums the partials in chunk order
-// (deterministic).
+// Tensor-core stages are 16 K columns (two K = 8 MMA steps).  FP32
+// accumulation in TMEM over very long K loses accuracy, so the GEMM1 chunks
+// end after at most kTcMaxChunkStages stages (512 K) and the FP64 reduction
+// sums the chunks.
 constexpr int kTcStageK = 16;
-constexpr int kTcMaxSegs = 384;
-constexpr int kTcTargetChunks = 8 * 152;
-// FP32 accumulation in TMEM over very long K loses accuracy; chunks end after
-// at most this many stages (512 K) and the FP64 reduction sums the chunks
 constexpr int kTcMaxChunkStages = 32;
-struct TcTile {
-    int32_t g, row0, col0, n;   // region, tile origin, tile width (multiple of 16, <= 256)
-    int32_t rows, n_chunks;     // valid rows (<= 128), chunks
-    int64_t part;               // offset (floats) of this tile's partials, -1 if single chunk
-};
-struct TcTask {                 // one chunk of one tile
-    int32_t tile, chunk;
-    int64_t sb, se;             // segment range
-    int32_t st0, n_stages;      // first stage index (tile numbering), stages in this chunk
-};
-// one K segment of one contribution, with everything staging needs (no
-// dependent lookups on the device)
-struct TcSeg {
-    uint64_t a;                 // offset of the left operator block (in the FP32 operator copy)
-    uint64_t w;                 // offset of the work matrix W_u (floats)
-    float alpha;                // alpha0 * alpha1
-    int32_t lda1, row0, m1, col0, n1;
-    int16_t kb, kl;             // k range [kb, kb + kl) of the contribution
-    int8_t koff, ta1, pad0, pad1;
-    int32_t stage;              // stage index within the tile
-};
 
 // Tensor-core phase 1: the distinct products W_u = psi_sub * op(R) that share
 // one right-operator block R are stacked row-wise into tiles of <= 128 rows
@@ -115,6 +86,55 @@ struct Tc1Row {
     uint64_t w;                 // work offset of the row (woff + r * n0)
 };
 
+// Image-fed tensor-core GEMM1 (the TF32x3 form's sigma phase).  The
+// contributions of a region are grouped by their sigma rectangle (rows
+// [row0, row0 + m1) x cols [col0, col0 + n1) of the region frame); a tile is
+// one 128-row x <=256-column piece of a rectangle, so every stage of a tile
+// fills the same accumulator rows.  Operands live in HBM already split into
+// TF32 hi/lo parts and laid out as the canonical no-swizzle K-major tiles the
+// MMA reads (8-row x 16-byte core matrices, 512 B between 8-row groups for a
+// 16-column K slab):
+//   A images (static per H_eff): alpha * op(L) of each distinct (block,
+//     alpha), per 128-row piece and 16-column slab [hi: rows8 x 64 B | lo];
+//   W images (per product, from the GEMM0 output): W_u^T per 16-row slab of
+//     W_u, [hi: npad x 64 B | lo: npad x 64 B], npad = n0 rounded up to 16.
+// A stage is one slab of one contribution: two bulk copies of A (hi, lo) and
+// two of B, then three MMAs per K = 8 half.  Every tile chunk stores a
+// partial tile; the reduction sums, per sigma cell, the partials of all the
+// tiles covering it in a fixed order (rectangles of one region may overlap).
+struct G1Tile {
+    int32_t g, row0, col0;      // region and origin (region frame)
+    int32_t rows, n, n_chunks;  // valid rows (<= 128), MMA width (multiple of 16, <= 256), chunks
+    int32_t ncols, pad;         // valid columns (<= n)
+    int64_t part;               // offset (floats) of chunk 0's partial tile
+};
+struct G1Stage {
+    uint64_t a;                 // byte offset of the A hi slab (lo follows after a_bytes)
+    uint64_t b;                 // byte offset of the B hi slab (per root, in the W image buffer)
+    uint32_t a_bytes;           // rows8 * 64
+    uint32_t b_lo;              // byte distance hi -> lo in the B image (npad * 64)
+};
+struct G1Task {
+    int32_t tile, chunk;
+    int64_t st0;                // first stage
+    int32_t n_stages, pad;
+};
+struct G1AImg {                 // one A image to build: alpha * op(L), all pieces and slabs
+    uint64_t src;               // operator offset (floats)
+    uint64_t dst;               // byte offset of the image
+    float alpha;
+    int32_t m1, k1, lda1, ta1, pad;
+};
+struct G1WImg {                 // one W image per distinct GEMM0 product
+    uint64_t dst;               // byte offset (per root)
+    int32_t u, npad;            // work product, padded width
+};
+struct G1Red {                  // reduction item: rows [r0, r1) of region g
+    int32_t g, r0, r1, t0;      // tile list [t0, t1) of the region (cover list)
+    int32_t t1, pad;
+};
+constexpr int kG1SlabK = 16;
+
 struct HostPlan {
     std::vector<Tc1Tile> tc1t;
     std::vector<Tc1Row> tc1r;
@@ -126,13 +146,19 @@ struct HostPlan {
     std::vector<Tile2> t2multi;
     uint64_t t2_part_tiles = 0;     // 4 x 256 partial tiles of split phase-2 tiles
     std::vector<int32_t> lists;
-    std::vector<TcTask> tct;
-    std::vector<TcSeg> tcs;
-    std::vector<TcTile> tctile;
-    std::vector<int32_t> tc_multi;  // tiles with more than one chunk
-    uint64_t tc_part_size = 0;      // floats of partial tiles
     uint64_t work_size = 0;
     double mnk = 0, mnk_exec = 0;
+    // image-fed tensor-core GEMM1
+    std::vector<G1Tile> g1tile;
+    std::vector<G1Stage> g1stage;
+    std::vector<G1Task> g1task;
+    std::vector<G1AImg> g1aimg;
+    std::vector<G1WImg> g1wimg;
+    std::vector<G1Red> g1red;
+    std::vector<int32_t> g1cover;   // tile ids per region (reduction cover lists)
+    uint64_t g1_abytes = 0;         // A image bytes
+    uint64_t g1_wbytes = 0;         // W image bytes per root
+    uint64_t g1_part = 0;           // partial floats per root
 };
 
 int build_plan(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size, uint64_t sigma_size,
@@ -150,12 +176,16 @@ struct DevicePlan {
     Tc1Tile *tc1t = nullptr;
     Tc1Row *tc1r = nullptr;
     int64_t n_tc1t = 0;
-    TcTask *tct = nullptr;
-    TcSeg *tcs = nullptr;
-    TcTile *tctile = nullptr;
-    int32_t *tc_multi = nullptr;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
-    int64_t n_tct = 0, n_tcs = 0, n_tctile = 0, n_tc_multi = 0;
+    G1Tile *g1tile = nullptr;
+    G1Stage *g1stage = nullptr;
+    G1Task *g1task = nullptr;
+    G1AImg *g1aimg = nullptr;
+    G1WImg *g1wimg = nullptr;
+    G1Red *g1red = nullptr;
+    int32_t *g1cover = nullptr;
+    int64_t n_g1task = 0, n_g1aimg = 0, n_g1wimg = 0, n_g1red = 0;
+    uint64_t g1_abytes = 0, g1_wbytes = 0, g1_part = 0;
 };
 
 // Several right-hand sides (roots) in one launch: root r (blockIdx.y) reads
@@ -164,15 +194,22 @@ struct DevicePlan {
 struct RootStrides {
     int nroots = 1;
     uint64_t psi = 0, sigma = 0, work = 0, part = 0;
+    uint64_t wimg = 0;   // W image bytes per root (image-fed GEMM1)
 };
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
 // bounded wait gives up
-cudaError_t launch_tc_phase2(const DevicePlan &p, const float *ops32, const float *work,
-                             double *sigma, float *part, double scale, int *err,
-                             const RootStrides &rs, cudaStream_t s);
 cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops32, const float *psi32,
                              float *work, int *err, const RootStrides &rs, cudaStream_t s);
+
+// image-fed tensor-core GEMM1 (b2g_g1.cu)
+cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned char *aimg,
+                              cudaStream_t s);
+cudaError_t launch_g1_build_w(const DevicePlan &p, const float *work, unsigned char *wimg,
+                              const RootStrides &rs, cudaStream_t s);
+cudaError_t launch_g1(const DevicePlan &p, const unsigned char *aimg, const unsigned char *wimg,
+                      float *part, double *sigma, double scale, int *err, const RootStrides &rs,
+                      cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>
@@ -202,11 +239,14 @@ struct b2g_heff {
     double *work = nullptr;  // cap_roots x work_size doubles (FP32 forms use it as floats)
     double *psi_stage = nullptr, *sigma_stage = nullptr; // device staging for the host entry
     void *simt_part = nullptr;   // cap_roots x phase-2 partial tiles (doubles)
-    float *tc_part = nullptr;    // cap_roots x tensor-core partial tiles
+    unsigned char *g1_aimg = nullptr;  // A images (made with ops32)
+    unsigned char *g1_wimg = nullptr;  // g1_roots x W images
+    float *g1_part = nullptr;          // g1_roots x image-fed GEMM1 partial tiles
+    int g1_roots = 0;                  // roots the W images / partials are sized for
     int cap_roots = 0;           // roots the per-root buffers are sized for
     int stage_roots = 0;         // roots the host staging buffers are sized for
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;
-    uint64_t simt_part_size = 0, tc_part_size = 0;  // per root, in elements
+    uint64_t simt_part_size = 0;  // per root, in elements
     b2g_heff_stats stats{};
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

@@ -14,6 +14,8 @@
 //     so no atomics, no sigma copies and no reduction are needed, and the
 //     summation order is fixed (bit-reproducible run to run).
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -228,90 +230,152 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                     plan.t2.push_back(t);
                 }
             }
-        // tensor-core tiles: 128 rows x up to 256 columns, contributions packed
-        // along K into stages of kTcStageK columns
-        for (int32_t r0 = 0; r0 < rows; r0 += 128)
-            for (int32_t c0 = 0; c0 < cols; c0 += 256) {
-                const int32_t nt = std::min(256, ((cols - c0) + 15) / 16 * 16);
-                const int64_t sb = (int64_t)plan.tcs.size();
-                int32_t stage = 0, koff = 0;
-                for (size_t q = c_begin; q < plan.contribs.size(); q++) {
-                    const Contrib &c = plan.contribs[q];
-                    if (c.row0 >= r0 + 128 || c.row0 + c.m1 <= r0 || c.col0 >= c0 + nt ||
-                        c.col0 + c.n1 <= c0)
-                        continue;
-                    for (int32_t kb = 0; kb < c.k1;) {
-                        const int32_t take = std::min(c.k1 - kb, kTcStageK - koff);
-                        TcSeg sg;
-                        sg.a = c.a1, sg.w = plan.works[c.u].woff, sg.alpha = (float)c.alpha;
-                        sg.lda1 = c.lda1, sg.row0 = c.row0, sg.m1 = c.m1, sg.col0 = c.col0, sg.n1 = c.n1;
-                        sg.kb = (int16_t)kb, sg.kl = (int16_t)take;
-                        sg.koff = (int8_t)koff, sg.ta1 = (int8_t)c.ta1, sg.pad0 = 0, sg.pad1 = 0;
-                        sg.stage = stage;
-                        plan.tcs.push_back(sg);
-                        kb += take, koff += take;
-                        if (koff == kTcStageK)
-                            stage++, koff = 0;
+        // image-fed tensor-core GEMM1: one tile per 128-row x 256-column piece of
+        // each distinct sigma rectangle, one stage per 16-row K slab of each
+        // contribution (stage offsets into the A / W images filled in below)
+        {
+            std::vector<std::array<int32_t, 4>> rkeys;   // rectangles, first-appearance order
+            std::map<std::array<int32_t, 4>, int32_t> rmap;
+            std::vector<std::vector<int32_t>> rlist;
+            for (size_t q = c_begin; q < plan.contribs.size(); q++) {
+                const Contrib &c = plan.contribs[q];
+                const std::array<int32_t, 4> rk{c.row0, c.m1, c.col0, c.n1};
+                auto it = rmap.find(rk);
+                if (it == rmap.end()) {
+                    it = rmap.emplace(rk, (int32_t)rkeys.size()).first;
+                    rkeys.push_back(rk);
+                    rlist.emplace_back();
+                }
+                rlist[it->second].push_back((int32_t)q);
+            }
+            const int32_t t_first = (int32_t)plan.g1tile.size();
+            for (size_t z = 0; z < rkeys.size(); z++) {
+                const int32_t row0 = rkeys[z][0], m1 = rkeys[z][1], col0 = rkeys[z][2], n1 = rkeys[z][3];
+                const int32_t npad = (n1 + 15) / 16 * 16;
+                for (int32_t rp = 0; rp * 128 < m1; rp++)
+                    for (int32_t cp = 0; cp * 256 < npad; cp++) {
+                        G1Tile t;
+                        t.g = g, t.row0 = row0 + 128 * rp, t.col0 = col0 + 256 * cp;
+                        t.rows = std::min(128, m1 - 128 * rp);
+                        t.n = std::min(256, npad - 256 * cp);
+                        t.ncols = std::min(t.n, n1 - 256 * cp);
+                        t.pad = 0;
+                        t.n_chunks = 0;
+                        t.part = (int64_t)plan.g1stage.size();  // first stage until chunking
+                        for (int32_t q : rlist[z]) {
+                            const Contrib &c = plan.contribs[q];
+                            const int32_t nsl = (c.k1 + kG1SlabK - 1) / kG1SlabK;
+                            for (int32_t sl = 0; sl < nsl; sl++) {
+                                G1Stage st;
+                                // a: A image id / piece / slab, b: work id / slab / column piece
+                                st.a = (uint64_t)q;
+                                st.b = ((uint64_t)(uint32_t)sl << 32) | (uint32_t)(rp << 16 | cp);
+                                st.a_bytes = 0, st.b_lo = 0;
+                                plan.g1stage.push_back(st);
+                            }
+                        }
+                        plan.g1tile.push_back(t);
                     }
-                }
-                const int64_t se = (int64_t)plan.tcs.size();
-                const int32_t n_stages = stage + (koff > 0 ? 1 : 0);
-                if (se == sb)
-                    continue;
-                TcTile tl;
-                tl.g = g, tl.row0 = r0, tl.col0 = c0, tl.n = nt;
-                tl.rows = std::min(128, rows - r0);
-                tl.n_chunks = n_stages;  // stage count until the chunking pass below
-                tl.part = sb;            // segment start until the chunking pass below
-                plan.tctile.push_back(tl);
             }
-    }
-    // ---- split-K chunking of the tensor-core tiles
-    {
-        int64_t total_stages = 0;
-        for (auto &tl : plan.tctile)
-            total_stages += tl.n_chunks;
-        const int32_t chunk_stages = (int32_t)std::min<int64_t>(
-            kTcMaxChunkStages,
-            std::max<int64_t>(8, (total_stages + kTcTargetChunks - 1) / kTcTargetChunks));
-        for (int32_t tile = 0; tile < (int32_t)plan.tctile.size(); tile++) {
-            TcTile &tl = plan.tctile[tile];
-            const int32_t n_stages = tl.n_chunks;
-            const int64_t sb = tl.part;
-            const int64_t se = tile + 1 < (int32_t)plan.tctile.size() ? plan.tctile[tile + 1].part
-                                                                      : (int64_t)plan.tcs.size();
-            std::vector<TcTask> chunks;
-            int64_t s = sb;
-            int32_t st = 0;
-            while (st < n_stages) {
-                TcTask t;
-                t.tile = tile, t.chunk = (int32_t)chunks.size(), t.st0 = st, t.sb = s;
-                // up to chunk_stages stages and kTcMaxSegs segments, whole stages only
-                int32_t ns = 0;
-                while (st + ns < n_stages && ns < chunk_stages) {
-                    int64_t e = s;
-                    while (e < se && plan.tcs[e].stage == st + ns)
-                        e++;
-                    if (ns > 0 && e - t.sb > kTcMaxSegs)
-                        break;
-                    s = e, ns++;
-                }
-                t.n_stages = ns, t.se = s;
-                st += ns;
-                chunks.push_back(t);
+            const int32_t t_last = (int32_t)plan.g1tile.size();
+            const int32_t cv0 = (int32_t)plan.g1cover.size();
+            for (int32_t t = t_first; t < t_last; t++)
+                plan.g1cover.push_back(t);
+            for (int32_t r0 = 0; r0 < rows; r0 += 16) {
+                G1Red it;
+                it.g = g, it.r0 = r0, it.r1 = std::min(rows, r0 + 16);
+                it.t0 = cv0, it.t1 = (int32_t)plan.g1cover.size(), it.pad = 0;
+                plan.g1red.push_back(it);
             }
-            tl.n_chunks = (int32_t)chunks.size();
-            tl.part = -1;
-            if (tl.n_chunks > 1) {
-                tl.part = (int64_t)plan.tc_part_size;
-                plan.tc_part_size += (uint64_t)tl.n_chunks * tl.rows * tl.n;
-                plan.tc_multi.push_back(tile);
-            }
-            plan.tct.insert(plan.tct.end(), chunks.begin(), chunks.end());
         }
     }
-    std::stable_sort(plan.tct.begin(), plan.tct.end(),
-                     [](const TcTask &a, const TcTask &b) { return a.n_stages > b.n_stages; });
+    // ---- image-fed GEMM1: A images (one per distinct operator block and
+    // coefficient), W image offsets, stage byte offsets, split-K chunks
+    {
+        struct AKey {
+            uint64_t a1;
+            int32_t m1, k1, lda1, ta1;
+            float alpha;
+            bool operator==(const AKey &o) const {
+                return a1 == o.a1 && m1 == o.m1 && k1 == o.k1 && lda1 == o.lda1 && ta1 == o.ta1 &&
+                       memcmp(&alpha, &o.alpha, sizeof(float)) == 0;
+            }
+        };
+        struct AKeyHash {
+            size_t operator()(const AKey &k) const {
+                uint32_t ab;
+                memcpy(&ab, &k.alpha, sizeof ab);
+                uint64_t h = k.a1 * 0x9E3779B97F4A7C15ULL;
+                h ^= ((uint64_t)(uint32_t)k.m1 << 32 | (uint32_t)k.k1) * 0xBF58476D1CE4E5B9ULL;
+                h ^= ((uint64_t)(uint32_t)k.lda1 << 33 | (uint64_t)k.ta1 << 32 | ab) * 0x94D049BB133111EBULL;
+                return (size_t)(h ^ (h >> 29));
+            }
+        };
+        std::unordered_map<AKey, int32_t, AKeyHash> amap;
+        std::vector<int32_t> cimg(plan.contribs.size(), -1);
+        for (size_t q = 0; q < plan.contribs.size(); q++) {
+            const Contrib &c = plan.contribs[q];
+            AKey k{c.a1, c.m1, c.k1, c.lda1, c.ta1, (float)c.alpha};
+            auto it = amap.find(k);
+            if (it == amap.end()) {
+                G1AImg im;
+                im.src = c.a1, im.dst = plan.g1_abytes, im.alpha = (float)c.alpha;
+                im.m1 = c.m1, im.k1 = c.k1, im.lda1 = c.lda1, im.ta1 = c.ta1, im.pad = 0;
+                const uint64_t nsl = (uint64_t)((c.k1 + kG1SlabK - 1) / kG1SlabK);
+                for (int32_t rp = 0; rp * 128 < c.m1; rp++) {
+                    const int32_t rows8 = (std::min(128, c.m1 - 128 * rp) + 7) / 8 * 8;
+                    plan.g1_abytes += (uint64_t)rows8 * 128 * nsl;
+                }
+                it = amap.emplace(k, (int32_t)plan.g1aimg.size()).first;
+                plan.g1aimg.push_back(im);
+            }
+            cimg[q] = it->second;
+        }
+        std::vector<uint64_t> wdst(plan.works.size());
+        for (size_t u = 0; u < plan.works.size(); u++) {
+            const WorkDesc &w = plan.works[u];
+            const int32_t npad = (w.n0 + 15) / 16 * 16;
+            G1WImg wi;
+            wi.dst = plan.g1_wbytes, wi.u = (int32_t)u, wi.npad = npad;
+            wdst[u] = wi.dst;
+            plan.g1wimg.push_back(wi);
+            plan.g1_wbytes += (uint64_t)((w.m0 + kG1SlabK - 1) / kG1SlabK) * npad * 128;
+        }
+        for (G1Stage &st : plan.g1stage) {
+            const Contrib &c = plan.contribs[(size_t)st.a];
+            const G1AImg &im = plan.g1aimg[cimg[(size_t)st.a]];
+            const int32_t sl = (int32_t)(st.b >> 32), rp = (int32_t)((st.b >> 16) & 0xFFFF),
+                          cp = (int32_t)(st.b & 0xFFFF);
+            const uint64_t nsl = (uint64_t)((c.k1 + kG1SlabK - 1) / kG1SlabK);
+            const int32_t rows8 = (std::min(128, c.m1 - 128 * rp) + 7) / 8 * 8;
+            const WorkDesc &w = plan.works[c.u];
+            const int32_t npad = (w.n0 + 15) / 16 * 16;
+            st.a = im.dst + (uint64_t)rp * 16384 * nsl + (uint64_t)sl * rows8 * 128;
+            st.a_bytes = (uint32_t)rows8 * 64;
+            st.b = wdst[c.u] + (uint64_t)sl * npad * 128 + (uint64_t)cp * 256 * 64;
+            st.b_lo = (uint32_t)npad * 64;
+        }
+        for (int32_t t = 0; t < (int32_t)plan.g1tile.size(); t++) {
+            G1Tile &tl = plan.g1tile[t];
+            const int64_t sb = tl.part;
+            const int64_t se = t + 1 < (int32_t)plan.g1tile.size() ? plan.g1tile[t + 1].part
+                                                                   : (int64_t)plan.g1stage.size();
+            int32_t ch = 0;
+            for (int64_t st = sb; st < se; st += kTcMaxChunkStages, ch++) {
+                G1Task k;
+                k.tile = t, k.chunk = ch, k.st0 = st;
+                k.n_stages = (int32_t)std::min<int64_t>(kTcMaxChunkStages, se - st), k.pad = 0;
+                plan.g1task.push_back(k);
+            }
+            tl.n_chunks = ch;
+        }
+        for (G1Tile &tl : plan.g1tile) {
+            tl.part = (int64_t)plan.g1_part;
+            plan.g1_part += (uint64_t)tl.n_chunks * tl.rows * tl.n;
+        }
+        std::stable_sort(plan.g1task.begin(), plan.g1task.end(),
+                         [](const G1Task &a, const G1Task &b) { return a.n_stages > b.n_stages; });
+    }
     // heavy tasks first: shortens the tail of the phase-2 grid
     std::stable_sort(plan.t2.begin(), plan.t2.end(),
                      [](const Task2 &a, const Task2 &b) { return a.le - a.lb > b.le - b.lb; });
