@@ -33,9 +33,9 @@ template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaSt
 static void free_plan(DevicePlan &p) {
     cudaFree(p.works), cudaFree(p.contribs), cudaFree(p.regions);
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
-    cudaFree(p.t2multi), cudaFree(p.tc1t), cudaFree(p.tc1r);
+    cudaFree(p.t2multi), cudaFree(p.g0tile), cudaFree(p.g0col);
     cudaFree(p.g1tile), cudaFree(p.g1stage), cudaFree(p.g1task), cudaFree(p.g1aimg);
-    cudaFree(p.g1wimg), cudaFree(p.g1red), cudaFree(p.g1cover);
+    cudaFree(p.g1red), cudaFree(p.g1cover);
     p = DevicePlan();
 }
 
@@ -85,6 +85,10 @@ static int ensure_g1(b2g_heff *h, int nroots) {
         return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the GEMM1 work images of " +
                                        std::to_string(nroots) + " roots");
     }
+    // the padding of the W images (rows past m0 in the last K slab, columns past
+    // n0) is never written by GEMM0 and must read as zero
+    if (p.g1_wbytes)
+        B2G_CUDA_TRY(cudaMemsetAsync(h->g1_wimg, 0, p.g1_wbytes * R, h->ctx->stream));
     h->g1_roots = nroots;
     return B2G_OK;
 }
@@ -191,16 +195,16 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
         (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
         (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
-        (rc = upload(hp.t2multi, &p.t2multi, s)) || (rc = upload(hp.tc1t, &p.tc1t, s)) ||
-        (rc = upload(hp.tc1r, &p.tc1r, s)) || (rc = upload(hp.g1tile, &p.g1tile, s)) ||
+        (rc = upload(hp.t2multi, &p.t2multi, s)) ||
+        (rc = upload(hp.g0tile, &p.g0tile, s)) || (rc = upload(hp.g0col, &p.g0col, s)) ||
+        (rc = upload(hp.g1tile, &p.g1tile, s)) ||
         (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
-        (rc = upload(hp.g1aimg, &p.g1aimg, s)) || (rc = upload(hp.g1wimg, &p.g1wimg, s)) ||
+        (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
         (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)))
         return bail(rc);
     p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
-    p.n_g1wimg = (int64_t)hp.g1wimg.size(), p.n_g1red = (int64_t)hp.g1red.size();
+    p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
     p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
-    p.n_tc1t = (int64_t)hp.tc1t.size();
     p.n_t2multi = (int64_t)hp.t2multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
     p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
@@ -363,17 +367,16 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
         // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
         B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
-        if (form == B2G_TF32X3)
-            B2G_CUDA_TRY(launch_tc_phase1(h->plan, h->ops32, h->psi32, w32, h->err, rs, s));
-        else
-            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
-        if (h->timing)
-            B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
         if (form == B2G_TF32X3) {
             if ((rc = ensure_g1(h, nroots)) != B2G_OK)
                 return rc;
             rs.wimg = h->plan.g1_wbytes, rs.part = h->plan.g1_part;
-            B2G_CUDA_TRY(launch_g1_build_w(h->plan, w32, h->g1_wimg, rs, s));
+            B2G_CUDA_TRY(launch_g0(h->plan, h->g1_aimg, h->psi32, h->g1_wimg, h->err, rs, s));
+        } else
+            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
+        if (h->timing)
+            B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+        if (form == B2G_TF32X3) {
             B2G_CUDA_TRY(launch_g1(h->plan, h->g1_aimg, h->g1_wimg, h->g1_part, sigma, scale, h->err, rs, s));
         } else {
             rs.part = 2 * h->simt_part_size;

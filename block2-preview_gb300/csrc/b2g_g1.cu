@@ -9,8 +9,8 @@
 // predicates in the main loop.
 //   * A images: alpha * op(L) for each distinct (operator block, alpha),
 //     built once per H_eff from the FP32 operator copy (g1_build_a).
-//   * W images: W_u^T per 16-row K slab, built per product from the GEMM0
-//     output (g1_build_w).
+//   * W images: W_u^T per 16-row K slab, written per product by the GEMM0
+//     kernel's epilogue (b2g_tc.cu).
 // One CTA per chunk (at most kG1ChunkStages slabs of one tile): warp 0 lane 0
 // issues the copies into a ring of stage slots, warp 1 lane 0 waits for a
 // slot, issues its six MMAs and commits them to the slot's empty barrier,
@@ -61,30 +61,6 @@ __global__ void __launch_bounds__(256) g1_build_a(const G1AImg *__restrict__ img
                 *(uint32_t *)(base + rows8 * 64 + off) = lo;
             }
         }
-    }
-}
-
-__global__ void __launch_bounds__(256) g1_build_w(const G1WImg *__restrict__ imgs,
-                                                  const WorkDesc *__restrict__ works,
-                                                  const float *__restrict__ work,
-                                                  unsigned char *__restrict__ out, RootStrides rs) {
-    const G1WImg im = imgs[blockIdx.x];
-    const WorkDesc wd = works[im.u];
-    work += blockIdx.y * rs.work;
-    out += blockIdx.y * rs.wimg;
-    const int ns = (wd.m0 + kG1SlabK - 1) / kG1SlabK;
-    const float *W = work + wd.woff;
-    const int total = ns * kG1SlabK * im.npad;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int k = e / im.npad, n = e - k * im.npad;  // consecutive threads: consecutive n
-        const float v = (k < wd.m0 && n < wd.n0) ? W[(uint64_t)k * wd.n0 + n] : 0.f;
-        uint32_t hi, lo;
-        split_tf32(v, hi, lo);
-        const int sl = k >> 4;
-        unsigned char *base = out + im.dst + (uint64_t)sl * im.npad * 128;
-        const uint32_t off = kmajor_off(n, k & 15);
-        *(uint32_t *)(base + off) = hi;
-        *(uint32_t *)(base + im.npad * 64 + off) = lo;
     }
 }
 
@@ -267,14 +243,6 @@ cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned 
     if (p.n_g1aimg == 0)
         return cudaSuccess;
     g1_build_a<<<(unsigned)p.n_g1aimg, 256, 0, s>>>(p.g1aimg, ops32, aimg);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_g1_build_w(const DevicePlan &p, const float *work, unsigned char *wimg,
-                              const RootStrides &rs, cudaStream_t s) {
-    if (p.n_g1wimg == 0)
-        return cudaSuccess;
-    g1_build_w<<<dim3((unsigned)p.n_g1wimg, rs.nroots), 256, 0, s>>>(p.g1wimg, p.works, work, wimg, rs);
     return cudaGetLastError();
 }
 

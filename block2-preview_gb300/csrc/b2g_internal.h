@@ -70,20 +70,27 @@ struct Tile2 {          // a phase-2 tile split over several chunks (reduced aft
 constexpr int kTcStageK = 16;
 constexpr int kTcMaxChunkStages = 32;
 
-// Tensor-core phase 1: the distinct products W_u = psi_sub * op(R) that share
-// one right-operator block R are stacked row-wise into tiles of <= 128 rows
-// (one CTA each, K = k0 in stages of kTcStageK, N <= 256 columns per tile).
-struct Tc1Tile {
-    uint64_t b0;                // right operator block offset
-    int32_t tb0, k0, n0, ldb0;  // its transpose flag, K, total columns, leading dimension
-    int32_t col0, n;            // column range [col0, col0 + n) of this tile (n multiple of 16)
-    int32_t rows;               // stacked rows (<= 128)
-    int32_t pad;
-    int64_t rb;                 // first entry in the row table
+// Tensor-core GEMM0 of the TF32x3 form, transposed: W_u^T = op(R)^T *
+// psi_u^T for the distinct products sharing one right operator block R.  A
+// tile is one 128-row piece of op(R)^T (rows = columns of W, M) times up to
+// 256 stacked psi rows of those products (N; each product's rows padded to a
+// multiple of 4), K = k0 in 16-column slabs.  The R piece comes from a static
+// operator image (bulk copies), the psi rows are gathered per stage, and the
+// epilogue writes the accumulator straight into the W images GEMM1 reads
+// (every 4 stacked columns are one 16-byte K chunk of one W image row).
+struct G0Tile {
+    uint64_t a;                 // byte offset of slab 0 of the op(R)^T image piece
+    uint32_t a_bytes;           // rows8 * 64: one split part of one slab
+    int32_t nsl;                // K slabs
+    int32_t rows, n, ncol;      // valid M rows (<= 128), MMA N (multiple of 16), valid columns
+    int32_t k0, npad, m_off;    // K, W image width (n0 rounded up to 16), W column of row 0
+    int64_t cb;                 // first entry in the column table
 };
-struct Tc1Row {
-    uint64_t psi;               // psi offset of the row (a0 + r * lda0)
-    uint64_t w;                 // work offset of the row (woff + r * n0)
+struct G0Col {                  // one stacked psi row (one W image K row)
+    uint64_t psi;               // psi offset of the row (a0 + i * lda0)
+    uint64_t w;                 // byte offset of its W image (per root)
+    int32_t k;                  // row index i within the product
+    int32_t live;               // i < m0 (padding rows read zeros)
 };
 
 // Image-fed tensor-core GEMM1 (the TF32x3 form's sigma phase).  The
@@ -136,8 +143,8 @@ struct G1Red {                  // reduction item: rows [r0, r1) of region g
 constexpr int kG1SlabK = 16;
 
 struct HostPlan {
-    std::vector<Tc1Tile> tc1t;
-    std::vector<Tc1Row> tc1r;
+    std::vector<G0Tile> g0tile;
+    std::vector<G0Col> g0col;
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
     std::vector<Region> regions;
@@ -173,18 +180,17 @@ struct DevicePlan {
     Tile2 *t2multi = nullptr;
     int64_t n_t2multi = 0;
     int32_t *lists = nullptr;
-    Tc1Tile *tc1t = nullptr;
-    Tc1Row *tc1r = nullptr;
-    int64_t n_tc1t = 0;
+    G0Tile *g0tile = nullptr;
+    G0Col *g0col = nullptr;
+    int64_t n_g0tile = 0;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
     G1Tile *g1tile = nullptr;
     G1Stage *g1stage = nullptr;
     G1Task *g1task = nullptr;
     G1AImg *g1aimg = nullptr;
-    G1WImg *g1wimg = nullptr;
     G1Red *g1red = nullptr;
     int32_t *g1cover = nullptr;
-    int64_t n_g1task = 0, n_g1aimg = 0, n_g1wimg = 0, n_g1red = 0;
+    int64_t n_g1task = 0, n_g1aimg = 0, n_g1red = 0;
     uint64_t g1_abytes = 0, g1_wbytes = 0, g1_part = 0;
 };
 
@@ -199,14 +205,12 @@ struct RootStrides {
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
 // bounded wait gives up
-cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops32, const float *psi32,
-                             float *work, int *err, const RootStrides &rs, cudaStream_t s);
+cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const float *psi32,
+                      unsigned char *wimg, int *err, const RootStrides &rs, cudaStream_t s);
 
 // image-fed tensor-core GEMM1 (b2g_g1.cu)
 cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned char *aimg,
                               cudaStream_t s);
-cudaError_t launch_g1_build_w(const DevicePlan &p, const float *work, unsigned char *wimg,
-                              const RootStrides &rs, cudaStream_t s);
 cudaError_t launch_g1(const DevicePlan &p, const unsigned char *aimg, const unsigned char *wimg,
                       float *part, double *sigma, double scale, int *err, const RootStrides &rs,
                       cudaStream_t s);

@@ -382,7 +382,8 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
     for (int32_t u = 0; u < (int32_t)plan.works.size(); u++)
         for (int32_t r = 0; r < plan.works[u].m0; r++)
             plan.t1.push_back(Task1{u, r});
-    // ---- tensor-core phase 1: stack rows of products sharing a right operator block
+    // ---- tensor-core GEMM0 (transposed): op(R)^T pieces x stacked psi rows of
+    // the products sharing R; op(R)^T images join the A image buffer
     {
         std::vector<int32_t> ord(plan.works.size());
         for (size_t i = 0; i < ord.size(); i++)
@@ -406,29 +407,48 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             while (ge < ord.size() && same_r(ord[gs], ord[ge]))
                 ge++;
             const WorkDesc &w0 = plan.works[ord[gs]];
-            // rows of the group in order, cut into tiles of 128
-            std::vector<Tc1Row> rows;
-            for (size_t q = gs; q < ge; q++) {
-                const WorkDesc &w = plan.works[ord[q]];
-                for (int32_t r = 0; r < w.m0; r++)
-                    rows.push_back(Tc1Row{w.a0 + (uint64_t)r * w.lda0, w.woff + (uint64_t)r * w.n0});
+            // the op(R)^T image: rows = the n0 columns of R, K = k0
+            G1AImg im;
+            im.src = w0.b0, im.dst = plan.g1_abytes, im.alpha = 1.0f;
+            im.m1 = w0.n0, im.k1 = w0.k0, im.lda1 = w0.ldb0, im.ta1 = w0.tb0 ? 0 : 1, im.pad = 0;
+            const int32_t nsl = (w0.k0 + kG1SlabK - 1) / kG1SlabK;
+            for (int32_t rp = 0; rp * 128 < w0.n0; rp++) {
+                const int32_t rows8 = (std::min(128, w0.n0 - 128 * rp) + 7) / 8 * 8;
+                plan.g1_abytes += (uint64_t)rows8 * 128 * nsl;
             }
-            for (size_t r0 = 0; r0 < rows.size(); r0 += 128) {
-                const int64_t rb = (int64_t)plan.tc1r.size();
-                const int32_t nr = (int32_t)std::min<size_t>(128, rows.size() - r0);
-                plan.tc1r.insert(plan.tc1r.end(), rows.begin() + r0, rows.begin() + r0 + nr);
-                for (int32_t c0 = 0; c0 < w0.n0; c0 += 256) {
-                    Tc1Tile t;
-                    t.b0 = w0.b0, t.tb0 = w0.tb0, t.k0 = w0.k0, t.n0 = w0.n0, t.ldb0 = w0.ldb0;
-                    t.col0 = c0, t.n = std::min(256, (w0.n0 - c0 + 15) / 16 * 16);
-                    t.rows = nr, t.pad = 0, t.rb = rb;
-                    plan.tc1t.push_back(t);
+            plan.g1aimg.push_back(im);
+            // stacked psi rows, each product padded to a multiple of 4
+            std::vector<G0Col> cols;
+            for (size_t q = gs; q < ge; q++) {
+                const int32_t u = ord[q];
+                const WorkDesc &w = plan.works[u];
+                const int32_t m0p = (w.m0 + 3) / 4 * 4;
+                for (int32_t i = 0; i < m0p; i++) {
+                    G0Col c;
+                    c.psi = i < w.m0 ? w.a0 + (uint64_t)i * w.lda0 : 0;
+                    c.w = plan.g1wimg[u].dst, c.k = i, c.live = i < w.m0 ? 1 : 0;
+                    cols.push_back(c);
+                }
+            }
+            const int32_t npad = (w0.n0 + 15) / 16 * 16;
+            for (size_t c0 = 0; c0 < cols.size(); c0 += 256) {
+                const int32_t nc = (int32_t)std::min<size_t>(256, cols.size() - c0);
+                const int64_t cb = (int64_t)plan.g0col.size();
+                plan.g0col.insert(plan.g0col.end(), cols.begin() + c0, cols.begin() + c0 + nc);
+                for (int32_t rp = 0; rp * 128 < w0.n0; rp++) {
+                    G0Tile t;
+                    t.rows = std::min(128, w0.n0 - 128 * rp);
+                    const uint32_t rows8 = (uint32_t)(t.rows + 7) / 8 * 8;
+                    t.a = im.dst + (uint64_t)rp * 16384 * nsl, t.a_bytes = rows8 * 64, t.nsl = nsl;
+                    t.n = (nc + 15) / 16 * 16, t.ncol = nc;
+                    t.k0 = w0.k0, t.npad = npad, t.m_off = 128 * rp, t.cb = cb;
+                    plan.g0tile.push_back(t);
                 }
             }
             gs = ge;
         }
-        std::stable_sort(plan.tc1t.begin(), plan.tc1t.end(),
-                         [](const Tc1Tile &a, const Tc1Tile &b) { return a.k0 * a.n > b.k0 * b.n; });
+        std::stable_sort(plan.g0tile.begin(), plan.g0tile.end(),
+                         [](const G0Tile &a, const G0Tile &b) { return (int64_t)a.nsl * a.n > (int64_t)b.nsl * b.n; });
     }
     return B2G_OK;
 }

@@ -1,18 +1,22 @@
-// Tensor-core (tcgen05, kind::tf32) GEMM0 of the TF32x3 form:
-// W_u = psi_sub * op(R) for the distinct products, split-TF32 x3 (hi*hi +
-// hi*lo + lo*hi) with FP32 accumulation in TMEM.
+// Tensor-core (tcgen05, kind::tf32) GEMM0 of the TF32x3 form, transposed:
+// W_u^T = op(R)^T * psi_u^T for the distinct products W_u = psi_u * op(R),
+// split-TF32 x3 (hi*hi + hi*lo + lo*hi) with an FP32 accumulator in TMEM.
 //
-// One CTA per tile: up to 128 rows of products that share one right
-// operator block R, stacked along M, times <= 256 columns of R.  Producer
-// warps gather the psi rows and the R slab of each 16-column K stage from
-// the FP32 copies, split them into TF32 hi/lo parts and write them into a
-// ring of shared-memory stage slots in the canonical no-swizzle K-major
-// layout; lane 0 of the MMA warp waits for a slot (mbarrier), issues the
-// stage's six MMAs and commits them to the slot's empty barrier; all warps
-// drain the accumulator (tcgen05.ld) into the FP32 work rows.
+// One CTA per tile (a 128-row piece of op(R)^T times up to 256 stacked psi
+// rows of the products that share R), K = k0 in 16-column stages:
+//   * warp 0 lane 0 bulk-copies the stage's op(R)^T slab (TF32 hi/lo,
+//     canonical K-major layout, built once per H_eff) into a ring slot;
+//   * warps 2..7 gather the stage's psi rows from the FP32 psi copy (L2
+//     resident), split them into hi/lo and store them in the slot;
+//   * warp 1 lane 0 waits for both (the copies' mbarrier with their byte
+//     count, the gather's mbarrier), issues the six MMAs and commits them to
+//     the slot's empty barrier;
+//   * warps 4..7 then drain the accumulator: each thread holds one column of
+//     W (a TMEM lane) and 16 stacked psi rows per tcgen05.ld, and writes every
+//     4 rows as one 16-byte chunk of the W image GEMM1 reads (hi and lo).
 //
 // Every mbarrier wait is bounded: on timeout the kernel sets *err, waits
-// (bounded) for its outstanding MMAs, frees its TMEM and returns.
+// (bounded) for its outstanding copies, frees its TMEM and returns.
 #include "b2g_internal.h"
 #include "b2g_tcgen05.cuh"
 
@@ -22,202 +26,217 @@ namespace {
 
 using namespace tcg;
 
-constexpr int kThreads = 256;                          // 8 warps
-constexpr int kProducers = 7;                          // warps 0..6 stage operands
-constexpr int kMmaWarp = 7;                            // lane 0 of warp 7 issues the MMAs
-constexpr int kMaxN = 256;
-constexpr int kMaxRing = 8;
-constexpr uint32_t kABytes = 128 * kTcStageK * 4;      // 8 KB per split part of A
-// ---------------------------------------------------------------------------
-// Phase 1 (GEMM0) on tensor cores: one CTA per Tc1Tile, D (128 x n) =
-// stacked psi rows (128 x k0) * op(R) (k0 x n), same TF32 x3 split, same
-// producer / single-thread-MMA ring as phase 2 (smaller ring: two CTAs per
-// SM), epilogue writes the FP32 work rows.
-constexpr uint32_t kRing1Bytes = 96 * 1024;
-constexpr uint32_t kSmem1Bytes = kRing1Bytes + 128 * sizeof(Tc1Row) + 256 + 1024;
+constexpr int kThreads = 256;
+constexpr int kGatherWarp0 = 2;                      // warps 2..7 gather psi
+constexpr int kGatherThreads = kThreads - 32 * kGatherWarp0;
+constexpr int kMaxRing = 4;
+constexpr uint32_t kABytes = 128 * kTcStageK * 4;    // one split part of the A slab (8 KB)
+constexpr uint32_t kRingBytes = 96 * 1024;           // two CTAs per SM
+constexpr uint32_t kSmemBytes = kRingBytes + 1024;
+constexpr uint32_t kTmemCols = 256;
 
-__global__ void __launch_bounds__(kThreads, 1)
-tc_phase1_kernel(const Tc1Tile *__restrict__ tiles, const Tc1Row *__restrict__ rowtab,
-                 const float *__restrict__ ops, const float *__restrict__ psi,
-                 float *__restrict__ work, int *err, RootStrides rs) {
+__device__ __forceinline__ void gather_bar() {
+    asm volatile("bar.sync 1, %0;" ::"n"(kGatherThreads) : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
+          const unsigned char *__restrict__ aimg, const float *__restrict__ psi,
+          unsigned char *__restrict__ wimg, int *err, RootStrides rs) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ G0Col scol[256];
+    __shared__ __align__(8) uint64_t full[kMaxRing], fullb[kMaxRing], empty[kMaxRing], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag, n_issued, n_consumed, gather_stop;
     psi += blockIdx.y * rs.psi;
-    work += blockIdx.y * rs.work;
+    wimg += blockIdx.y * rs.wimg;
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    Tc1Row *srow = (Tc1Row *)(smem + kRing1Bytes);
-    uint64_t *full = (uint64_t *)(smem + kRing1Bytes + 128 * sizeof(Tc1Row));
-    uint64_t *empty = full + kMaxRing;
-    uint64_t *done = empty + kMaxRing;
-    uint32_t *tmem_slot = (uint32_t *)(done + 1);
-    int *abort_flag = (int *)(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const Tc1Tile tl = tiles[blockIdx.x];
-    const int n_stages = (tl.k0 + kTcStageK - 1) / kTcStageK;
-    const uint32_t slot_bytes = (2 * kABytes + (uint32_t)tl.n * kTcStageK * 8 + 1023) & ~1023u;
-    const int Rmax = min(kMaxRing, (int)(kRing1Bytes / slot_bytes));
-    const int P = min(kProducers, Rmax), D = Rmax / P, R = P * D;
-    const float *Rm = ops + tl.b0;
+    const G0Tile tl = tiles[blockIdx.x];
+    const int ns = tl.nsl;
+    const uint32_t b_bytes = (uint32_t)tl.n * 64;
+    const uint32_t slot_bytes = (2 * kABytes + 2 * b_bytes + 1023) & ~1023u;
+    const int R = min(kMaxRing, (int)(kRingBytes / slot_bytes));
+    const uint32_t rows8 = tl.a_bytes / 64;
 
-    for (int i = tid; i < tl.rows; i += kThreads)
-        srow[i] = rowtab[tl.rb + i];
+    for (int i = tid; i < tl.ncol; i += kThreads)
+        scol[i] = coltab[tl.cb + i];
     if (tid == 0) {
         for (int i = 0; i < R; i++) {
-            mbar_init(smem_u32(&full[i]), 1);
+            mbar_init(smem_u32(&full[i]), 1);   // the copy thread's expect_tx (bytes of the A slab)
+            mbar_init(smem_u32(&fullb[i]), 1);  // the gather leader (psi rows stored)
             mbar_init(smem_u32(&empty[i]), 1);
         }
-        mbar_init(smem_u32(done), 1);
-        *abort_flag = 0;
+        mbar_init(smem_u32(&done), 1);
+        abort_flag = 0, n_issued = 0, n_consumed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_u32(tmem_slot)), "r"(kMaxN));
+                     ::"r"(smem_u32(&tmem_slot)), "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    // A rows the copies never write (rows8 .. 127) stay zero for the whole tile
+    {
+        const uint32_t tail = kABytes - rows8 * 64;
+        for (int sl = 0; sl < R; sl++) {
+            unsigned char *a = smem + (uint32_t)sl * slot_bytes;
+            for (uint32_t o = (uint32_t)tid * 16; o < tail; o += kThreads * 16) {
+                *(uint4 *)(a + rows8 * 64 + o) = make_uint4(0, 0, 0, 0);
+                *(uint4 *)(a + kABytes + rows8 * 64 + o) = make_uint4(0, 0, 0, 0);
+            }
+        }
+    }
+    fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
+    const uint32_t tmem = tmem_slot;
 
-    if (warp < P) {
-        for (int ls = warp, j = 0; ls < n_stages; ls += P, j++) {
-            const int slot = warp + P * (j % D), use = j / D;
-            unsigned char *buf = smem + (uint32_t)slot * slot_bytes;
-            if (use >= 1) {
-                bool ok = false;
-                if (lane == 0)
-                    ok = mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1));
-                ok = __shfl_sync(0xffffffffu, ok, 0);
-                if (!ok) {
-                    if (lane == 0) {
-                        atomicExch(err, 1);
-                        atomicExch(abort_flag, 1);
-                    }
-                    break;
-                }
-            }
-            const int k0 = ls * kTcStageK;
-            // A: stacked psi rows lane + 32 i
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int row = lane + 32 * i;
-                float av[kTcStageK];
-                const bool live = row < tl.rows;
-                const uint64_t po = live ? srow[row].psi : 0;
-#pragma unroll
-                for (int q = 0; q < kTcStageK; q++)
-                    av[q] = (live && k0 + q < tl.k0) ? __ldg(psi + po + k0 + q) : 0.f;
-#pragma unroll
-                for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
-                    uint32_t h[4], l[4];
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++)
-                        split_tf32(av[4 * k4 + jj], h[jj], l[jj]);
-                    const uint32_t off = kmajor_off(row, 4 * k4);
-                    *(uint4 *)(buf + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                    *(uint4 *)(buf + kABytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
-                }
-            }
-            // B[n][k] = op(R)(k, col0 + n)
-            const uint32_t b_hi = 2 * kABytes, b_lo = b_hi + (uint32_t)tl.n * kTcStageK * 4;
-            for (int nn = lane; nn < tl.n; nn += 32) {
-                const int c = tl.col0 + nn;
-                float bv[kTcStageK];
-#pragma unroll
-                for (int q = 0; q < kTcStageK; q++) {
-                    const int k = k0 + q;
-                    bv[q] = (c < tl.n0 && k < tl.k0)
-                                ? __ldg(Rm + (tl.tb0 ? (uint64_t)c * tl.ldb0 + k : (uint64_t)k * tl.ldb0 + c))
-                                : 0.f;
-                }
-#pragma unroll
-                for (int k4 = 0; k4 < kTcStageK / 4; k4++) {
-                    uint32_t h[4], l[4];
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++)
-                        split_tf32(bv[4 * k4 + jj], h[jj], l[jj]);
-                    const uint32_t off = kmajor_off(nn, 4 * k4);
-                    *(uint4 *)(buf + b_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                    *(uint4 *)(buf + b_lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-                }
-            }
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0)
-                mbar_arrive(smem_u32(&full[slot]));
-        }
-    } else if (warp == kMmaWarp && lane == 0) {
-        const uint32_t idesc = make_idesc(tl.n);
-        for (int ls = 0; ls < n_stages; ls++) {
-            const int jj = ls / P, slot = ls % P + P * (jj % D), use = jj / D;
-            if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(use & 1))) {
+    if (warp == 0 && lane == 0) {
+        // ---------------- op(R)^T slabs by bulk copy
+        for (int j = 0; j < ns; j++) {
+            const int slot = j % R, use = j / R;
+            if (use >= 1 && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1))) {
                 atomicExch(err, 1);
-                atomicExch(abort_flag, 1);
+                atomicExch(&abort_flag, 1);
+                break;
+            }
+            if (*(volatile int *)&abort_flag)
+                break;
+            const uint32_t buf = smem_u32(smem + (uint32_t)slot * slot_bytes);
+            const uint32_t fb = smem_u32(&full[slot]);
+            const unsigned char *src = aimg + tl.a + (uint64_t)j * rows8 * 128;
+            mbar_expect_tx(fb, 2 * tl.a_bytes);
+            bulk_g2s(buf, src, tl.a_bytes, fb);
+            bulk_g2s(buf + kABytes, src + tl.a_bytes, tl.a_bytes, fb);
+            n_issued = j + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer
+        const uint32_t idesc = make_idesc(tl.n);
+        for (int j = 0; j < ns; j++) {
+            const int slot = j % R, use = j / R;
+            if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(use & 1)) ||
+                !mbar_wait(smem_u32(&fullb[slot]), (uint32_t)(use & 1))) {
+                atomicExch(err, 1);
+                atomicExch(&abort_flag, 1);
                 break;
             }
             tc_fence_after();
             const uint32_t a_hi = smem_u32(smem + (uint32_t)slot * slot_bytes), a_lo = a_hi + kABytes;
-            const uint32_t b_hi = a_hi + 2 * kABytes, b_lo = b_hi + (uint32_t)tl.n * kTcStageK * 4;
+            const uint32_t b_hi = a_hi + 2 * kABytes, b_lo = b_hi + b_bytes;
 #pragma unroll
             for (int h = 0; h < kTcStageK / 8; h++) {
-                const uint32_t ko = h * 2 * kLBO;
-                const uint32_t acc0 = (ls > 0 || h > 0) ? 1u : 0u;
+                const uint32_t ko = h * 2 * kLBO;  // K = 8 = two core matrices
+                const uint32_t acc0 = (j > 0 || h > 0) ? 1u : 0u;
                 mma_tf32(tmem, make_desc(a_hi + ko), make_desc(b_hi + ko), idesc, acc0);
                 mma_tf32(tmem, make_desc(a_hi + ko), make_desc(b_lo + ko), idesc, 1u);
                 mma_tf32(tmem, make_desc(a_lo + ko), make_desc(b_hi + ko), idesc, 1u);
             }
             mma_commit(smem_u32(&empty[slot]));
+            n_consumed = j + 1;
         }
-        mma_commit(smem_u32(done));
+        mma_commit(smem_u32(&done));
+    } else if (warp >= kGatherWarp0) {
+        // ---------------- psi rows (B, N x 16 per stage), all gather warps in step
+        const int gt = tid - 32 * kGatherWarp0;
+        for (int j = 0; j < ns; j++) {
+            const int slot = j % R, use = j / R;
+            if (use >= 1) {
+                // the leader's decision is broadcast through gather_stop so every
+                // gather thread leaves the loop together (no named-barrier mismatch)
+                if (gt == 0) {
+                    if (!mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1))) {
+                        atomicExch(err, 1);
+                        atomicExch(&abort_flag, 1);
+                    }
+                    gather_stop = *(volatile int *)&abort_flag;
+                }
+                gather_bar();
+                if (gather_stop)
+                    break;
+            }
+            unsigned char *buf = smem + (uint32_t)slot * slot_bytes + 2 * kABytes;
+            const int k0 = j * kTcStageK;
+            for (int e = gt; e < tl.n * kTcStageK; e += kGatherThreads) {
+                const int c = e >> 4, kk = e & 15, k = k0 + kk;
+                float v = 0.f;
+                if (c < tl.ncol && k < tl.k0 && scol[c].live)
+                    v = __ldg(psi + scol[c].psi + k);
+                uint32_t hi, lo;
+                split_tf32(v, hi, lo);
+                const uint32_t off = kmajor_off(c, kk);
+                *(uint32_t *)(buf + off) = hi;
+                *(uint32_t *)(buf + b_bytes + off) = lo;
+            }
+            fence_async_smem();
+            gather_bar();
+            if (gt == 0)
+                mbar_arrive(smem_u32(&fullb[slot]));
+        }
     }
+    // ---- epilogue: warps 4..7 own TMEM lane quarters (warp & 3)
     __syncwarp();
-    const int good = __syncthreads_and(mbar_wait(smem_u32(done), 0u) ? 1 : 0);
+    const int good = __syncthreads_and(mbar_wait(smem_u32(&done), 0u) ? 1 : 0);
     tc_fence_after();
     if (!good && tid == 0)
         atomicExch(err, 1);
-    if (good && *abort_flag == 0) {
-        const int q4 = warp & 3, half = warp >> 2;
-        const int trow = q4 * 32 + lane;
+    if (good && abort_flag == 0 && warp >= 4) {
+        const int q4 = warp & 3;
+        const int m = q4 * 32 + lane;               // W column m_off + m
         const uint32_t tbase = tmem + ((uint32_t)(q4 * 32) << 16);
-        for (int c16 = half * 16; c16 < tl.n; c16 += 32) {
+        const int nw = tl.m_off + m;
+        for (int c16 = 0; c16 < tl.n; c16 += 16) {
             float v[16];
             tmem_ld16(tbase + (uint32_t)c16, v);
-            if (trow >= tl.rows)
+            if (m >= tl.rows)
                 continue;
-            float *wrow = work + srow[trow].w + tl.col0 + c16;
-            const int lim = tl.n0 - tl.col0 - c16;
 #pragma unroll
-            for (int j = 0; j < 16; j++)
-                if (j < lim)
-                    wrow[j] = v[j];
+            for (int g = 0; g < 4; g++) {
+                const int c = c16 + 4 * g;
+                if (c >= tl.ncol)
+                    break;
+                const G0Col cl = scol[c];           // first of 4 rows of one product (k % 4 == 0)
+                unsigned char *base = wimg + cl.w + (uint64_t)(cl.k >> 4) * tl.npad * 128 +
+                                      kmajor_off(nw, cl.k & 15);
+                uint32_t h[4], l[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    split_tf32(v[4 * g + i], h[i], l[i]);
+                *(uint4 *)base = make_uint4(h[0], h[1], h[2], h[3]);
+                *(uint4 *)(base + tl.npad * 64) = make_uint4(l[0], l[1], l[2], l[3]);
+            }
         }
     }
     tc_fence_before();
     __syncthreads();
+    if (abort_flag && tid == 0) {
+        // copies issued but never consumed must land before the CTA exits
+        for (int j = n_consumed; j < n_issued; j++)
+            mbar_wait(smem_u32(&full[j % R]), (uint32_t)((j / R) & 1));
+    }
+    __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kMaxN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
 } // namespace
 
-} // namespace b2g
-
-namespace b2g {
-
-cudaError_t launch_tc_phase1(const DevicePlan &p, const float *ops, const float *psi, float *work,
-                             int *err, const RootStrides &rs, cudaStream_t s) {
-    if (p.n_tc1t == 0)
+cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const float *psi32,
+                      unsigned char *wimg, int *err, const RootStrides &rs, cudaStream_t s) {
+    if (p.n_g0tile == 0)
         return cudaSuccess;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(tc_phase1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmem1Bytes);
+        cudaError_t e = cudaFuncSetAttribute(g0_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmemBytes);
         if (e != cudaSuccess)
             return e;
         attr_set = true;
     }
-    tc_phase1_kernel<<<dim3((unsigned)p.n_tc1t, rs.nroots), kThreads, kSmem1Bytes, s>>>(
-        p.tc1t, p.tc1r, ops, psi, work, err, rs);
+    g0_kernel<<<dim3((unsigned)p.n_g0tile, rs.nroots), kThreads, kSmemBytes, s>>>(
+        p.g0tile, p.g0col, aimg, psi32, wimg, err, rs);
     return cudaGetLastError();
 }
 
