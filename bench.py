@@ -213,7 +213,8 @@ def run_ours(args, rank, local_rank, world, dist):
     head = args.form
     per_form = {}
     head_res = None
-    for name in [head] + [f for f in FORMS if f != head]:
+    forms_timed = [head] if args.headline_only else [head] + [f for f in FORMS if f != head]
+    for name in forms_timed:
         clocks = ClockSampler(local_rank) if name == head else None
         total, t_wall, p1, p2, ck, nrm = time_form(FORMS[name], clocks)
         tt = torch.tensor([total], dtype=torch.float64, device=dev)
@@ -232,7 +233,7 @@ def run_ours(args, rank, local_rank, world, dist):
         ref = torch.zeros_like(sig)
     heff.apply_ptr(psi.data_ptr(), ref.data_ptr(), 1.0, FORMS["fp64"])
     heff.status()
-    for name in FORMS:
+    for name in forms_timed:
         with torch.cuda.stream(stream):
             out = torch.zeros_like(sig)
         heff.apply_ptr(psi.data_ptr(), out.data_ptr(), 1.0, FORMS[name])
@@ -246,7 +247,7 @@ def run_ours(args, rank, local_rank, world, dist):
     xb = torch.randn((nb, prob.psi_size), dtype=torch.float64, device=dev)
     yb = torch.zeros((nb, prob.sigma_size), dtype=torch.float64, device=dev)
     torch.cuda.synchronize()  # made on torch's stream, used on the library's
-    for name in ("tf32x3", "fp64"):
+    for name in (() if args.headline_only else ("tf32x3", "fp64")):
         form = FORMS[name]
         for _ in range(2):
             heff.apply_batch(xb, yb, 1.0, form)
@@ -364,7 +365,7 @@ def run_ours(args, rank, local_rank, world, dist):
     dh = b2g.EffectiveHamiltonian(ctx, dprob.seq(), dprob.ops, dprob.psi_size, dprob.sigma_size)
     dav = {"workload": "heff_hub16_su2_M250", "reference_energy": dprob.meta["davidson_energy"],
            "conv_thrd": dprob.meta["conv_thrd"]}
-    for name in ("fp64", "tf32x3"):
+    for name in (() if args.headline_only else ("fp64", "tf32x3")):
         x = np.array(dprob.psi, copy=True)
         e, ndav, nfl, tdav = dh.eigs(dprob.diag, x, conv_thrd=dprob.meta["conv_thrd"],
                                      def_min=dprob.meta["def_min"], def_max=dprob.meta["def_max"],
@@ -417,6 +418,9 @@ def main():
     ap.add_argument("--workload", default=None)
     ap.add_argument("--form", default="tf32x3", choices=sorted(FORMS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="time only the headline form (no other forms, batched roots or Davidson "
+                         "sections); for profiler runs")
     args = ap.parse_args()
     from b2g import workloads
     if args.workload is None:

@@ -200,7 +200,11 @@ g1_kernel(const G1Task *__restrict__ tasks, const G1Tile *__restrict__ tiles,
 }
 
 // sigma += scale * (sum of the partials of every tile covering the cell), per
-// reduction item (rows [r0, r1) of one region), tiles and chunks in fixed order
+// reduction item (rows [r0, r1) of one region, with the list of the tiles that
+// meet those rows), tiles and chunks in fixed order.  The partials are summed
+// in FP32 with Kahan compensation (FP64 adds would run on GB300's narrow FP64
+// pipe) and added to sigma in FP64.
+constexpr int kRedTiles = 64;
 __global__ void __launch_bounds__(256) g1_reduce(const G1Red *__restrict__ items,
                                                  const int32_t *__restrict__ cover,
                                                  const G1Tile *__restrict__ tiles,
@@ -208,31 +212,48 @@ __global__ void __launch_bounds__(256) g1_reduce(const G1Red *__restrict__ items
                                                  const float *__restrict__ part,
                                                  double *__restrict__ sigma, double scale,
                                                  RootStrides rs) {
+    __shared__ G1Tile st[kRedTiles];
     const G1Red it = items[blockIdx.x];
     part += blockIdx.y * rs.part;
     sigma += blockIdx.y * rs.sigma;
     const Region rg = regions[it.g];
+    const int nt = it.t1 - it.t0;
+    for (int i = threadIdx.x; i < min(nt, kRedTiles); i += blockDim.x)
+        st[i] = tiles[cover[it.t0 + i]];
+    __syncthreads();
     const int nr = it.r1 - it.r0;
     for (int e = threadIdx.x; e < nr * rg.cols; e += blockDim.x) {
         const int r = it.r0 + e / rg.cols, c = e % rg.cols;
         const uint64_t a = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
         if (a < rg.lo || a >= rg.hi)
             continue;
-        double s = 0.0;
+        float s = 0.f, comp = 0.f;
         bool covered = false;
-        for (int q = it.t0; q < it.t1; q++) {
-            const G1Tile tl = tiles[cover[q]];
+        for (int q = 0; q < nt; q++) {
+            const G1Tile tl = q < kRedTiles ? st[q] : tiles[cover[it.t0 + q]];
             const int rr = r - tl.row0, cc = c - tl.col0;
             if (rr < 0 || rr >= tl.rows || cc < 0 || cc >= tl.ncols)
                 continue;
             covered = true;
             const float *p = part + tl.part + (int64_t)rr * tl.n + cc;
             const int64_t plane = (int64_t)tl.rows * tl.n;
-            for (int ch = 0; ch < tl.n_chunks; ch++)
-                s += (double)p[ch * plane];
+            // eight chunk loads in flight, then their compensated adds in order
+            for (int ch0 = 0; ch0 < tl.n_chunks; ch0 += 8) {
+                float x[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+                    x[i] = ch0 + i < tl.n_chunks ? __ldg(p + (ch0 + i) * plane) : 0.f;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const float y = x[i] - comp;
+                    const float t = s + y;
+                    comp = (t - s) - y;
+                    s = t;
+                }
+            }
         }
         if (covered)
-            sigma[a] += scale * s;
+            sigma[a] += scale * ((double)s - (double)comp);
     }
 }
 

@@ -278,14 +278,19 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                     }
             }
             const int32_t t_last = (int32_t)plan.g1tile.size();
-            const int32_t cv0 = (int32_t)plan.g1cover.size();
-            for (int32_t t = t_first; t < t_last; t++)
-                plan.g1cover.push_back(t);
+            // reduction items: 16 region rows each, with the tiles meeting those rows
             for (int32_t r0 = 0; r0 < rows; r0 += 16) {
                 G1Red it;
                 it.g = g, it.r0 = r0, it.r1 = std::min(rows, r0 + 16);
-                it.t0 = cv0, it.t1 = (int32_t)plan.g1cover.size(), it.pad = 0;
-                plan.g1red.push_back(it);
+                it.t0 = (int32_t)plan.g1cover.size();
+                for (int32_t t = t_first; t < t_last; t++) {
+                    const G1Tile &tt = plan.g1tile[t];
+                    if (tt.row0 < it.r1 && tt.row0 + tt.rows > it.r0)
+                        plan.g1cover.push_back(t);
+                }
+                it.t1 = (int32_t)plan.g1cover.size(), it.pad = 0;
+                if (it.t1 > it.t0)
+                    plan.g1red.push_back(it);
             }
         }
     }

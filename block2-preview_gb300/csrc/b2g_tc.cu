@@ -7,7 +7,8 @@
 //   * warp 0 lane 0 bulk-copies the stage's op(R)^T slab (TF32 hi/lo,
 //     canonical K-major layout, built once per H_eff) into a ring slot;
 //   * warps 2..7 gather the stage's psi rows from the FP32 psi copy (L2
-//     resident), split them into hi/lo and store them in the slot;
+//     resident) with 4-byte cp.async copies (two stages in flight), then
+//     split them in shared memory into the TF32 hi/lo parts;
 //   * warp 1 lane 0 waits for both (the copies' mbarrier with their byte
 //     count, the gather's mbarrier), issues the six MMAs and commits them to
 //     the slot's empty barrier;
@@ -38,6 +39,15 @@ constexpr uint32_t kTmemCols = 256;
 __device__ __forceinline__ void gather_bar() {
     asm volatile("bar.sync 1, %0;" ::"n"(kGatherThreads) : "memory");
 }
+
+// 4-byte asynchronous copy global -> shared; src_bytes = 0 writes a zero
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float *src, uint32_t src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 __global__ void __launch_bounds__(kThreads, 2)
 g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
@@ -139,42 +149,65 @@ g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
         }
         mma_commit(smem_u32(&done));
     } else if (warp >= kGatherWarp0) {
-        // ---------------- psi rows (B, N x 16 per stage), all gather warps in step
+        // ---------------- psi rows (B, N x 16 per stage): 4-byte cp.async copies
+        // straight into the slot's hi region (zero-filled where a row or K
+        // column is padding), two stages in flight; the stage before is then
+        // split in place (hi) and into the lo region, and released to the MMA
         const int gt = tid - 32 * kGatherWarp0;
-        for (int j = 0; j < ns; j++) {
-            const int slot = j % R, use = j / R;
-            if (use >= 1) {
-                // the leader's decision is broadcast through gather_stop so every
-                // gather thread leaves the loop together (no named-barrier mismatch)
-                if (gt == 0) {
-                    if (!mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1))) {
-                        atomicExch(err, 1);
-                        atomicExch(&abort_flag, 1);
+        const int ne = tl.n * kTcStageK;
+        bool stop = false;
+        for (int j = 0; j <= ns && !stop; j++) {
+            if (j < ns) {
+                const int slot = j % R, use = j / R;
+                if (use >= 1) {
+                    // the leader's decision reaches every gather thread through
+                    // gather_stop, so they leave the loop together
+                    if (gt == 0) {
+                        if (!mbar_wait(smem_u32(&empty[slot]), (uint32_t)((use - 1) & 1))) {
+                            atomicExch(err, 1);
+                            atomicExch(&abort_flag, 1);
+                        }
+                        gather_stop = *(volatile int *)&abort_flag;
                     }
-                    gather_stop = *(volatile int *)&abort_flag;
+                    gather_bar();
+                    stop = gather_stop != 0;
                 }
+                if (!stop) {
+                    const uint32_t buf = smem_u32(smem + (uint32_t)slot * slot_bytes + 2 * kABytes);
+                    const int k0 = j * kTcStageK;
+                    for (int e = gt; e < ne; e += kGatherThreads) {
+                        const int c = e >> 4, kk = e & 15, k = k0 + kk;
+                        const bool ok = c < tl.ncol && k < tl.k0 && scol[c].live;
+                        cp_async4(buf + kmajor_off(c, kk), ok ? psi + scol[c].psi + k : psi, ok ? 4u : 0u);
+                    }
+                }
+                cp_async_commit();
+            }
+            if (j >= 1 && !stop) {
+                if (j < ns)
+                    cp_async_wait1();
+                else
+                    cp_async_wait0();
                 gather_bar();
-                if (gather_stop)
-                    break;
+                const int slot = (j - 1) % R;
+                unsigned char *buf = smem + (uint32_t)slot * slot_bytes + 2 * kABytes;
+                for (int q = gt; q < tl.n * 4; q += kGatherThreads) {
+                    const float4 x = *(const float4 *)(buf + q * 16);
+                    uint32_t h[4], l[4];
+                    split_tf32(x.x, h[0], l[0]);
+                    split_tf32(x.y, h[1], l[1]);
+                    split_tf32(x.z, h[2], l[2]);
+                    split_tf32(x.w, h[3], l[3]);
+                    *(uint4 *)(buf + q * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *(uint4 *)(buf + b_bytes + q * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+                }
+                fence_async_smem();
+                gather_bar();
+                if (gt == 0)
+                    mbar_arrive(smem_u32(&fullb[slot]));
             }
-            unsigned char *buf = smem + (uint32_t)slot * slot_bytes + 2 * kABytes;
-            const int k0 = j * kTcStageK;
-            for (int e = gt; e < tl.n * kTcStageK; e += kGatherThreads) {
-                const int c = e >> 4, kk = e & 15, k = k0 + kk;
-                float v = 0.f;
-                if (c < tl.ncol && k < tl.k0 && scol[c].live)
-                    v = __ldg(psi + scol[c].psi + k);
-                uint32_t hi, lo;
-                split_tf32(v, hi, lo);
-                const uint32_t off = kmajor_off(c, kk);
-                *(uint32_t *)(buf + off) = hi;
-                *(uint32_t *)(buf + b_bytes + off) = lo;
-            }
-            fence_async_smem();
-            gather_bar();
-            if (gt == 0)
-                mbar_arrive(smem_u32(&fullb[slot]));
         }
+        cp_async_wait0();  // nothing may land after the CTA has moved on
     }
     // ---- epilogue: warps 4..7 own TMEM lane quarters (warp & 3)
     __syncwarp();
