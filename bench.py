@@ -377,6 +377,11 @@ def run_ours(args, rank, local_rank, world, dist):
                      "reduced_products": r.n_apply_mixed, "seconds": tdav}
     dh.close()
     result["davidson"] = dav
+    # ---- density-matrix truncation of the reference's converged psi at the
+    # n=24 M=1000 middle site (28 blocks, 2827 states): GPU vs the oracle's
+    # numpy/LAPACK restatement, spectrum and discarded weight vs the reference
+    if not args.headline_only:
+        result["truncation"] = truncation_section(ctx)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, nth, blas = cpu_replay_timing(prob, max_steps=10, budget_s=20.0, warmup=1)
         result["cpu_baseline"] = {
@@ -388,6 +393,38 @@ def run_ours(args, rank, local_rank, world, dist):
     heff.close()
     ctx.close()
     return result
+
+
+def truncation_section(ctx):
+
+    from b2g.truncation import DensityMatrixLayout, split_density_matrix
+    path = os.path.join(ROOT, "tests", "golden", "syn24_su2_M1000_dm.npz")
+    z = np.load(path)
+    lay = DensityMatrixLayout(bool(z["trace_right"]), z["psi_dm"], z["psi_rows"], z["psi_cols"],
+                              z["psi_off"], z["dm_dim"])
+    k, cut = int(z["bond_dim"]), float(z["cutoff"])
+    for _ in range(2):
+        res = split_density_matrix(ctx, lay, z["psi"], k, cut)
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        res = split_density_matrix(ctx, lay, z["psi"], k, cut)
+        ts.append(time.perf_counter() - t0)
+    eig_ref = z["dm_eig"]
+    eig = np.concatenate(res.eigenvalues)
+    out = {"workload": "syn24_su2_M1000 middle-site density matrix (" + str(int(z["dm_dim"].size))
+                       + " blocks, " + str(int(z["dm_dim"].sum())) + " states, largest "
+                       + str(int(z["dm_dim"].max())) + ")",
+           "gpu_ms": 1e3 * statistics.median(ts), "kept": res.n_kept,
+           "error": res.error, "reference_error": float(z["error"]),
+           "max_abs_eig_err_vs_reference": float(np.abs(eig - eig_ref).max())}
+    from oracle import oracle as _oracle
+    t0 = time.perf_counter()
+    _oracle.dm_truncate(bool(z["trace_right"]), z["psi_dm"], z["psi_rows"], z["psi_cols"], z["psi_off"],
+                        z["dm_dim"], z["psi"], k, cut)
+    out["cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["cpu_oracle"] = "numpy (LAPACK syevd) restatement, host threads of the BLAS"
+    return out
 
 
 def run_reference(args):

@@ -149,10 +149,36 @@ def run_case(name, args, desc):
               f"M={int(ts['bond_dim'])} error={ts['error']:.3e} -> {os.path.getsize(tpath)} bytes")
 
 
+def dm_fixture_from_dump(site_dir, name, desc):
+    """A *_dm.npz fixture from an existing harness site dump (for the large
+    truncation case, whose reference run takes ~25 minutes: the synthetic
+    n=24 M=1000 SU(2) run of block2-preview_gb300/workloads/make_workload.py,
+    sweep 2 middle site)."""
+    ta, ts = read_dump(os.path.join(site_dir, "truncation"))
+    post_a, _ = read_dump(os.path.join(site_dir, "post"))
+    keep = {k: v for k, v in ta.items() if not k.startswith(("left_data", "right_data", "rho"))}
+    tpath = os.path.join(HERE, name + "_dm.npz")
+    np.savez_compressed(
+        tpath, psi=post_a["psi"], trace_right=np.int32(ts["trace_right"]),
+        bond_dim=np.int32(ts["bond_dim"]), cutoff=np.float64(ts["cutoff"]),
+        error=np.float64(ts["error"]), **keep,
+        meta=np.array(json.dumps({"name": name + "_dm", "kind": "truncation", "description": desc,
+                                  "split_tensors": False})))
+    print(f"{name}_dm: dm blocks={ta['dm_dim'].size} states={int(ta['dm_dim'].sum())} "
+          f"-> {os.path.getsize(tpath)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default=None)
+    ap.add_argument("--dm-from-dump", nargs=2, metavar=("SITE_DIR", "NAME"), default=None,
+                    help="write NAME_dm.npz (spectrum and discarded weight only) from a site dump")
     a = ap.parse_args()
+    if a.dm_from_dump:
+        dm_fixture_from_dump(a.dm_from_dump[0], a.dm_from_dump[1],
+                             "density-matrix truncation, synthetic ab initio n=24 N=24 (seed 0), "
+                             "SU(2), M=1000, sweep 2 middle site (spectrum and discarded weight)")
+        return
     if not os.path.exists(HARNESS):
         subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     for name, (args, desc) in CASES.items():
