@@ -12,7 +12,7 @@ namespace tcg {
 
 constexpr uint32_t kSBO = 512;                          // bytes between 8-row groups (K slab of 16)
 constexpr uint32_t kLBO = 128;                         // bytes between K-adjacent core matrices
-constexpr long long kSpinLimit = 1ll << 24;            // bounded waits (a stage takes microseconds)
+constexpr long long kSpinLimit = 1ll << 23;            // bounded waits (tries, mostly 256 ns apart)
 
 static __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -62,8 +62,12 @@ static __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) 
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// bounded wait for phase `parity` of an mbarrier; false on timeout
+// bounded wait for phase `parity` of an mbarrier; false on timeout.  After a
+// few immediate tries the waiting thread backs off with __nanosleep (32 ns
+// doubling to 256 ns), so waiting warps leave the issue slots to the warps
+// doing the work; at most kSpinLimit tries (about two seconds).
 static __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t ns = 32;
     for (long long it = 0; it < kSpinLimit; it++) {
         uint32_t done;
         asm volatile(
@@ -73,6 +77,10 @@ static __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
             : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
         if (done)
             return true;
+        if (it >= 4) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : 256;
+        }
     }
     return false;
 }
