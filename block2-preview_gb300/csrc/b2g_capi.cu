@@ -75,13 +75,14 @@ static int ensure_g1(b2g_heff *h, int nroots) {
     if (nroots <= h->g1_roots)
         return B2G_OK;
     B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
-    cudaFree(h->g1_wimg), cudaFree(h->g1_part);
-    h->g1_wimg = nullptr, h->g1_part = nullptr, h->g1_roots = 0;
+    cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
+    h->g1_wimg = nullptr, h->g1_part = nullptr, h->g0_psi = nullptr, h->g1_roots = 0;
     const size_t R = (size_t)nroots;
     if ((p.g1_wbytes && cudaMalloc(&h->g1_wimg, p.g1_wbytes * R) != cudaSuccess) ||
-        (p.g1_part && cudaMalloc(&h->g1_part, sizeof(float) * p.g1_part * R) != cudaSuccess)) {
-        cudaFree(h->g1_wimg), cudaFree(h->g1_part);
-        h->g1_wimg = nullptr, h->g1_part = nullptr;
+        (p.g1_part && cudaMalloc(&h->g1_part, sizeof(float) * p.g1_part * R) != cudaSuccess) ||
+        (p.g0_psi_floats && cudaMalloc(&h->g0_psi, sizeof(float) * p.g0_psi_floats * R) != cudaSuccess)) {
+        cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
+        h->g1_wimg = nullptr, h->g1_part = nullptr, h->g0_psi = nullptr;
         return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the GEMM1 work images of " +
                                        std::to_string(nroots) + " roots");
     }
@@ -167,7 +168,7 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         free_plan(h->plan);
         cudaFree(h->ops), cudaFree(h->work), cudaFree(h->err);
         cudaFree(h->simt_part), cudaFree(h->psi32);
-        cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part);
+        cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
         delete h;
         return code;
     };
@@ -200,10 +201,12 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         (rc = upload(hp.g1tile, &p.g1tile, s)) ||
         (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
         (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
-        (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)))
+        (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
+        (rc = upload(hp.g0psi, &p.g0psi, s)))
         return bail(rc);
     p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
     p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
+    p.n_g0psi = (int64_t)hp.g0psi.size(), p.g0_psi_floats = hp.g0_psi_floats;
     p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
     p.n_t2multi = (int64_t)hp.t2multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
@@ -251,7 +254,7 @@ int b2g_heff_destroy(b2g_heff *h) {
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
     cudaFree(h->simt_part);
-    cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part);
+    cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
     cudaFree(h->psi_stage), cudaFree(h->sigma_stage), cudaFree(h->err);
     for (auto &e : h->ev)
         if (e)
@@ -365,15 +368,17 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
         rs.work = 2 * h->work_size;  // floats per root in a buffer sized in doubles
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-        // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
-        B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
         if (form == B2G_TF32X3) {
+            // psi enters as a packed FP32 copy of its sub-blocks (made by launch_g0)
             if ((rc = ensure_g1(h, nroots)) != B2G_OK)
                 return rc;
             rs.wimg = h->plan.g1_wbytes, rs.part = h->plan.g1_part;
-            B2G_CUDA_TRY(launch_g0(h->plan, h->g1_aimg, h->psi32, h->g1_wimg, h->err, rs, s));
-        } else
+            B2G_CUDA_TRY(launch_g0(h->plan, h->g1_aimg, psi, h->g0_psi, h->g1_wimg, h->err, rs, s));
+        } else {
+            // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
+            B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
             B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
+        }
         if (h->timing)
             B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
         if (form == B2G_TF32X3) {

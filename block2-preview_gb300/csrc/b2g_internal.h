@@ -86,8 +86,13 @@ struct G0Tile {
     int32_t k0, npad, m_off;    // K, W image width (n0 rounded up to 16), W column of row 0
     int64_t cb;                 // first entry in the column table
 };
+struct G0Psi {                  // one distinct psi sub-block, packed per product
+    uint64_t src;               // psi offset (a0)
+    uint64_t dst;               // packed offset (floats, multiple of 4)
+    int32_t m0, k0, lda0, k0p;  // rows, columns, psi leading dimension, packed row stride (k0 -> 4)
+};
 struct G0Col {                  // one stacked psi row (one W image K row)
-    uint64_t psi;               // psi offset of the row (a0 + i * lda0)
+    uint64_t psi;               // packed-psi offset of the row (16-byte aligned)
     uint64_t w;                 // byte offset of its W image (per root)
     int32_t k;                  // row index i within the product
     int32_t live;               // i < m0 (padding rows read zeros)
@@ -145,6 +150,8 @@ constexpr int kG1SlabK = 16;
 struct HostPlan {
     std::vector<G0Tile> g0tile;
     std::vector<G0Col> g0col;
+    std::vector<G0Psi> g0psi;
+    uint64_t g0_psi_floats = 0;     // packed psi floats per root
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
     std::vector<Region> regions;
@@ -182,7 +189,9 @@ struct DevicePlan {
     int32_t *lists = nullptr;
     G0Tile *g0tile = nullptr;
     G0Col *g0col = nullptr;
-    int64_t n_g0tile = 0;
+    G0Psi *g0psi = nullptr;
+    int64_t n_g0tile = 0, n_g0psi = 0;
+    uint64_t g0_psi_floats = 0;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
     G1Tile *g1tile = nullptr;
     G1Stage *g1stage = nullptr;
@@ -205,8 +214,9 @@ struct RootStrides {
 
 // tensor-core launchers (b2g_tc.cu); err: device int set non-zero when a
 // bounded wait gives up
-cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const float *psi32,
-                      unsigned char *wimg, int *err, const RootStrides &rs, cudaStream_t s);
+cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const double *psi,
+                      float *psi_packed, unsigned char *wimg, int *err, const RootStrides &rs,
+                      cudaStream_t s);
 
 // image-fed tensor-core GEMM1 (b2g_g1.cu)
 cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned char *aimg,
@@ -247,6 +257,7 @@ struct b2g_heff {
     unsigned char *g1_wimg = nullptr;  // g1_roots x W images
     float *g1_part = nullptr;          // g1_roots x image-fed GEMM1 partial tiles
     int g1_roots = 0;                  // roots the W images / partials are sized for
+    float *g0_psi = nullptr;           // g1_roots x packed psi sub-blocks (GEMM0 operand)
     int cap_roots = 0;           // roots the per-root buffers are sized for
     int stage_roots = 0;         // roots the host staging buffers are sized for
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0, work_size = 0;

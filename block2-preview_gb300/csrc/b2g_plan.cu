@@ -407,6 +407,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             const WorkDesc &a = plan.works[x], &b = plan.works[y];
             return a.b0 == b.b0 && a.tb0 == b.tb0 && a.k0 == b.k0 && a.n0 == b.n0 && a.ldb0 == b.ldb0;
         };
+        std::map<std::array<int64_t, 4>, int32_t> pmap;  // distinct psi sub-blocks
         for (size_t gs = 0; gs < ord.size();) {
             size_t ge = gs + 1;
             while (ge < ord.size() && same_r(ord[gs], ord[ge]))
@@ -422,15 +423,27 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 plan.g1_abytes += (uint64_t)rows8 * 128 * nsl;
             }
             plan.g1aimg.push_back(im);
-            // stacked psi rows, each product padded to a multiple of 4
+            // stacked psi rows, each product padded to a multiple of 4; the rows
+            // point into the packed copy of their psi sub-block
             std::vector<G0Col> cols;
             for (size_t q = gs; q < ge; q++) {
                 const int32_t u = ord[q];
                 const WorkDesc &w = plan.works[u];
+                const std::array<int64_t, 4> pk{(int64_t)w.a0, w.m0, w.k0, w.lda0};
+                auto pit = pmap.find(pk);
+                if (pit == pmap.end()) {
+                    G0Psi ps;
+                    ps.src = w.a0, ps.dst = plan.g0_psi_floats;
+                    ps.m0 = w.m0, ps.k0 = w.k0, ps.lda0 = w.lda0, ps.k0p = (w.k0 + 3) / 4 * 4;
+                    plan.g0_psi_floats += (uint64_t)ps.m0 * ps.k0p;
+                    pit = pmap.emplace(pk, (int32_t)plan.g0psi.size()).first;
+                    plan.g0psi.push_back(ps);
+                }
+                const G0Psi &ps = plan.g0psi[pit->second];
                 const int32_t m0p = (w.m0 + 3) / 4 * 4;
                 for (int32_t i = 0; i < m0p; i++) {
                     G0Col c;
-                    c.psi = i < w.m0 ? w.a0 + (uint64_t)i * w.lda0 : 0;
+                    c.psi = i < w.m0 ? ps.dst + (uint64_t)i * ps.k0p : 0;
                     c.w = plan.g1wimg[u].dst, c.k = i, c.live = i < w.m0 ? 1 : 0;
                     cols.push_back(c);
                 }

@@ -6,9 +6,10 @@
 // rows of the products that share R), K = k0 in 16-column stages:
 //   * warp 0 lane 0 bulk-copies the stage's op(R)^T slab (TF32 hi/lo,
 //     canonical K-major layout, built once per H_eff) into a ring slot;
-//   * warps 2..7 gather the stage's psi rows from the FP32 psi copy (L2
-//     resident) with 4-byte cp.async copies (two stages in flight), then
-//     split them in shared memory into the TF32 hi/lo parts;
+//   * warps 2..7 gather the stage's psi rows from a packed FP32 copy of the
+//     psi sub-blocks (rows 16-byte aligned and zero-padded to 4 columns, made
+//     per product, L2 resident) with 16-byte cp.async copies (two stages in
+//     flight), then split them in shared memory into the TF32 hi/lo parts;
 //   * warp 1 lane 0 waits for both (the copies' mbarrier with their byte
 //     count, the gather's mbarrier), issues the six MMAs and commits them to
 //     the slot's empty barrier;
@@ -40,10 +41,24 @@ __device__ __forceinline__ void gather_bar() {
     asm volatile("bar.sync 1, %0;" ::"n"(kGatherThreads) : "memory");
 }
 
-// 4-byte asynchronous copy global -> shared; src_bytes = 0 writes a zero
-__device__ __forceinline__ void cp_async4(uint32_t dst, const float *src, uint32_t src_bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
+// 16-byte asynchronous copy global -> shared (L2 only); src_bytes = 0 writes zeros
+__device__ __forceinline__ void cp_async16(uint32_t dst, const float *src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
                  : "memory");
+}
+
+// psi sub-blocks -> packed FP32 copy with rows padded (zeros) to a multiple of 4
+__global__ void __launch_bounds__(256) g0_pack_psi(const G0Psi *__restrict__ blocks,
+                                                   const double *__restrict__ psi,
+                                                   float *__restrict__ out, RootStrides rs,
+                                                   uint64_t out_stride) {
+    const G0Psi b = blocks[blockIdx.x];
+    psi += blockIdx.y * rs.psi;
+    out += blockIdx.y * out_stride;
+    for (int e = threadIdx.x; e < b.m0 * b.k0p; e += blockDim.x) {
+        const int i = e / b.k0p, k = e - i * b.k0p;
+        out[b.dst + e] = k < b.k0 ? (float)psi[b.src + (uint64_t)i * b.lda0 + k] : 0.f;
+    }
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
@@ -154,7 +169,7 @@ g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
         // column is padding), two stages in flight; the stage before is then
         // split in place (hi) and into the lo region, and released to the MMA
         const int gt = tid - 32 * kGatherWarp0;
-        const int ne = tl.n * kTcStageK;
+        const int ne = tl.n * kTcStageK / 4;
         bool stop = false;
         for (int j = 0; j <= ns && !stop; j++) {
             if (j < ns) {
@@ -176,9 +191,11 @@ g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
                     const uint32_t buf = smem_u32(smem + (uint32_t)slot * slot_bytes + 2 * kABytes);
                     const int k0 = j * kTcStageK;
                     for (int e = gt; e < ne; e += kGatherThreads) {
-                        const int c = e >> 4, kk = e & 15, k = k0 + kk;
+                        // one 16-byte chunk (4 K columns of one row) of the packed psi
+                        // copy, whose rows are zero-padded to a multiple of 4 columns
+                        const int c = e >> 2, kq = 4 * (e & 3), k = k0 + kq;
                         const bool ok = c < tl.ncol && k < tl.k0 && scol[c].live;
-                        cp_async4(buf + kmajor_off(c, kk), ok ? psi + scol[c].psi + k : psi, ok ? 4u : 0u);
+                        cp_async16(buf + kmajor_off(c, kq), ok ? psi + scol[c].psi + k : psi, ok ? 16u : 0u);
                     }
                 }
                 cp_async_commit();
@@ -256,8 +273,9 @@ g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
 
 } // namespace
 
-cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const float *psi32,
-                      unsigned char *wimg, int *err, const RootStrides &rs, cudaStream_t s) {
+cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const double *psi,
+                      float *psi_packed, unsigned char *wimg, int *err, const RootStrides &rs,
+                      cudaStream_t s) {
     if (p.n_g0tile == 0)
         return cudaSuccess;
     static bool attr_set = false;
@@ -268,8 +286,15 @@ cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const floa
             return e;
         attr_set = true;
     }
+    g0_pack_psi<<<dim3((unsigned)p.n_g0psi, rs.nroots), 256, 0, s>>>(p.g0psi, psi, psi_packed, rs,
+                                                                    p.g0_psi_floats);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    RootStrides rp = rs;
+    rp.psi = p.g0_psi_floats;  // the kernel reads the packed copy
     g0_kernel<<<dim3((unsigned)p.n_g0tile, rs.nroots), kThreads, kSmemBytes, s>>>(
-        p.g0tile, p.g0col, aimg, psi32, wimg, err, rs);
+        p.g0tile, p.g0col, aimg, psi_packed, wimg, err, rp);
     return cudaGetLastError();
 }
 
