@@ -151,6 +151,7 @@ struct HostPlan {
     std::vector<G0Tile> g0tile;
     std::vector<G0Col> g0col;
     std::vector<G0Psi> g0psi;
+    int64_t g0_wide = 0;            // tiles [0, g0_wide) are wider than 128 columns
     uint64_t g0_psi_floats = 0;     // packed psi floats per root
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
@@ -190,7 +191,7 @@ struct DevicePlan {
     G0Tile *g0tile = nullptr;
     G0Col *g0col = nullptr;
     G0Psi *g0psi = nullptr;
-    int64_t n_g0tile = 0, n_g0psi = 0;
+    int64_t n_g0tile = 0, n_g0psi = 0, n_g0wide = 0;  // tiles [0, n_g0wide) are wider than 128
     uint64_t g0_psi_floats = 0;
     int64_t n_works = 0, n_contribs = 0, n_regions = 0, n_t1 = 0, n_t2 = 0, n_lists = 0;
     G1Tile *g1tile = nullptr;

@@ -278,10 +278,11 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                     }
             }
             const int32_t t_last = (int32_t)plan.g1tile.size();
-            // reduction items: 16 region rows each, with the tiles meeting those rows
-            for (int32_t r0 = 0; r0 < rows; r0 += 16) {
+            // reduction items: 4 region rows each (enough CTAs to keep the chunk
+            // loads in flight), with the tiles meeting those rows
+            for (int32_t r0 = 0; r0 < rows; r0 += 4) {
                 G1Red it;
-                it.g = g, it.r0 = r0, it.r1 = std::min(rows, r0 + 16);
+                it.g = g, it.r0 = r0, it.r1 = std::min(rows, r0 + 4);
                 it.t0 = (int32_t)plan.g1cover.size();
                 for (int32_t t = t_first; t < t_last; t++) {
                     const G1Tile &tt = plan.g1tile[t];
@@ -465,8 +466,16 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             }
             gs = ge;
         }
-        std::stable_sort(plan.g0tile.begin(), plan.g0tile.end(),
-                         [](const G0Tile &a, const G0Tile &b) { return (int64_t)a.nsl * a.n > (int64_t)b.nsl * b.n; });
+        // wide tiles (N > 128) first, each class longest first
+        std::stable_sort(plan.g0tile.begin(), plan.g0tile.end(), [](const G0Tile &a, const G0Tile &b) {
+            const bool wa = a.n > 128, wb = b.n > 128;
+            if (wa != wb)
+                return wa;
+            return (int64_t)a.nsl * a.n > (int64_t)b.nsl * b.n;
+        });
+        plan.g0_wide = 0;
+        while (plan.g0_wide < (int64_t)plan.g0tile.size() && plan.g0tile[plan.g0_wide].n > 128)
+            plan.g0_wide++;
     }
     return B2G_OK;
 }

@@ -33,9 +33,9 @@ constexpr int kGatherWarp0 = 2;                      // warps 2..7 gather psi
 constexpr int kGatherThreads = kThreads - 32 * kGatherWarp0;
 constexpr int kMaxRing = 4;
 constexpr uint32_t kABytes = 128 * kTcStageK * 4;    // one split part of the A slab (8 KB)
-constexpr uint32_t kRingBytes = 96 * 1024;           // two CTAs per SM
-constexpr uint32_t kSmemBytes = kRingBytes + 1024;
-constexpr uint32_t kTmemCols = 256;
+// two instantiations: tiles wider than 128 columns (96 KB ring, 256 TMEM
+// columns, two CTAs per SM) and the rest (64 KB ring, 128 columns, three)
+constexpr uint32_t kWideRing = 96 * 1024, kNarrowRing = 64 * 1024;
 
 __device__ __forceinline__ void gather_bar() {
     asm volatile("bar.sync 1, %0;" ::"n"(kGatherThreads) : "memory");
@@ -64,7 +64,8 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-__global__ void __launch_bounds__(kThreads, 2)
+template <uint32_t kRingBytes, uint32_t kTmemCols, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
 g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
           const unsigned char *__restrict__ aimg, const float *__restrict__ psi,
           unsigned char *__restrict__ wimg, int *err, RootStrides rs) {
@@ -273,29 +274,44 @@ g0_kernel(const G0Tile *__restrict__ tiles, const G0Col *__restrict__ coltab,
 
 } // namespace
 
+template <uint32_t kRingBytes, uint32_t kTmemCols, int kMinBlocks>
+static cudaError_t launch_g0_class(const G0Tile *tiles, int64_t n, const DevicePlan &p,
+                                   const unsigned char *aimg, const float *psi_packed,
+                                   unsigned char *wimg, int *err, const RootStrides &rs, cudaStream_t s) {
+    if (n == 0)
+        return cudaSuccess;
+    constexpr uint32_t smem = kRingBytes + 1024;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(g0_kernel<kRingBytes, kTmemCols, kMinBlocks>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        attr_set = true;
+    }
+    g0_kernel<kRingBytes, kTmemCols, kMinBlocks><<<dim3((unsigned)n, rs.nroots), kThreads, smem, s>>>(
+        tiles, p.g0col, aimg, psi_packed, wimg, err, rs);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const double *psi,
                       float *psi_packed, unsigned char *wimg, int *err, const RootStrides &rs,
                       cudaStream_t s) {
     if (p.n_g0tile == 0)
         return cudaSuccess;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(g0_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmemBytes);
-        if (e != cudaSuccess)
-            return e;
-        attr_set = true;
-    }
     g0_pack_psi<<<dim3((unsigned)p.n_g0psi, rs.nroots), 256, 0, s>>>(p.g0psi, psi, psi_packed, rs,
                                                                     p.g0_psi_floats);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
     RootStrides rp = rs;
-    rp.psi = p.g0_psi_floats;  // the kernel reads the packed copy
-    g0_kernel<<<dim3((unsigned)p.n_g0tile, rs.nroots), kThreads, kSmemBytes, s>>>(
-        p.g0tile, p.g0col, aimg, psi_packed, wimg, err, rp);
-    return cudaGetLastError();
+    rp.psi = p.g0_psi_floats;  // the kernels read the packed copy
+    // tiles [0, n_g0wide) are wider than 128 columns, the rest are not
+    if ((e = launch_g0_class<kWideRing, 256, 2>(p.g0tile, p.n_g0wide, p, aimg, psi_packed, wimg, err,
+                                                rp, s)) != cudaSuccess)
+        return e;
+    return launch_g0_class<kNarrowRing, 128, 3>(p.g0tile + p.n_g0wide, p.n_g0tile - p.n_g0wide, p, aimg,
+                                                psi_packed, wimg, err, rp, s);
 }
 
 } // namespace b2g
