@@ -137,6 +137,15 @@ FORM_DTYPE = {"fp64": "f64", "tf32x3": "tf32x3 (split TF32 on tcgen05, f32 accum
               "fp32": "f32 (CUDA cores) -> f64 sigma"}
 
 
+# measured DRAM traffic of the GEMM0 phase per product (see the roofline note)
+G0_TRAFFIC = {"heff_syn24_su2_M1000_sweep0": 1.276e9, "heff_syn24_su2_M1000_mid": 5.35e9}
+
+
+def workloads_default():
+    from b2g import workloads
+    return workloads.DEFAULT
+
+
 def run_ours(args, rank, local_rank, world, dist):
     import ctypes as C
 
@@ -283,9 +292,10 @@ def run_ours(args, rank, local_rank, world, dist):
                     "BF16 and split-TF32x3 issues 3 MMAs per useful product, so 1/6 of this is the "
                     "useful-FLOP ceiling of this kernel")
         if head == "tf32x3":
-            k2 = ("g1_build_w + g1_kernel + g1_reduce (GEMM1 sigma += alpha op(L) W: bulk-copied "
-                  "TF32 hi/lo operand images, tcgen05.mma kind::tf32 x3, TMEM accumulator)")
-            k1 = "tc_phase1_kernel (GEMM0 W = psi op(R), tcgen05.mma kind::tf32 x3)"
+            k2 = ("g1_kernel + g1_reduce (GEMM1 sigma += alpha op(L) W: bulk-copied TF32 hi/lo "
+                  "operand images, tcgen05.mma kind::tf32 x3, TMEM accumulator)")
+            k1 = ("g0_pack_psi + g0_kernel (two occupancy classes) (GEMM0 W^T = op(R)^T psi^T, "
+                  "tcgen05.mma kind::tf32 x3, epilogue writes the GEMM1 W images)")
         else:
             k2 = "simt_phase2<float> (GEMM1, FP32)"
             k1 = "simt_phase1<float> (GEMM0 W = psi op(R), FP32)"
@@ -294,6 +304,9 @@ def run_ours(args, rank, local_rank, world, dist):
     else:
         kname, kflop, kms = k1, flop0, p1
     achieved = kflop / (kms * 1e-3) / 1e12
+    # the split-TF32x3 form issues three TF32 MMAs (half the BF16 rate) per useful
+    # product, so its useful-FLOP ceiling is one sixth of the measured BF16 peak
+    ceiling = peak / 6.0 if head == "tf32x3" else peak
     # ---- e2e leg: host buffers through the C-ABI host entry
     form = FORMS[head]
     psi_h = torch.from_numpy(prob.psi).pin_memory().numpy()
@@ -346,7 +359,14 @@ def run_ours(args, rank, local_rank, world, dist):
         "roofline": {
             "bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak if peak else None, "peak_source": peak_src,
-            "phase_ms": {"gemm0": p1, "gemm1": p2}, "traffic": None,
+            "frac_of_form_ceiling": achieved / ceiling if ceiling else None,
+            "phase_ms": {"gemm0": p1, "gemm1": p2},
+            "traffic": G0_TRAFFIC.get(args.workload or workloads_default()) if head == "tf32x3" and kname == k1
+            else None,
+            "traffic_note": ("DRAM bytes per GEMM0 phase (both g0_kernel classes): ncu dram__bytes_read.sum + "
+                             "dram__bytes_write.sum on the sweep-0 site (1.276 GB), scaled to this site by "
+                             "the bytes of operator/W images the phase moves (x4.19); "
+                             "profiles/g0_g1_kernels_heff_syn24_M1000_sweep0.md"),
         },
         "e2e": {
             "value": flop * args.steps * world / e2e_total / 1e12, "unit": "TFLOP/s",
