@@ -307,6 +307,18 @@ def run_ours(args, rank, local_rank, world, dist):
     # the split-TF32x3 form issues three TF32 MMAs (half the BF16 rate) per useful
     # product, so its useful-FLOP ceiling is one sixth of the measured BF16 peak
     ceiling = peak / 6.0 if head == "tf32x3" else peak
+    # ---- diag(H_eff) from the recorded pairs (once per site in a sweep)
+    if not args.headline_only:
+        dd = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+        heff.diag(dd)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        heff.diag(dd)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_form["diag_ms"] = e0.elapsed_time(e1)
+        del dd
     # ---- e2e leg: host buffers through the C-ABI host entry
     form = FORMS[head]
     psi_h = torch.from_numpy(prob.psi).pin_memory().numpy()

@@ -93,6 +93,8 @@ SIGNATURES = {
     "b2g_heff_apply_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
     "b2g_heff_apply_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                        C.c_int]),
+    "b2g_heff_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "b2g_heff_diag_host": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),
     "b2g_heff_set_timing": (C.c_int, [C.c_void_p, C.c_int]),

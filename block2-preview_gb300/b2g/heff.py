@@ -113,6 +113,19 @@ class EffectiveHamiltonian:
         check(lib().b2g_heff_apply_batch(self._h, _ptr(b), _ptr(c), int(b.shape[0]), scale, form))
         return c
 
+    # diag(H_eff): the reference builds it in the EffectiveHamiltonian ctor
+    # (effective_hamiltonian.hpp:190-200); here it follows from the recorded pairs
+    def diag(self, out=None):
+        """diag(H_eff) as a float64 numpy array (out=None) or into the CUDA tensor out."""
+        if out is None:
+            d = np.zeros(self.sigma_size)
+            check(lib().b2g_heff_diag_host(self._h, d.ctypes.data))
+            return d
+        if not (out.is_cuda and out.is_contiguous()) or out.numel() != self.sigma_size:
+            raise ValueError("out must be a contiguous CUDA tensor of sigma_size doubles")
+        check(lib().b2g_heff_diag(self._h, _ptr(out)))
+        return out
+
     def status(self):
         """Synchronize and raise if a tensor-core kernel gave up a bounded wait."""
         check(lib().b2g_heff_status(self._h))

@@ -1,5 +1,6 @@
 // C ABI entry points (declared in include/b2g.h): context, H_eff plan
 // creation/upload, H_eff*psi in the FP64 and tensor-core forms.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -35,7 +36,7 @@ static void free_plan(DevicePlan &p) {
     cudaFree(p.t1), cudaFree(p.t2), cudaFree(p.lists);
     cudaFree(p.t2multi), cudaFree(p.g0tile), cudaFree(p.g0col);
     cudaFree(p.g1tile), cudaFree(p.g1stage), cudaFree(p.g1task), cudaFree(p.g1aimg);
-    cudaFree(p.g1red), cudaFree(p.g1cover);
+    cudaFree(p.g1red), cudaFree(p.g1cover), cudaFree(p.region_cb);
     p = DevicePlan();
 }
 
@@ -202,12 +203,14 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
         (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
         (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
         (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
-        (rc = upload(hp.g0psi, &p.g0psi, s)))
+        (rc = upload(hp.g0psi, &p.g0psi, s)) || (rc = upload(hp.region_cb, &p.region_cb, s)))
         return bail(rc);
     p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
     p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
     p.n_g0psi = (int64_t)hp.g0psi.size(), p.g0_psi_floats = hp.g0_psi_floats;
     p.n_g0wide = hp.g0_wide;
+    for (const Region &r : hp.regions)
+        p.max_region_cells = std::max<int64_t>(p.max_region_cells, (int64_t)r.rows * r.cols);
     p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
     p.n_t2multi = (int64_t)hp.t2multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
@@ -262,6 +265,38 @@ int b2g_heff_destroy(b2g_heff *h) {
             cudaEventDestroy(e);
     delete h;
     return B2G_OK;
+}
+
+int b2g_heff_diag(b2g_heff *h, double *diag) {
+    if (h == nullptr || (h->sigma_size && diag == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_diag: null argument");
+    if (h->psi_size != h->sigma_size)
+        return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_diag: bra and ket spaces differ");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    cudaStream_t s = h->ctx->stream;
+    B2G_CUDA_TRY(cudaMemsetAsync(diag, 0, sizeof(double) * h->sigma_size, s));
+    B2G_CUDA_TRY(launch_diag(h->plan, h->ops, diag, s));
+    return B2G_OK;
+}
+
+int b2g_heff_diag_host(b2g_heff *h, double *diag) {
+    if (h == nullptr || (h->sigma_size && diag == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_diag_host: null argument");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    double *d = nullptr;
+    if (h->sigma_size && cudaMalloc(&d, sizeof(double) * h->sigma_size) != cudaSuccess)
+        return fail(B2G_ERR_NOMEM, "b2g_heff_diag_host: cudaMalloc failed");
+    int rc = b2g_heff_diag(h, d);
+    if (rc == B2G_OK && h->sigma_size) {
+        cudaError_t e = cudaMemcpyAsync(diag, d, sizeof(double) * h->sigma_size, cudaMemcpyDeviceToHost,
+                                        h->ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(h->ctx->stream);
+        if (e != cudaSuccess)
+            rc = fail(B2G_ERR_CUDA, std::string("b2g_heff_diag_host: ") + cudaGetErrorString(e));
+    }
+    cudaFree(d);
+    return rc;
 }
 
 int b2g_heff_set_timing(b2g_heff *h, int enable) {

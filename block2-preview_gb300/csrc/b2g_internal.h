@@ -156,6 +156,7 @@ struct HostPlan {
     std::vector<WorkDesc> works;
     std::vector<Contrib> contribs;
     std::vector<Region> regions;
+    std::vector<int64_t> region_cb;  // contributions of region g: [region_cb[g], region_cb[g + 1])
     std::vector<Task1> t1;
     std::vector<Task2> t2;
     std::vector<Tile2> t2multi;
@@ -183,6 +184,8 @@ struct DevicePlan {
     WorkDesc *works = nullptr;
     Contrib *contribs = nullptr;
     Region *regions = nullptr;
+    int64_t *region_cb = nullptr;
+    int64_t max_region_cells = 0;
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;
     Tile2 *t2multi = nullptr;
@@ -225,6 +228,9 @@ cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned 
 cudaError_t launch_g1(const DevicePlan &p, const unsigned char *aimg, const unsigned char *wimg,
                       float *part, double *sigma, double scale, int *err, const RootStrides &rs,
                       cudaStream_t s);
+
+// diag(H_eff) from the recorded pairs (b2g_diag.cu), FP64, device output
+cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cudaStream_t s);
 
 // CUDA-core launchers (b2g_simt.cu), T = double (FP64 form) or float (FP32 form)
 template <typename T>

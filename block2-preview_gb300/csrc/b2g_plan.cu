@@ -186,6 +186,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         }
         rg.rows = rows, rg.cols = cols;
         plan.regions.push_back(rg);
+        plan.region_cb.push_back((int64_t)c_begin);
         const int32_t nrb = (rows + kRowsPerTask - 1) / kRowsPerTask;
         const int32_t ncs = (cols + kColsPerTask - 1) / kColsPerTask;
         std::vector<std::vector<int32_t>> tl((size_t)nrb * ncs);
@@ -295,6 +296,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             }
         }
     }
+    plan.region_cb.push_back((int64_t)plan.contribs.size());
     // ---- image-fed GEMM1: A images (one per distinct operator block and
     // coefficient), W image offsets, stage byte offsets, split-K chunks
     {

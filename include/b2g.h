@@ -136,6 +136,19 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
                          int form);
 
 /*
+ * diag(H_eff) in FP64 (the Davidson preconditioner), computed on the device
+ * from the recorded pairs: entry x collects, over the pairs whose sigma block
+ * holds x, alpha0 * alpha1 * op(L)[i][k] * op(R)[l][j] for the psi index
+ * y = x.  Replaces the diagonal the reference builds in the EffectiveHamiltonian
+ * constructor (src/dmrg/effective_hamiltonian.hpp:190-200, via
+ * TensorFunctions::tensor_product_diagonal, src/core/tensor_functions.hpp:2027-2183).
+ * diag: sigma_size doubles, a DEVICE pointer (b2g_heff_diag, asynchronous) or a
+ * HOST pointer (b2g_heff_diag_host, synchronous).  Needs psi_size == sigma_size.
+ */
+int b2g_heff_diag(b2g_heff *h, double *diag);
+int b2g_heff_diag_host(b2g_heff *h, double *diag);
+
+/*
  * sigma += scale * H_eff * psi in plain FP64 without allocating anything.
  * No counterpart in the reference: this entry point exists for callers that
  * cannot call cudaMalloc (a program that hands the GPU a fixed memory budget,
