@@ -74,6 +74,17 @@ class DmResultC(C.Structure):
     _fields_ = [("error", C.c_double), ("n_kept", C.c_int32)]
 
 
+class BlockSeqC(C.Structure):
+    _fields_ = [
+        ("n_iadd", C.c_int64), ("ia_m", C.c_void_p), ("ia_n", C.c_void_p), ("ia_conj", C.c_void_p),
+        ("ia_src_blob", C.c_void_p), ("ia_dst", C.c_void_p), ("ia_src", C.c_void_p), ("ia_f", C.c_void_p),
+        ("n_kron", C.c_int64), ("kr_am", C.c_void_p), ("kr_an", C.c_void_p), ("kr_ca", C.c_void_p),
+        ("kr_bm", C.c_void_p), ("kr_bn", C.c_void_p), ("kr_cb", C.c_void_p), ("kr_cn", C.c_void_p),
+        ("kr_ablob", C.c_void_p), ("kr_bblob", C.c_void_p), ("kr_a", C.c_void_p), ("kr_b", C.c_void_p),
+        ("kr_c", C.c_void_p), ("kr_f", C.c_void_p),
+    ]
+
+
 # every symbol declared in include/b2g.h, with its ctypes signature
 SIGNATURES = {
     "b2g_version": (C.c_int, []),
@@ -94,6 +105,8 @@ SIGNATURES = {
     "b2g_heff_apply_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                        C.c_int]),
     "b2g_heff_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "b2g_block_contract": (C.c_int, [C.c_void_p, C.POINTER(BlockSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
+                                     C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64]),
     "b2g_heff_diag_host": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),

@@ -149,6 +149,37 @@ int b2g_heff_diag(b2g_heff *h, double *diag);
 int b2g_heff_diag_host(b2g_heff *h, double *diag);
 
 /*
+ * Environment blocking: the operators of the enlarged block, built from the
+ * environment operators and the site operators by the reference's
+ * TensorFunctions::left_contract / right_contract
+ * (src/core/tensor_functions.hpp:2842-2986), given as block-level records:
+ *   iadd  (OperatorFunctions::iadd, src/core/operator_functions.hpp:135-170):
+ *         tmp[dst](m x n) += f * op(blob_src[src])      (op = transpose if conj;
+ *         blob 0 = env, 1 = site)
+ *   kron  (OperatorFunctions::tensor_product, operator_functions.hpp:672-710,
+ *         GMatrixFunctions::tensor_product, src/core/matrix_functions.hpp:1269):
+ *         out[c + (i bm' + k) cn + j bn' + l] += f * A'(i,j) * B'(k,l),
+ *         A' = op(blob_a[a]) (am x an stored, transposed if ca), B' likewise,
+ *         blobs 0 = env, 1 = site, 2 = the iadd intermediates.
+ * out (out_size doubles) is overwritten with the sum of the kron records; all
+ * iadd records are applied before any kron record.  Host buffers; FP64.
+ */
+typedef struct {
+    int64_t n_iadd;
+    const int32_t *ia_m, *ia_n, *ia_conj, *ia_src_blob;
+    const uint64_t *ia_dst, *ia_src;
+    const double *ia_f;
+    int64_t n_kron;
+    const int32_t *kr_am, *kr_an, *kr_ca, *kr_bm, *kr_bn, *kr_cb, *kr_cn, *kr_ablob, *kr_bblob;
+    const uint64_t *kr_a, *kr_b, *kr_c;
+    const double *kr_f;
+} b2g_block_seq;
+
+int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
+                       uint64_t env_size, const double *site, uint64_t site_size,
+                       uint64_t tmp_size, double *out, uint64_t out_size);
+
+/*
  * sigma += scale * H_eff * psi in plain FP64 without allocating anything.
  * No counterpart in the reference: this entry point exists for callers that
  * cannot call cudaMalloc (a program that hands the GPU a fixed memory budget,

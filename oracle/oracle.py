@@ -165,3 +165,37 @@ def dm_truncate(trace_right, psi_dm, psi_rows, psi_cols, psi_off, dm_dim, psi, k
     nrm = np.sqrt(sum(float((x * x).sum()) for x in wfns if x is not None))
     wfns = [None if x is None else x / nrm for x in wfns]
     return eigs, kept, rots, wfns, error
+
+
+def block_contract(rec, env, site, tmp_size, out_size):
+    """Environment blocking replayed from block-level records (the checker of
+    b2g_block_contract): iadd records (OperatorFunctions::iadd,
+    src/core/operator_functions.hpp:135-170) then Kronecker records
+    (GMatrixFunctions::tensor_product, src/core/matrix_functions.hpp:1269-1400),
+    in recorded order."""
+    tmp = np.zeros(int(tmp_size))
+    out = np.zeros(int(out_size))
+    blobs = [np.asarray(env, dtype=np.float64), np.asarray(site, dtype=np.float64), tmp]
+    for q in range(len(rec["ia_m"])):
+        m, n = int(rec["ia_m"][q]), int(rec["ia_n"][q])
+        src = blobs[int(rec["ia_src_blob"][q])]
+        so, do = int(rec["ia_src"][q]), int(rec["ia_dst"][q])
+        if rec["ia_conj"][q]:
+            b = src[so:so + m * n].reshape(n, m).T
+        else:
+            b = src[so:so + m * n].reshape(m, n)
+        tmp[do:do + m * n] += float(rec["ia_f"][q]) * b.ravel()
+    for q in range(len(rec["kr_am"])):
+        am, an, bm, bn = (int(rec[k][q]) for k in ("kr_am", "kr_an", "kr_bm", "kr_bn"))
+        A = blobs[int(rec["kr_ablob"][q])][int(rec["kr_a"][q]):][:am * an].reshape(am, an)
+        B = blobs[int(rec["kr_bblob"][q])][int(rec["kr_b"][q]):][:bm * bn].reshape(bm, bn)
+        if rec["kr_ca"][q]:
+            A = A.T
+        if rec["kr_cb"][q]:
+            B = B.T
+        K = float(rec["kr_f"][q]) * np.kron(A, B)
+        cn, c = int(rec["kr_cn"][q]), int(rec["kr_c"][q])
+        rows, cols = K.shape
+        for r in range(rows):
+            out[c + r * cn:c + r * cn + cols] += K[r]
+    return out

@@ -24,6 +24,7 @@
 #include "block2_core.hpp"
 #include "block2_dmrg.hpp"
 #include <sys/stat.h>
+#include <mutex>
 
 using namespace block2;
 
@@ -347,7 +348,8 @@ template <typename S> struct Dumper : CallbackKernel {
     }
     // the next operator rotation after a dumped site is recorded too
     mutable bool want_rotation = false;
-    mutable string rot_dir;
+    mutable bool want_blocking = false;  // the next left/right_contract is recorded
+    mutable string rot_dir, blk_dir;
     void compute(const string &name, int iprint) const override {
         if (d == nullptr || d->current_eff_ham == nullptr || !selected())
             return;
@@ -356,8 +358,154 @@ template <typename S> struct Dumper : CallbackKernel {
         else if (name == "DMRG::sweep::iter.eff_ham.end") {
             dump_post(d->current_eff_ham);
             want_rotation = true;
+            want_blocking = true;
             rot_dir = site_dir() + "/rotation";
+            blk_dir = site_dir() + "/blocking";
         }
+    }
+};
+
+// Blocking recorder.  TensorFunctions::left_contract / right_contract
+// (src/core/tensor_functions.hpp:2842-2986) run unchanged; while one is being
+// recorded, the OperatorFunctions calls they make are logged at block level,
+// restating the block loops of OperatorFunctions::iadd
+// (src/core/operator_functions.hpp:135-170: a_blk = a_blk + f op(b_blk)) and
+// OperatorFunctions::tensor_product (operator_functions.hpp:672-710, through
+// GMatrixFunctions::tensor_product, src/core/matrix_functions.hpp:1269-1400:
+// c[stride + (i bm' + k) c.n + j bn' + l] += f A'(i,j) B'(k,l), A' = op(a_blk),
+// B' = op(b_blk)).  Operands live in four blobs: the enlarged block's inputs
+// (env ops and site ops), intermediates (sums built by iadd) and the outputs.
+struct BlockRecorder {
+    std::mutex mu;
+    map<const double *, pair<int, size_t>> where;  // data pointer -> (blob, offset)
+    vector<double> env, site;
+    size_t tmp_size = 0;
+    map<const double *, size_t> tmp_open;          // live intermediates
+    map<const double *, size_t> out_off;           // output matrices (packed after)
+    // records
+    vector<int32_t> ia_m, ia_n, ia_conj;           // iadd: dst block m x n, src transposed
+    vector<uint64_t> ia_dst, ia_src;
+    vector<int32_t> ia_src_blob;
+    vector<double> ia_f;
+    vector<int32_t> kr_am, kr_an, kr_ca, kr_bm, kr_bn, kr_cb, kr_cn, kr_ablob, kr_bblob;
+    vector<uint64_t> kr_a, kr_b, kr_c;
+    vector<double> kr_f;
+    size_t out_size = 0;
+    vector<pair<const double *, size_t>> out_list;  // (data, total_memory) in order
+    size_t pack(vector<double> &blob, const double *p, size_t n) {
+        size_t o = blob.size();
+        blob.insert(blob.end(), p, p + n);
+        return o;
+    }
+    // where an operand's data lives (an intermediate is opened by its first iadd)
+    pair<int, size_t> locate(const double *p) {
+        auto it = where.find(p);
+        if (it != where.end())
+            return it->second;
+        auto t = tmp_open.find(p);
+        if (t != tmp_open.end())
+            return make_pair(2, t->second);
+        return make_pair(-1, (size_t)0);
+    }
+};
+static BlockRecorder *g_blk = nullptr;  // set while a contraction is recorded
+
+template <typename S> struct RecordingOpf : OperatorFunctions<S, double> {
+    typedef OperatorFunctions<S, double> OPF;
+    explicit RecordingOpf(const shared_ptr<CG<S>> &cg) : OPF(cg) {}
+    shared_ptr<OPF> copy() const override {
+        shared_ptr<OPF> p = make_shared<RecordingOpf>(this->cg);
+        p->seq = this->seq->copy();
+        return p;
+    }
+    void iadd(const shared_ptr<SparseMatrix<S, double>> &a, const shared_ptr<SparseMatrix<S, double>> &b,
+              double scale = 1.0, bool conj = false) const override {
+        BlockRecorder *R = g_blk;
+        if (R != nullptr && abs(b->factor * scale) >= TINY) {
+            lock_guard<std::mutex> lk(R->mu);
+            if (a->factor != 1.0)
+                throw runtime_error("blocking recorder: iadd into a scaled matrix");
+            // the destination is an intermediate: open it at its first use
+            size_t dst_base;
+            auto t = R->tmp_open.find(a->data);
+            if (t == R->tmp_open.end()) {
+                dst_base = R->tmp_size;
+                R->tmp_open[a->data] = dst_base;
+                R->tmp_size += a->total_memory;
+            } else
+                dst_base = t->second;
+            pair<int, size_t> src = R->locate(b->data);
+            if (src.first < 0)
+                throw runtime_error("blocking recorder: iadd source not found");
+            S bdq = b->info->delta_quantum;
+            for (int ia = 0, ib; ia < a->info->n; ia++) {
+                S bra = a->info->quanta[ia].get_bra(a->info->delta_quantum);
+                S ket = a->info->quanta[ia].get_ket();
+                S bq = conj ? bdq.combine(ket, bra) : bdq.combine(bra, ket);
+                if (bq == S(S::invalid) || (ib = b->info->find_state(bq)) == -1)
+                    continue;
+                double f = scale * b->factor;
+                if (conj)
+                    f *= this->cg->transpose_cg(bdq, bra, ket);
+                GMatrix<double> ma = (*a)[ia], mb = (*b)[ib];
+                R->ia_m.push_back(ma.m), R->ia_n.push_back(ma.n), R->ia_conj.push_back(conj ? 1 : 0);
+                R->ia_dst.push_back(dst_base + (ma.data - a->data));
+                R->ia_src_blob.push_back(src.first);
+                R->ia_src.push_back(src.second + (mb.data - b->data));
+                R->ia_f.push_back(f);
+            }
+        }
+        OPF::iadd(a, b, scale, conj);
+    }
+    void tensor_product(uint8_t conj, const shared_ptr<SparseMatrix<S, double>> &a,
+                        const shared_ptr<SparseMatrix<S, double>> &b,
+                        const shared_ptr<SparseMatrix<S, double>> &c, double scale = 1.0) const override {
+        BlockRecorder *R = g_blk;
+        if (R != nullptr) {
+            lock_guard<std::mutex> lk(R->mu);
+            const double sc = scale * a->factor * b->factor;
+            if (abs(sc) >= TINY && a->data != nullptr && b->data != nullptr && c->data != nullptr) {
+                if (c->factor != 1.0)
+                    throw runtime_error("blocking recorder: scaled output");
+                pair<int, size_t> la = R->locate(a->data), lb = R->locate(b->data);
+                if (la.first < 0 || lb.first < 0)
+                    throw runtime_error("blocking recorder: operand not found");
+                auto oc = R->out_off.find(c->data);
+                size_t cbase;
+                if (oc == R->out_off.end()) {
+                    cbase = R->out_size;
+                    R->out_off[c->data] = cbase;
+                    R->out_size += c->total_memory;
+                    R->out_list.push_back(make_pair((const double *)c->data, (size_t)c->total_memory));
+                } else
+                    cbase = oc->second;
+                S adq = a->info->delta_quantum, bdq = b->info->delta_quantum, cdq = c->info->delta_quantum;
+                auto cinfo = c->info->cinfo;
+                S abdq = cdq.combine((conj & 1) ? -adq : adq, (conj & 2) ? bdq : -bdq);
+                int ik = (int)(lower_bound(cinfo->quanta + cinfo->n[conj], cinfo->quanta + cinfo->n[conj + 1],
+                                           abdq) - cinfo->quanta);
+                int ixa = cinfo->idx[ik];
+                int ixb = ik == cinfo->n[4] - 1 ? cinfo->nc : cinfo->idx[ik + 1];
+                for (int il = ixa; il < ixb; il++) {
+                    int ia = cinfo->ia[il], ib = cinfo->ib[il], ic = cinfo->ic[il];
+                    GMatrix<double> ma = (*a)[ia], mb = (*b)[ib], mc = (*c)[ic];
+                    R->kr_am.push_back(ma.m), R->kr_an.push_back(ma.n), R->kr_ca.push_back(conj & 1);
+                    R->kr_bm.push_back(mb.m), R->kr_bn.push_back(mb.n), R->kr_cb.push_back((conj & 2) >> 1);
+                    R->kr_cn.push_back(mc.n);
+                    R->kr_ablob.push_back(la.first), R->kr_bblob.push_back(lb.first);
+                    R->kr_a.push_back(la.second + (ma.data - a->data));
+                    R->kr_b.push_back(lb.second + (mb.data - b->data));
+                    R->kr_c.push_back(cbase + (mc.data - c->data) + cinfo->stride[il]);
+                    R->kr_f.push_back(sc * cinfo->factor[il]);
+                }
+                // an intermediate is consumed by one product; its memory may be reused
+                if (la.first == 2)
+                    R->tmp_open.erase(a->data);
+                if (lb.first == 2)
+                    R->tmp_open.erase(b->data);
+            }
+        }
+        OPF::tensor_product(conj, a, b, c, scale);
     }
 };
 
@@ -377,6 +525,76 @@ template <typename S> struct RecordingTF : TensorFunctions<S, double> {
         : TF(opf), dumper(dp) {}
     shared_ptr<TF> copy() const override {
         return make_shared<RecordingTF>(this->opf->copy(), dumper);
+    }
+    void left_contract(const shared_ptr<OperatorTensor<S, double>> &a,
+                       const shared_ptr<OperatorTensor<S, double>> &b,
+                       shared_ptr<OperatorTensor<S, double>> &c,
+                       const shared_ptr<Symbolic<S>> &cexprs = nullptr,
+                       OpNamesSet delayed = OpNamesSet()) const override {
+        if (!begin_blocking(a, b))
+            return TF::left_contract(a, b, c, cexprs, delayed);
+        TF::left_contract(a, b, c, cexprs, delayed);
+        end_blocking(false);
+    }
+    void right_contract(const shared_ptr<OperatorTensor<S, double>> &a,
+                        const shared_ptr<OperatorTensor<S, double>> &b,
+                        shared_ptr<OperatorTensor<S, double>> &c,
+                        const shared_ptr<Symbolic<S>> &cexprs = nullptr,
+                        OpNamesSet delayed = OpNamesSet()) const override {
+        if (!begin_blocking(a, b))
+            return TF::right_contract(a, b, c, cexprs, delayed);
+        TF::right_contract(a, b, c, cexprs, delayed);
+        end_blocking(true);
+    }
+    mutable shared_ptr<BlockRecorder> blk;
+    bool begin_blocking(const shared_ptr<OperatorTensor<S, double>> &a,
+                        const shared_ptr<OperatorTensor<S, double>> &b) const {
+        if (dumper == nullptr || !dumper->want_blocking || a == nullptr)
+            return false;
+        dumper->want_blocking = false;
+        blk = make_shared<BlockRecorder>();
+        for (auto &p : a->ops)
+            if (p.second->data != nullptr && blk->where.count(p.second->data) == 0)
+                blk->where[p.second->data] =
+                    make_pair(0, blk->pack(blk->env, p.second->data, p.second->total_memory));
+        for (auto &p : b->ops)
+            if (p.second->data != nullptr && blk->where.count(p.second->data) == 0)
+                blk->where[p.second->data] =
+                    make_pair(1, blk->pack(blk->site, p.second->data, p.second->total_memory));
+        g_blk = blk.get();
+        return true;
+    }
+    void end_blocking(bool right) const {
+        g_blk = nullptr;
+        BlockRecorder &R = *blk;
+        if (R.kr_am.empty()) {
+            // nothing contracted here (every operator delayed): wait for the next one
+            dumper->want_blocking = true;
+            blk.reset();
+            return;
+        }
+        vector<double> out(R.out_size, 0.0);
+        size_t pos = 0;
+        for (auto &o : R.out_list) {
+            memcpy(out.data() + pos, o.first, sizeof(double) * o.second);
+            pos += o.second;
+        }
+        Writer w(dumper->blk_dir);
+        w.scalar("right", right);
+        w.scalar("n_iadd", (double)R.ia_m.size());
+        w.scalar("n_kron", (double)R.kr_am.size());
+        w.scalar("tmp_size", (double)R.tmp_size);
+        w.vec("ia_m", R.ia_m, "i4"), w.vec("ia_n", R.ia_n, "i4"), w.vec("ia_conj", R.ia_conj, "i4");
+        w.vec("ia_dst", R.ia_dst, "u8"), w.vec("ia_src", R.ia_src, "u8");
+        w.vec("ia_src_blob", R.ia_src_blob, "i4"), w.vec("ia_f", R.ia_f, "f8");
+        w.vec("kr_am", R.kr_am, "i4"), w.vec("kr_an", R.kr_an, "i4"), w.vec("kr_ca", R.kr_ca, "i4");
+        w.vec("kr_bm", R.kr_bm, "i4"), w.vec("kr_bn", R.kr_bn, "i4"), w.vec("kr_cb", R.kr_cb, "i4");
+        w.vec("kr_cn", R.kr_cn, "i4"), w.vec("kr_ablob", R.kr_ablob, "i4");
+        w.vec("kr_bblob", R.kr_bblob, "i4"), w.vec("kr_a", R.kr_a, "u8"), w.vec("kr_b", R.kr_b, "u8");
+        w.vec("kr_c", R.kr_c, "u8"), w.vec("kr_f", R.kr_f, "f8");
+        w.vec("env", R.env, "f8"), w.vec("site", R.site, "f8"), w.vec("out", out, "f8");
+        w.man.flush();
+        blk.reset();
     }
     void left_rotate(const shared_ptr<OperatorTensor<S, double>> &a,
                      const shared_ptr<SparseMatrix<S, double>> &bra,
@@ -499,7 +717,11 @@ template <typename S> int run(const Opts &o) {
     mps_info->deallocate_mutable();
     auto dumper = make_shared<Dumper<S>>();
     dumper->o = o;
-    mpo->tf = make_shared<RecordingTF<S>>(mpo->tf->opf, dumper.get());
+    {
+        auto ropf = make_shared<RecordingOpf<S>>(mpo->tf->opf->cg);
+        ropf->seq = mpo->tf->opf->seq;
+        mpo->tf = make_shared<RecordingTF<S>>(ropf, dumper.get());
+    }
     auto me = make_shared<MovingEnvironment<S, FL, FL>>(mpo, mps, mps, "DMRG");
     me->init_environments(false);
     me->delayed_contraction = OpNamesSet::normal_ops();

@@ -133,6 +133,19 @@ def run_case(name, args, desc):
         rot.save(rpath)
         print(f"{name}_rot: pairs={rmeta['n_pairs']} in={rot.psi_size} out={rot.sigma_size} "
               f"-> {os.path.getsize(rpath)} bytes")
+    # the environment blocking that followed this site (block-level records)
+    bdir = os.path.join(out, site_dirs[0], "blocking")
+    if os.path.isdir(bdir):
+        ba, bs = read_dump(bdir)
+        bpath = os.path.join(HERE, name + "_blk.npz")
+        np.savez_compressed(
+            bpath, right=np.int32(bs["right"]), tmp_size=np.int64(bs["tmp_size"]), **ba,
+            meta=np.array(json.dumps({"name": name + "_blk", "kind": "blocking",
+                                      "description": "environment blocking ("
+                                      + ("right" if bs["right"] else "left")
+                                      + "_contract) after the site of " + name})))
+        print(f"{name}_blk: iadd={int(bs['n_iadd'])} kron={int(bs['n_kron'])} env={ba['env'].size} "
+              f"site={ba['site'].size} out={ba['out'].size} -> {os.path.getsize(bpath)} bytes")
     # density matrix of the converged psi and the reference's truncation/split
     tdir = os.path.join(out, site_dirs[0], "truncation")
     if os.path.isdir(tdir):
