@@ -1,5 +1,6 @@
 // C ABI entry points (declared in include/b2g.h): context, H_eff plan
-// creation/upload, H_eff*psi in the FP64 and tensor-core forms.
+// creation/upload, H_eff*psi in the FP64, FP32 and TF32x3 (tensor-core)
+// forms for one or several roots, diag(H_eff), timing and the FP64 probe.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>

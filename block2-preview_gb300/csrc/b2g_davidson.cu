@@ -1,11 +1,17 @@
-// Device-resident Davidson eigensolver for the lowest eigenpair of H_eff.
+// Device-resident Davidson eigensolver for the lowest eigenpair(s) of H_eff.
 //
-// Restates IterativeMatrixFunctions::davidson for one root, Normal type,
-// Olsen preconditioner (src/core/iterative_matrix_functions.hpp:864-1173,
-// 93-108) with the same basis growth, convergence test (|r|^2 < conv_thrd),
-// restart to def_min vectors when def_max is reached, and orthogonalisation
-// of the correction vector.  Arithmetic differences from the reference,
-// all exact in exact arithmetic:
+// Restates IterativeMatrixFunctions::davidson, Normal type, Olsen
+// preconditioner (src/core/iterative_matrix_functions.hpp:864-1173, 93-108)
+// with the same basis growth, convergence test (|r|^2 < conv_thrd), restart
+// to def_min vectors when def_max is reached, and orthogonalisation of the
+// correction vectors.  One root (b2g_davidson) or k state-averaged roots
+// (b2g_davidson_multi): the block variant adds the corrections of all
+// unconverged roots per iteration and applies H_eff to them in one
+// b2g_heff_apply_batch call.  In a reduced-precision form (FP32, TF32x3) the
+// products are reduced-precision and convergence is only declared on an FP64
+// residual of the Ritz vector (defect correction; the energy returned is the
+// FP64 Rayleigh quotient).  Arithmetic differences from the reference, all
+// exact in exact arithmetic:
 //   * the basis is not rotated to Ritz vectors every iteration; the Ritz
 //     vector x = B v and its H-image s = Sigma v are formed directly and the
 //     subspace matrix grows by one row per new vector (the reference rotates
@@ -15,8 +21,8 @@
 //     solved on the device by parallel cyclic Jacobi (one CTA, FP64);
 //   * the correction vector is orthogonalised by classical Gram-Schmidt
 //     applied twice (the reference applies modified Gram-Schmidt once).
-// All vectors live in HBM; per iteration only (lambda, |r|^2) come back to
-// the host for the convergence decision.  Reductions are two-stage
+// All vectors live in HBM; per iteration only the Ritz values and residual
+// norms come back to the host for the convergence decision.  Reductions are two-stage
 // (per-block partials, then a fixed-order sum): results are bit-reproducible.
 #include <algorithm>
 #include <cmath>

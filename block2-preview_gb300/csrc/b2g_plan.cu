@@ -13,6 +13,10 @@
 //   * sigma is cut into disjoint regions and tasks, each task owns its cells,
 //     so no atomics, no sigma copies and no reduction are needed, and the
 //     summation order is fixed (bit-reproducible run to run).
+// For the tensor-core form it also lays out the operand images: GEMM0 tiles
+// (products sharing a right operator, stacked psi rows, transposed), GEMM1
+// tiles per sigma rectangle with one stage per 16-row K slab of each
+// contribution, split-K chunks, and the cover lists of the reduction.
 #include <algorithm>
 #include <array>
 #include <map>
