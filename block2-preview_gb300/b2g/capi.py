@@ -100,6 +100,7 @@ SIGNATURES = {
     "b2g_heff_stats_get": (C.c_int, [C.c_void_p, C.POINTER(HeffStatsC)]),
     "b2g_plan_stats": (C.c_int, [C.POINTER(PairSeqC), C.c_uint64, C.c_uint64, C.c_uint64,
                                  C.POINTER(HeffStatsC)]),
+    "b2g_partition_pairs": (C.c_int, [C.POINTER(PairSeqC), C.c_int, C.c_void_p, C.c_void_p]),
     "b2g_heff_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
     "b2g_heff_apply_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
     "b2g_heff_apply_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
@@ -188,6 +189,11 @@ class PairSeq:
         for k in PAIR_U64_FIELDS:
             setattr(s, k, self.arrays[k].ctypes.data_as(_u64p))
         self.c = s
+
+    def subset(self, idx) -> "PairSeq":
+        """The pairs at positions idx (in that order) as a new sequence."""
+        idx = np.asarray(idx, dtype=np.int64)
+        return PairSeq({k: v[idx] for k, v in self.arrays.items()})
 
     def mnk(self) -> float:
         a = self.arrays

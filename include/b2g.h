@@ -120,6 +120,17 @@ int b2g_heff_status(b2g_heff *h);
  * sequence against the sizes and reports the schedule statistics. */
 int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size,
                    uint64_t sigma_size, b2g_heff_stats *out);
+/* Host-only term partition of one H_eff over n_ranks ranks.  Replaces the
+ * reference's term distribution (ParallelRuleQC, src/dmrg/qc_parallel_rule.hpp:31-85)
+ * whose partial sigmas ParallelTensorFunctions::operator() sums with
+ * allreduce_sum (src/core/parallel_tensor_functions.hpp:51-55).  Pairs sharing
+ * a GEMM0 product stay on one rank; products go largest first to the
+ * least-loaded rank (ties: lower rank, earlier product), so every rank derives
+ * the same partition.  rank_of_pair[i] receives the rank of pair i; load
+ * (optional, n_ranks doubles) the multiply-adds each rank executes.  Each rank
+ * builds b2g_heff_create from its own pairs and sums sigma across ranks. */
+int b2g_partition_pairs(const b2g_pair_seq *seq, int n_ranks, int32_t *rank_of_pair,
+                        double *load);
 
 /* sigma += scale * H_eff * psi; psi and sigma are DEVICE pointers (sizes as created),
  * form = B2G_FP64 or B2G_TF32X3.  Asynchronous on the context stream. */

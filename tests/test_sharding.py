@@ -1,0 +1,155 @@
+"""Term-sharded H_eff*psi: the partition (b2g_partition_pairs, host only), the
+sum of the ranks' shares against the reference's sigma, and the collective
+path over world_size-2 gloo ranks on the CPU (each rank replays its share
+with the oracle), as the reference's ParallelTensorFunctions::operator()
+(src/core/parallel_tensor_functions.hpp:51-55) sums sigma with allreduce_sum."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, fixture_ids
+
+import b2g  # noqa: E402
+from b2g.sharding import ShardedEffectiveHamiltonian, partition_pairs, rank_pairs  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+RTOL = 1e-12
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def product_keys(seq):
+    a = seq.arrays
+    return list(zip(a["a0"].tolist(), a["b0"].tolist(), a["m0"].tolist(), a["n0"].tolist(),
+                    a["k0"].tolist(), a["lda0"].tolist(), a["ldb0"].tolist(),
+                    (a["tb0"] != 0).tolist()))
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+@pytest.mark.parametrize("n_ranks", [1, 2, 3, 8])
+def test_partition_keeps_products_together_and_balances(problems, name, n_ranks):
+    seq = problems[name].seq()
+    rank_of, load = partition_pairs(seq, n_ranks)
+    assert rank_of.shape == (seq.n,) and rank_of.min() >= 0 and rank_of.max() < n_ranks
+    owner, cost = {}, {}
+    a = seq.arrays
+    for i, k in enumerate(product_keys(seq)):
+        assert owner.setdefault(k, rank_of[i]) == rank_of[i]
+        if k not in cost:
+            cost[k] = float(a["m0"][i]) * a["n0"][i] * a["k0"][i]
+        cost[k] += float(a["m1"][i]) * a["n1"][i] * a["k1"][i]
+    want = np.zeros(n_ranks)
+    for k, r in owner.items():
+        want[r] += cost[k]
+    np.testing.assert_allclose(load, want, rtol=1e-12)
+    # largest-first greedy: no rank exceeds the mean by more than the largest product
+    assert load.max() <= load.sum() / n_ranks + max(cost.values()) + 1e-6
+    again, _ = partition_pairs(seq, n_ranks)
+    assert np.array_equal(again, rank_of)
+
+
+def test_partition_rejects_bad_arguments(problems):
+    import ctypes as C
+    seq = problems[fixture_ids()[0]].seq()
+    out = np.zeros(seq.n, dtype=np.int32)
+    assert b2g.lib().b2g_partition_pairs(None, 2, out.ctypes.data, None) == 1
+    assert b2g.lib().b2g_partition_pairs(C.byref(seq.c), 0, out.ctypes.data, None) == 1
+    assert b2g.lib().b2g_partition_pairs(C.byref(seq.c), 2, None, None) == 1
+    with pytest.raises(ValueError):
+        partition_pairs(seq, 0)
+    with pytest.raises(ValueError):
+        rank_pairs(seq, 2, 2)
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+@pytest.mark.parametrize("n_ranks", [2, 3])
+def test_sum_of_rank_shares_matches_reference(problems, name, n_ranks):
+    p = problems[name]
+    seq = p.seq()
+    total = np.zeros(p.sigma_size)
+    n = 0
+    for r in range(n_ranks):
+        sub = rank_pairs(seq, n_ranks, r)
+        n += sub.n
+        total += oracle.replay(sub, p.ops, p.psi, p.sigma_size)
+    assert n == seq.n
+    assert rel(total, p.sigma) <= RTOL
+
+
+class OracleShare:
+    """One rank's share replayed on the CPU by the oracle (test stand-in for the GPU engine)."""
+
+    def __init__(self, ctx, seq, ops, psi_size, sigma_size):
+        self.seq, self.ops, self.sigma_size = seq, ops, sigma_size
+
+    def __call__(self, b, c, scale=1.0, form=b2g.FP64):
+        oracle.replay(self.seq, self.ops, b, self.sigma_size, scale, sigma=c)
+        return c
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _gloo_rank(rank, world, port, name, out_dir):
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "block2-preview_gb300"))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    from b2g.problem import load_problem
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        p = load_problem(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+        h = ShardedEffectiveHamiltonian(None, p.seq(), p.ops, p.psi_size, p.sigma_size,
+                                        engine=OracleShare)
+        c = np.full(p.sigma_size, 0.25)   # c += scale * H psi keeps what c held
+        h(p.psi, c, scale=0.5)
+        np.save(os.path.join(out_dir, f"sigma{rank}.npy"), c)
+        np.save(os.path.join(out_dir, f"npairs{rank}.npy"), np.array([h.local_seq.n]))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name", ["hub8_su2", "syn8_sz"])
+def test_gloo_two_ranks_sum_sigma(problems, name, tmp_path):
+    mp = pytest.importorskip("torch.multiprocessing")
+    p = problems[name]
+    port = _free_port()
+    mp.start_processes(_gloo_rank, args=(2, port, name, str(tmp_path)), nprocs=2,
+                       start_method="spawn", join=True)
+    want = 0.25 + 0.5 * p.sigma
+    got = [np.load(tmp_path / f"sigma{r}.npy") for r in range(2)]
+    npairs = sum(int(np.load(tmp_path / f"npairs{r}.npy")[0]) for r in range(2))
+    assert npairs == p.seq().n
+    assert np.array_equal(got[0], got[1])
+    assert rel(got[0], want) <= RTOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", fixture_ids())
+def test_gpu_rank_shares_sum_to_reference(problems, name):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    p = problems[name]
+    seq = p.seq()
+    ctx = b2g.Context(0)
+    try:
+        psi = torch.from_numpy(p.psi).cuda()
+        total = torch.zeros(p.sigma_size, dtype=torch.float64, device="cuda")
+        for r in range(2):
+            h = b2g.EffectiveHamiltonian(ctx, rank_pairs(seq, 2, r), p.ops, p.psi_size,
+                                         p.sigma_size)
+            h(psi, total)
+            h.status()
+            h.close()
+        assert rel(total.cpu().numpy(), p.sigma) <= RTOL
+    finally:
+        ctx.close()
