@@ -22,7 +22,47 @@ constexpr int kLanesCols = 8;  // column chunks of 32 per warp (256 columns)
 //   W_u[r, c] = sum_k psi[a0 + r*lda0 + k] * B(k, c),
 //   B(k, c) = ops[b0 + k*ldb0 + c] (tb0 = 0) or ops[b0 + c*ldb0 + k] (tb0 = 1).
 // psi loads are warp-broadcast; B loads are coalesced for tb0 = 0 and
-// L1-served column walks for tb0 = 1.
+// L1-served column walks for tb0 = 1.  A predicated-off FMA still occupies
+// the FP64 pipe for a whole warp instruction, so the number of column chunks
+// (NJ) is a compile-time, warp-uniform count: every issued FMA carries at
+// least one live column.
+template <typename T, int NJ>
+__device__ __forceinline__ void p1_chunk(const T *__restrict__ prow, const T *__restrict__ B,
+                                         const WorkDesc &wd, int cbase, int lane,
+                                         T *__restrict__ wrow) {
+    T acc[NJ];
+    int col[NJ];
+    bool live[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; j++) {
+        acc[j] = T(0);
+        col[j] = cbase + lane + 32 * j;
+        live[j] = col[j] < wd.n0;
+    }
+    if (!wd.tb0) {
+        for (int k = 0; k < wd.k0; k++) {
+            const T a = __ldg(prow + k);
+            const T *brow = B + (uint64_t)k * wd.ldb0;
+#pragma unroll
+            for (int j = 0; j < NJ; j++)
+                if (live[j])
+                    acc[j] = fma(a, __ldg(brow + col[j]), acc[j]);
+        }
+    } else {
+        for (int k = 0; k < wd.k0; k++) {
+            const T a = __ldg(prow + k);
+#pragma unroll
+            for (int j = 0; j < NJ; j++)
+                if (live[j])
+                    acc[j] = fma(a, __ldg(B + (uint64_t)col[j] * wd.ldb0 + k), acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NJ; j++)
+        if (live[j])
+            wrow[col[j]] = acc[j];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ works,
                                                    const Task1 *__restrict__ tasks, int64_t n_tasks,
@@ -41,36 +81,21 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
     const T *B = ops + wd.b0;
     T *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
     for (int cbase = 0; cbase < wd.n0; cbase += 32 * kLanesCols) {
-        T acc[kLanesCols];
-#pragma unroll
-        for (int j = 0; j < kLanesCols; j++)
-            acc[j] = T(0);
-        const int nj = min(kLanesCols, (wd.n0 - cbase + 31) >> 5);
-        if (!wd.tb0) {
-            for (int k = 0; k < wd.k0; k++) {
-                const T a = (T)__ldg(prow + k);
-                const T *brow = B + (uint64_t)k * wd.ldb0 + cbase + lane;
-#pragma unroll
-                for (int j = 0; j < kLanesCols; j++)
-                    if (j < nj && cbase + lane + 32 * j < wd.n0)
-                        acc[j] = fma(a, __ldg(brow + 32 * j), acc[j]);
-            }
-        } else {
-            for (int k = 0; k < wd.k0; k++) {
-                const T a = (T)__ldg(prow + k);
-#pragma unroll
-                for (int j = 0; j < kLanesCols; j++) {
-                    const int c = cbase + lane + 32 * j;
-                    if (j < nj && c < wd.n0)
-                        acc[j] = fma(a, __ldg(B + (uint64_t)c * wd.ldb0 + k), acc[j]);
-                }
-            }
+        if constexpr (sizeof(T) == 4) {
+            // the FP32 pipe is wide: predicated chunks cost little and the
+            // fixed 8-chunk body keeps more loads in flight
+            p1_chunk<T, 8>(prow, B, wd, cbase, lane, wrow);
+            continue;
         }
-#pragma unroll
-        for (int j = 0; j < kLanesCols; j++) {
-            const int c = cbase + lane + 32 * j;
-            if (j < nj && c < wd.n0)
-                wrow[c] = acc[j];
+        switch (min(kLanesCols, (wd.n0 - cbase + 31) >> 5)) {
+        case 1: p1_chunk<T, 1>(prow, B, wd, cbase, lane, wrow); break;
+        case 2: p1_chunk<T, 2>(prow, B, wd, cbase, lane, wrow); break;
+        case 3: p1_chunk<T, 3>(prow, B, wd, cbase, lane, wrow); break;
+        case 4: p1_chunk<T, 4>(prow, B, wd, cbase, lane, wrow); break;
+        case 5: p1_chunk<T, 5>(prow, B, wd, cbase, lane, wrow); break;
+        case 6: p1_chunk<T, 6>(prow, B, wd, cbase, lane, wrow); break;
+        case 7: p1_chunk<T, 7>(prow, B, wd, cbase, lane, wrow); break;
+        default: p1_chunk<T, 8>(prow, B, wd, cbase, lane, wrow); break;
         }
     }
 }
@@ -83,6 +108,63 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
 // sigma += scale * acc directly; otherwise the chunk stores its partial tile
 // and simt_reduce sums the chunks in order.  Only cells inside the region's
 // write span are stored (no atomics, deterministic).
+//
+// Per contribution only the column chunks [J0, J1) that meet its columns are
+// issued (compile-time range picked by a warp-uniform dispatch), the dot
+// products are summed unscaled and alpha is applied once per contribution,
+// so the FP64 pipe issues no FMA without a live column and no per-k multiply.
+template <typename T, int J0, int J1>
+__device__ __forceinline__ void p2_contrib(T (&acc)[kLanesCols], const T *__restrict__ A,
+                                           const T *__restrict__ W, const Contrib &c, int ar,
+                                           int colbase) {
+    constexpr int NJ = J1 - J0;
+    T t[NJ];
+    int col[NJ];
+    bool live[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; j++) {
+        t[j] = T(0);
+        col[j] = colbase + 32 * (J0 + j);
+        live[j] = col[j] >= 0 && col[j] < c.n1;
+    }
+    const uint64_t astep = c.ta1 ? (uint64_t)c.lda1 : 1;
+    const T *ap = A + (c.ta1 ? (uint64_t)ar : (uint64_t)ar * c.lda1);
+    for (int k = 0; k < c.k1; k++) {
+        const T a = __ldg(ap + (uint64_t)k * astep);
+        const T *wrow = W + (uint64_t)k * c.n1;
+#pragma unroll
+        for (int j = 0; j < NJ; j++)
+            if (live[j])
+                t[j] = fma(a, __ldg(wrow + col[j]), t[j]);
+    }
+    const T alpha = (T)c.alpha;
+#pragma unroll
+    for (int j = 0; j < NJ; j++)
+        acc[J0 + j] = fma(alpha, t[j], acc[J0 + j]);
+}
+
+template <typename T, int J0, int J1>
+__device__ __forceinline__ void p2_pick_j1(int j1, T (&acc)[kLanesCols], const T *A, const T *W,
+                                           const Contrib &c, int ar, int colbase) {
+    if constexpr (J1 <= kLanesCols) {
+        if (j1 == J1)
+            p2_contrib<T, J0, J1>(acc, A, W, c, ar, colbase);
+        else
+            p2_pick_j1<T, J0, J1 + 1>(j1, acc, A, W, c, ar, colbase);
+    }
+}
+
+template <typename T, int J0>
+__device__ __forceinline__ void p2_pick(int j0, int j1, T (&acc)[kLanesCols], const T *A,
+                                        const T *W, const Contrib &c, int ar, int colbase) {
+    if constexpr (J0 < kLanesCols) {
+        if (j0 == J0)
+            p2_pick_j1<T, J0, J0 + 1>(j1, acc, A, W, c, ar, colbase);
+        else
+            p2_pick<T, J0 + 1>(j0, j1, acc, A, W, c, ar, colbase);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tasks,
                                                    const int32_t *__restrict__ lists,
@@ -112,24 +194,14 @@ __global__ void __launch_bounds__(128) simt_phase2(const Task2 *__restrict__ tas
         const int ar = r - c.row0;
         if (ar < 0 || ar >= c.m1)
             continue;  // warp-uniform
-        const T *A = ops + c.a1;
-        const T *W = work + works[c.u].woff;
-        int cc[kLanesCols];
-#pragma unroll
-        for (int j = 0; j < kLanesCols; j++) {
-            const int col = tk.col0 + lane + 32 * j - c.col0;
-            cc[j] = (col >= 0 && col < c.n1) ? col : -1;
-        }
-        const T alpha = (T)c.alpha;
-        for (int k = 0; k < c.k1; k++) {
-            const T a = alpha * __ldg(c.ta1 ? A + (uint64_t)k * c.lda1 + ar
-                                            : A + (uint64_t)ar * c.lda1 + k);
-            const T *wrow = W + (uint64_t)k * c.n1;
-#pragma unroll
-            for (int j = 0; j < kLanesCols; j++)
-                if (cc[j] >= 0)
-                    acc[j] = fma(a, __ldg(wrow + cc[j]), acc[j]);
-        }
+        // column chunks of the window [tk.col0, tk.col0 + 256) meeting the
+        // contribution's columns [c.col0, c.col0 + n1)
+        const int lo = c.col0 - tk.col0, hi = lo + c.n1;
+        const int j0 = lo > 0 ? lo >> 5 : 0;
+        const int j1 = min(kLanesCols, (hi + 31) >> 5);
+        if (j1 <= j0)
+            continue;
+        p2_pick<T, 0>(j0, j1, acc, ops + c.a1, work + works[c.u].woff, c, ar, tk.col0 + lane - c.col0);
     }
     if (tk.part >= 0) {
         T *prow = part + ((tk.part + tk.chunk) * 4 + wr) * (int64_t)(32 * kLanesCols);
