@@ -112,6 +112,8 @@ SIGNATURES = {
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),
     "b2g_heff_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "b2g_heff_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "b2g_heff_graph_count": (C.c_int, [C.c_void_p]),
     "b2g_heff_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,

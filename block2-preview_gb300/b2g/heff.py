@@ -126,6 +126,15 @@ class EffectiveHamiltonian:
         check(lib().b2g_heff_diag(self._h, _ptr(out)))
         return out
 
+    def set_graphs(self, enable: bool):
+        """Replay repeated applies as CUDA graphs (default on); False drops them."""
+        check(lib().b2g_heff_set_graphs(self._h, int(bool(enable))))
+
+    @property
+    def graph_count(self) -> int:
+        """Captured apply graphs currently held."""
+        return lib().b2g_heff_graph_count(self._h)
+
     def status(self):
         """Synchronize and raise if a tensor-core kernel gave up a bounded wait."""
         check(lib().b2g_heff_status(self._h))

@@ -41,11 +41,20 @@ static void free_plan(DevicePlan &p) {
     p = DevicePlan();
 }
 
+// drop every captured apply (their buffers are about to move, or the H_eff goes)
+static void clear_graphs(b2g_heff *h) {
+    for (auto &g : h->graphs)
+        if (g.exec)
+            cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
+}
+
 // per-root buffers (work matrices, split-K partials, float psi) for nroots roots
 static int ensure_roots(b2g_heff *h, int nroots) {
     if (nroots <= h->cap_roots)
         return B2G_OK;
     B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+    clear_graphs(h);
     cudaFree(h->work), cudaFree(h->simt_part), cudaFree(h->psi32);
     h->work = nullptr, h->simt_part = nullptr, h->psi32 = nullptr;
     h->cap_roots = 0;
@@ -77,6 +86,7 @@ static int ensure_g1(b2g_heff *h, int nroots) {
     if (nroots <= h->g1_roots)
         return B2G_OK;
     B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+    clear_graphs(h);
     cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
     h->g1_wimg = nullptr, h->g1_part = nullptr, h->g0_psi = nullptr, h->g1_roots = 0;
     const size_t R = (size_t)nroots;
@@ -256,6 +266,7 @@ int b2g_heff_destroy(b2g_heff *h) {
         return B2G_OK;
     cudaSetDevice(h->ctx->device);
     cudaStreamSynchronize(h->ctx->stream);
+    clear_graphs(h);
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
     cudaFree(h->simt_part);
@@ -366,18 +377,34 @@ int b2g_plan_stats(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size
     return B2G_OK;
 }
 
-int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
-                         int form) {
-    if (h == nullptr || nroots < 1 || (h->psi_size && psi == nullptr) ||
-        (h->sigma_size && sigma == nullptr))
-        return fail(B2G_ERR_ARG, "b2g_heff_apply: null argument or nroots < 1");
-    if (nroots > 65535)
-        return fail(B2G_ERR_ARG, "b2g_heff_apply: too many roots");
-    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
-    cudaStream_t s = h->ctx->stream;
+} // extern "C"
+
+namespace b2g {
+
+// buffers and one-time conversions an apply needs (allocations, syncs: never
+// inside a stream capture)
+static int apply_prepare(b2g_heff *h, int nroots, int form) {
     int rc = ensure_roots(h, nroots);
     if (rc != B2G_OK)
         return rc;
+    if (form == B2G_FP32 || form == B2G_TF32X3) {
+        if (h->ops32 == nullptr && h->ops_size) {
+            if (cudaMalloc(&h->ops32, sizeof(float) * h->ops_size) != cudaSuccess) {
+                h->ops32 = nullptr;
+                return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the float operator copy");
+            }
+            B2G_CUDA_TRY(launch_to_float(h->ops, h->ops32, h->ops_size, h->ctx->stream));
+        }
+        if (form == B2G_TF32X3 && (rc = ensure_g1(h, nroots)) != B2G_OK)
+            return rc;
+    }
+    return B2G_OK;
+}
+
+// the kernel launches of one apply (stream-ordered only: capturable)
+static int apply_launches(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
+                          int form) {
+    cudaStream_t s = h->ctx->stream;
     RootStrides rs;
     rs.nroots = nroots, rs.psi = h->psi_size, rs.sigma = h->sigma_size;
     if (form == B2G_FP64) {
@@ -393,43 +420,138 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
             B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
         return B2G_OK;
     }
-    if (form == B2G_FP32 || form == B2G_TF32X3) {
-        if (h->ops32 == nullptr && h->ops_size) {
-            if (cudaMalloc(&h->ops32, sizeof(float) * h->ops_size) != cudaSuccess) {
-                h->ops32 = nullptr;
-                return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the float operator copy");
-            }
-            B2G_CUDA_TRY(launch_to_float(h->ops, h->ops32, h->ops_size, s));
+    float *w32 = (float *)h->work;
+    rs.work = 2 * h->work_size;  // floats per root in a buffer sized in doubles
+    if (h->timing)
+        B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    if (form == B2G_TF32X3) {
+        // psi enters as a packed FP32 copy of its sub-blocks (made by launch_g0)
+        rs.wimg = h->plan.g1_wbytes, rs.part = h->plan.g1_part;
+        B2G_CUDA_TRY(launch_g0(h->plan, h->g1_aimg, psi, h->g0_psi, h->g1_wimg, h->err, rs, s));
+    } else {
+        // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
+        B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
+        B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
+    }
+    if (h->timing)
+        B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    if (form == B2G_TF32X3) {
+        B2G_CUDA_TRY(launch_g1(h->plan, h->g1_aimg, h->g1_wimg, h->g1_part, sigma, scale, h->err, rs, s));
+    } else {
+        rs.part = 2 * h->simt_part_size;
+        B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, (float *)h->simt_part,
+                                               scale, rs, s));
+    }
+    if (h->timing)
+        B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+    return B2G_OK;
+}
+
+// apply through the graph cache: first use of an argument set runs eagerly,
+// the second captures and replays, later ones replay (LRU of kMaxApplyGraphs)
+static int apply_graphed(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
+                         int form) {
+    cudaStream_t s = h->ctx->stream;
+    ApplyGraph *g = nullptr;
+    for (auto &e : h->graphs)
+        if (e.psi == psi && e.sigma == sigma && e.nroots == nroots && e.form == form &&
+            memcmp(&e.scale, &scale, sizeof scale) == 0) {
+            g = &e;
+            break;
         }
-        float *w32 = (float *)h->work;
-        rs.work = 2 * h->work_size;  // floats per root in a buffer sized in doubles
-        if (h->timing)
-            B2G_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-        if (form == B2G_TF32X3) {
-            // psi enters as a packed FP32 copy of its sub-blocks (made by launch_g0)
-            if ((rc = ensure_g1(h, nroots)) != B2G_OK)
-                return rc;
-            rs.wimg = h->plan.g1_wbytes, rs.part = h->plan.g1_part;
-            B2G_CUDA_TRY(launch_g0(h->plan, h->g1_aimg, psi, h->g0_psi, h->g1_wimg, h->err, rs, s));
-        } else {
-            // psi rounded once (FP64 conversions run on the narrow FP64 pipe of GB300)
-            B2G_CUDA_TRY(launch_to_float(psi, h->psi32, h->psi_size * (uint64_t)nroots, s));
-            B2G_CUDA_TRY(launch_simt_phase1<float>(h->plan, h->ops32, h->psi32, w32, rs, s));
+    if (g == nullptr) {
+        if (h->graphs.size() >= kMaxApplyGraphs) {
+            size_t v = 0;
+            for (size_t i = 1; i < h->graphs.size(); i++)
+                if (h->graphs[i].last < h->graphs[v].last)
+                    v = i;
+            if (h->graphs[v].exec)
+                cudaGraphExecDestroy(h->graphs[v].exec);
+            h->graphs.erase(h->graphs.begin() + (ptrdiff_t)v);
         }
-        if (h->timing)
-            B2G_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-        if (form == B2G_TF32X3) {
-            B2G_CUDA_TRY(launch_g1(h->plan, h->g1_aimg, h->g1_wimg, h->g1_part, sigma, scale, h->err, rs, s));
-        } else {
-            rs.part = 2 * h->simt_part_size;
-            B2G_CUDA_TRY(launch_simt_phase2<float>(h->plan, h->ops32, w32, sigma, (float *)h->simt_part,
-                                                   scale, rs, s));
-        }
-        if (h->timing)
-            B2G_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+        ApplyGraph e;
+        e.psi = psi, e.sigma = sigma, e.nroots = nroots, e.form = form, e.scale = scale;
+        e.last = ++h->graph_tick;
+        h->graphs.push_back(e);
+        return apply_launches(h, psi, sigma, nroots, scale, form);
+    }
+    g->last = ++h->graph_tick;
+    if (g->state == 1) {
+        B2G_CUDA_TRY(cudaGraphLaunch(g->exec, s));
         return B2G_OK;
     }
-    return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_apply: unknown form " + std::to_string(form));
+    if (g->state < 0)
+        return apply_launches(h, psi, sigma, nroots, scale, form);
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        g->state = -1;
+        return apply_launches(h, psi, sigma, nroots, scale, form);
+    }
+    const int rc = apply_launches(h, psi, sigma, nroots, scale, form);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    if (rc != B2G_OK) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return rc;
+    }
+    cudaError_t ei = cudaErrorUnknown;
+    if (ec == cudaSuccess && graph != nullptr)
+        ei = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (graph)
+        cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        cudaGetLastError();
+        g->exec = nullptr;
+        g->state = -1;
+        return apply_launches(h, psi, sigma, nroots, scale, form);
+    }
+    g->state = 1;
+    B2G_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+    return B2G_OK;
+}
+
+} // namespace b2g
+
+extern "C" {
+
+int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroots, double scale,
+                         int form) {
+    if (h == nullptr || nroots < 1 || (h->psi_size && psi == nullptr) ||
+        (h->sigma_size && sigma == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_heff_apply: null argument or nroots < 1");
+    if (nroots > 65535)
+        return fail(B2G_ERR_ARG, "b2g_heff_apply: too many roots");
+    if (form != B2G_FP64 && form != B2G_FP32 && form != B2G_TF32X3)
+        return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_apply: unknown form " + std::to_string(form));
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    int rc = apply_prepare(h, nroots, form);
+    if (rc != B2G_OK)
+        return rc;
+    if (h->graphs_on && !h->timing)
+        return apply_graphed(h, psi, sigma, nroots, scale, form);
+    return apply_launches(h, psi, sigma, nroots, scale, form);
+}
+
+int b2g_heff_set_graphs(b2g_heff *h, int enable) {
+    if (h == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_set_graphs: null handle");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    if (!enable) {
+        B2G_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+        clear_graphs(h);
+    }
+    h->graphs_on = enable != 0;
+    return B2G_OK;
+}
+
+int b2g_heff_graph_count(const b2g_heff *h) {
+    if (h == nullptr)
+        return -1;
+    int n = 0;
+    for (const auto &g : h->graphs)
+        n += g.state == 1;
+    return n;
 }
 
 int b2g_heff_apply(b2g_heff *h, const double *psi, double *sigma, double scale, int form) {

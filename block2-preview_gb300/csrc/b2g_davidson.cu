@@ -18,7 +18,8 @@
 //     all m vectors and recomputes all m^2 dot products each iteration);
 //     the rotation to the def_min lowest Ritz vectors happens only at restart;
 //   * the small subspace eigenproblem (LAPACK dsyev in the reference) is
-//     solved on the device by parallel cyclic Jacobi (one CTA, FP64);
+//     solved on the device by threshold cyclic Jacobi (one CTA, FP64),
+//     warm-started from the previous iteration's eigenvectors;
 //   * the correction vector is orthogonalised by classical Gram-Schmidt
 //     applied twice (the reference applies modified Gram-Schmidt once).
 // All vectors live in HBM; per iteration only the Ritz values and residual
@@ -151,59 +152,84 @@ __global__ void normalize_into(double *__restrict__ y, const double *__restrict_
         y[i] = x[i] * f;
 }
 
-// Parallel cyclic Jacobi (round-robin pairing) on the m x m symmetric matrix
-// A (row-major, lda), one CTA.  Outputs eigenvalues ascending in w[0..m) and
-// eigenvectors as columns of V (row-major, ldv = kMaxSub).
+// Parallel cyclic Jacobi on the m x m symmetric matrix A (row-major, lda), one
+// CTA.  Outputs eigenvalues ascending in w[0..m) and eigenvectors as columns
+// of V (row-major, ldv = kMaxSub).  Round s of a sweep pairs the indices by
+// the circle method (0 with 1 + s, and 1 + (s + j) with 1 + (s - j) modulo
+// mm - 1), so every pair meets once per sweep.  Rotations whose off-diagonal
+// element is below 1e-17 of the Frobenius norm are skipped (threshold
+// Jacobi): the FP64 pipe of one SM is the limit here, and a warm-started or
+// late sweep touches few pairs.  Stops when the off-diagonal mass is below
+// 1e-30 of the total or a sweep rotates nothing.
 __global__ void __launch_bounds__(256) jacobi_eig(const double *__restrict__ Ain, int lda, int m,
                                                   double *__restrict__ w, double *__restrict__ V) {
     __shared__ double A[kMaxSub][kMaxSub + 1];
     __shared__ double Vs[kMaxSub][kMaxSub + 1];
     __shared__ double cs[kMaxSub / 2], sn[kMaxSub / 2];
     __shared__ int pp[kMaxSub / 2], qq[kMaxSub / 2];
-    __shared__ int perm[kMaxSub];
-    __shared__ double off_s;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    __shared__ int n_act, n_rot, perm[kMaxSub];
+    __shared__ double red_off[8], red_tot[8], thr_s, stop_s;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
     const int mm = m + (m & 1);  // padded to even: the extra index is a dummy
     for (int i = tid; i < mm * mm; i += nt) {
         const int r = i / mm, c = i % mm;
         A[r][c] = (r < m && c < m) ? Ain[r * lda + c] : 0.0;
         Vs[r][c] = r == c ? 1.0 : 0.0;
     }
-    for (int i = tid; i < mm; i += nt)
-        perm[i] = i;
     __syncthreads();
-    const int half = mm / 2;
+    const int half = mm / 2, n1 = mm - 1;
     for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0, tot = 0.0;
+        for (int i = tid; i < m * m; i += nt) {
+            const int r = i / m, c = i % m;
+            const double v = A[r][c] * A[r][c];
+            (r == c ? tot : off) += v;
+        }
+        off = warp_sum(off), tot = warp_sum(tot);
+        if (lane == 0)
+            red_off[wid] = off, red_tot[wid] = tot;
+        __syncthreads();
         if (tid == 0) {
-            double off = 0.0, tot = 0.0;
-            for (int r = 0; r < m; r++)
-                for (int c = 0; c < m; c++)
-                    (r == c ? tot : off) += A[r][c] * A[r][c];
-            off_s = (off <= 1e-30 * (tot + off)) ? -1.0 : off;
+            double o = 0.0, t = 0.0;
+            for (int i = 0; i < nt / 32; i++)
+                o += red_off[i], t += red_tot[i];
+            stop_s = (o <= 1e-30 * (t + o)) ? 1.0 : 0.0;
+            thr_s = 1e-17 * sqrt(t + o);
+            n_rot = 0;
         }
         __syncthreads();
-        if (off_s < 0.0)
+        if (stop_s != 0.0)
             break;
-        for (int step = 0; step < mm - 1; step++) {
-            // pairs of this round: (perm[k], perm[mm-1-k])
+        const double thr = thr_s;
+        for (int step = 0; step < n1; step++) {
+            if (tid == 0)
+                n_act = 0;
+            __syncthreads();
             for (int k = tid; k < half; k += nt) {
-                int p = perm[k], q = perm[mm - 1 - k];
+                int p = k == 0 ? 0 : 1 + (step + k) % n1;
+                int q = 1 + (step + n1 - k) % n1;
+                if (k == 0)
+                    q = 1 + step % n1;
                 if (p > q) {
-                    int t = p;
+                    const int t = p;
                     p = q, q = t;
                 }
-                pp[k] = p, qq[k] = q;
-                double c = 1.0, s = 0.0;
-                if (q < m && A[p][q] != 0.0) {
+                if (q < m && fabs(A[p][q]) > thr) {
                     const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
                     const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-                    c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                    const double c = 1.0 / sqrt(t * t + 1.0);
+                    const int slot = atomicAdd(&n_act, 1);  // pairs are disjoint: order is immaterial
+                    pp[slot] = p, qq[slot] = q, cs[slot] = c, sn[slot] = t * c;
                 }
-                cs[k] = c, sn[k] = s;
             }
             __syncthreads();
-            // columns: A <- A J
-            for (int i = tid; i < half * mm; i += nt) {
+            const int na = n_act;
+            if (na == 0)
+                continue;  // uniform: every thread read the same count
+            if (tid == 0)
+                n_rot += na;
+            // columns: A <- A J, V <- V J
+            for (int i = tid; i < na * mm; i += nt) {
                 const int k = i / mm, r = i % mm, p = pp[k], q = qq[k];
                 const double c = cs[k], s = sn[k];
                 const double arp = A[r][p], arq = A[r][q];
@@ -215,7 +241,7 @@ __global__ void __launch_bounds__(256) jacobi_eig(const double *__restrict__ Ain
             }
             __syncthreads();
             // rows: A <- J^T A
-            for (int i = tid; i < half * mm; i += nt) {
+            for (int i = tid; i < na * mm; i += nt) {
                 const int k = i / mm, r = i % mm, p = pp[k], q = qq[k];
                 const double c = cs[k], s = sn[k];
                 const double apr = A[p][r], aqr = A[q][r];
@@ -223,15 +249,10 @@ __global__ void __launch_bounds__(256) jacobi_eig(const double *__restrict__ Ain
                 A[q][r] = s * apr + c * aqr;
             }
             __syncthreads();
-            // rotate the tournament (index 0 fixed)
-            if (tid == 0) {
-                const int last = perm[mm - 1];
-                for (int k = mm - 1; k > 1; k--)
-                    perm[k] = perm[k - 1];
-                perm[1] = last;
-            }
-            __syncthreads();
         }
+        __syncthreads();
+        if (n_rot == 0)
+            break;
     }
     if (tid == 0) {
         // sort ascending (selection), record order in perm
@@ -252,6 +273,61 @@ __global__ void __launch_bounds__(256) jacobi_eig(const double *__restrict__ Ain
     for (int i = tid; i < m * m; i += nt) {
         const int r = i / m, c = i % m;
         V[r * kMaxSub + c] = Vs[r][perm[c]];
+    }
+}
+
+// Warm start of the subspace eigenproblem: with the previous eigenvectors
+// Vp (mw x mw, ld kMaxSub) of the leading block, which the new basis vectors
+// only border, E = blockdiag(Vp, I) turns A into E^T A E, diagonal but for the
+// new rows, so Jacobi touches few pairs; the eigenvectors are then E times
+// Jacobi's.  One CTA per row (these products are O(m^3) FP64 work, spread
+// over m SMs).
+// T = A E
+__global__ void __launch_bounds__(64) sub_warm_right(const double *__restrict__ A, int m, int mw,
+                                                     const double *__restrict__ Vp,
+                                                     double *__restrict__ T) {
+    const int r = blockIdx.x;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        double v = 0.0;
+        if (c < mw) {
+            for (int b = 0; b < mw; b++)
+                v = fma(A[r * kMaxSub + b], Vp[b * kMaxSub + c], v);
+        } else {
+            v = A[r * kMaxSub + c];
+        }
+        T[r * kMaxSub + c] = v;
+    }
+}
+// A2 = E^T T
+__global__ void __launch_bounds__(64) sub_warm_left(const double *__restrict__ T, int m, int mw,
+                                                    const double *__restrict__ Vp,
+                                                    double *__restrict__ A2) {
+    const int r = blockIdx.x;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        double v = 0.0;
+        if (r < mw) {
+            for (int a = 0; a < mw; a++)
+                v = fma(Vp[a * kMaxSub + r], T[a * kMaxSub + c], v);
+        } else {
+            v = T[r * kMaxSub + c];
+        }
+        A2[r * kMaxSub + c] = v;
+    }
+}
+// V = E Vj
+__global__ void __launch_bounds__(64) sub_warm_vec(const double *__restrict__ Vp, int m, int mw,
+                                                   const double *__restrict__ Vj,
+                                                   double *__restrict__ V) {
+    const int r = blockIdx.x;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        double v = 0.0;
+        if (r < mw) {
+            for (int b = 0; b < mw; b++)
+                v = fma(Vp[r * kMaxSub + b], Vj[b * kMaxSub + c], v);
+        } else {
+            v = Vj[r * kMaxSub + c];
+        }
+        V[r * kMaxSub + c] = v;
     }
 }
 
@@ -308,7 +384,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     const int g = grid_for(n);
     double *B = nullptr, *S = nullptr, *X = nullptr, *SX = nullptr, *Q = nullptr, *t = nullptr,
            *R = nullptr, *D = nullptr, *small = nullptr, *partial = nullptr;
-    const size_t nsmall = (size_t)kMaxSub * kMaxSub * 2 + 6 * kMaxSub + 16;
+    const size_t nsmall = (size_t)kMaxSub * kMaxSub * 6 + 6 * kMaxSub + 16;
     auto cleanup = [&]() {
         cudaFree(B), cudaFree(S), cudaFree(X), cudaFree(SX), cudaFree(Q), cudaFree(t), cudaFree(R);
         cudaFree(D), cudaFree(small), cudaFree(partial);
@@ -324,7 +400,10 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     }
     double *A = small;                          // kMaxSub x kMaxSub subspace matrix
     double *V = A + kMaxSub * kMaxSub;          // eigenvectors (columns), ld kMaxSub
-    double *w = V + kMaxSub * kMaxSub;          // eigenvalues (ascending)
+    double *Vprev = V + kMaxSub * kMaxSub;      // the previous Ritz solve's eigenvectors
+    double *T = Vprev + kMaxSub * kMaxSub;      // warm-start scratch (A E, then Jacobi's vectors)
+    double *A2 = T + kMaxSub * kMaxSub;         // E^T A E
+    double *w = A2 + 2 * kMaxSub * kMaxSub;     // eigenvalues (ascending)
     double *dots = w + kMaxSub;                 // kMaxSub dot results
     double *qqd = dots + kMaxSub;               // kMaxSub residual norms
     double *sc = qqd + kMaxSub;                 // scratch scalars
@@ -336,6 +415,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     std::vector<double> lam(kMaxSub), qq(kMaxSub);
     int rc = B2G_OK;
     int m = 0, msig = 0, xiter = 0, n_fp64 = 0, n_mixed = 0, n_refine = 0, since_refine = 0;
+    int vw = 0;  // leading block of A whose eigenvectors V holds (warm start), 0 = none
     bool converged = false, have_exact = false;
     // host-side helpers; each returns false after recording an error in rc
     auto cuda_ok = [&](cudaError_t e, const char *what) {
@@ -381,7 +461,16 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     };
     // Rayleigh-Ritz: X, SX = the k lowest Ritz vectors and their images, residual norms
     auto ritz = [&]() -> bool {
-        jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
+        if (vw > 0 && vw < m) {
+            std::swap(V, Vprev);
+            sub_warm_right<<<m, 64, 0, st>>>(A, m, vw, Vprev, T);
+            sub_warm_left<<<m, 64, 0, st>>>(T, m, vw, Vprev, A2);
+            jacobi_eig<<<1, 256, 0, st>>>(A2, kMaxSub, m, w, T);
+            sub_warm_vec<<<m, 64, 0, st>>>(Vprev, m, vw, T, V);
+        } else {
+            jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
+        }
+        vw = m;
         rotate_basis<<<g, 256, 0, st>>>(X, B, n, m, k, V, kMaxSub, n);
         rotate_basis<<<g, 256, 0, st>>>(SX, S, n, m, k, V, kMaxSub, n);
         for (int i = 0; i < k; i++) {
@@ -431,7 +520,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             // is below conv_thrd, otherwise continue from this exact basis.
             if (!cuda_ok(cudaMemcpyAsync(B, X, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st), "X"))
                 goto done;
-            m = k, msig = 0;
+            m = k, msig = 0, vw = 0;
             if (!cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A") ||
                 !expand(B2G_FP64) || !ritz())
                 goto done;
@@ -458,6 +547,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
                 goto done;
             set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, def_min, w);
             m = msig = def_min;
+            vw = 0;
         }
         // ---- Olsen corrections of the unconverged roots
         int added = 0;

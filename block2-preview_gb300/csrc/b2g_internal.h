@@ -251,6 +251,22 @@ struct b2g_context {
     int n_sm = 0;
 };
 
+namespace b2g {
+// one captured H_eff*psi (CUDA graph) for a fixed argument set: the second
+// apply with the same psi, sigma, root count, scale and form captures its
+// launches, later ones replay the graph
+struct ApplyGraph {
+    const double *psi = nullptr;
+    double *sigma = nullptr;
+    int nroots = 0, form = 0;
+    double scale = 0.0;
+    cudaGraphExec_t exec = nullptr;
+    int state = 0;        // 0 seen once, 1 captured, -1 not capturable (runs eagerly)
+    uint64_t last = 0;    // LRU tick
+};
+constexpr size_t kMaxApplyGraphs = 64;
+} // namespace b2g
+
 struct b2g_heff {
     b2g_context *ctx = nullptr;
     b2g::DevicePlan plan;
@@ -273,4 +289,7 @@ struct b2g_heff {
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     int *err = nullptr;     // device flag: a bounded wait in a tensor-core kernel gave up
+    bool graphs_on = true;  // replay repeated applies as CUDA graphs
+    std::vector<b2g::ApplyGraph> graphs;
+    uint64_t graph_tick = 0;
 };

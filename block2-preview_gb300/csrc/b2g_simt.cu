@@ -42,11 +42,11 @@ __device__ __forceinline__ void p1_chunk(const T *__restrict__ prow, const T *__
     if (!wd.tb0) {
         for (int k = 0; k < wd.k0; k++) {
             const T a = __ldg(prow + k);
-            const T *brow = B + (uint64_t)k * wd.ldb0;
+            const T *brow = B + (uint64_t)k * wd.ldb0 + cbase + lane;
 #pragma unroll
             for (int j = 0; j < NJ; j++)
                 if (live[j])
-                    acc[j] = fma(a, __ldg(brow + col[j]), acc[j]);
+                    acc[j] = fma(a, __ldg(brow + 32 * j), acc[j]);
         }
     } else {
         for (int k = 0; k < wd.k0; k++) {
@@ -81,12 +81,6 @@ __global__ void __launch_bounds__(128) simt_phase1(const WorkDesc *__restrict__ 
     const T *B = ops + wd.b0;
     T *wrow = work + wd.woff + (uint64_t)tk.r * wd.n0;
     for (int cbase = 0; cbase < wd.n0; cbase += 32 * kLanesCols) {
-        if constexpr (sizeof(T) == 4) {
-            // the FP32 pipe is wide: predicated chunks cost little and the
-            // fixed 8-chunk body keeps more loads in flight
-            p1_chunk<T, 8>(prow, B, wd, cbase, lane, wrow);
-            continue;
-        }
         switch (min(kLanesCols, (wd.n0 - cbase + 31) >> 5)) {
         case 1: p1_chunk<T, 1>(prow, B, wd, cbase, lane, wrow); break;
         case 2: p1_chunk<T, 2>(prow, B, wd, cbase, lane, wrow); break;

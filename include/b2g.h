@@ -214,6 +214,17 @@ int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops, uint64_t 
 int b2g_heff_set_timing(b2g_heff *h, int enable);
 int b2g_heff_last_timing(b2g_heff *h, float *ms);
 
+/* CUDA-graph replay of repeated applies (on by default).  The reference
+ * replays its recorded BatchGEMMSeq on every Davidson iteration
+ * (src/core/batch_gemm.hpp:1570-1690); here the first apply with a given
+ * (psi, sigma, nroots, scale, form) runs its kernels directly, the second is
+ * captured into a CUDA graph and replayed, later ones replay it (at most 64
+ * graphs per H_eff, least recently used dropped; growing the root count drops
+ * them all).  Timing mode bypasses the graphs.  enable = 0 drops every graph. */
+int b2g_heff_set_graphs(b2g_heff *h, int enable);
+/* number of captured graphs held (-1 for a null handle) */
+int b2g_heff_graph_count(const b2g_heff *h);
+
 /* Measured compute ceiling of one arithmetic form on this device (a
  * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as
  * the roofline denominator where no measured peak exists (FP64). */
