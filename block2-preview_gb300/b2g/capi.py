@@ -120,6 +120,15 @@ SIGNATURES = {
                                C.c_int, C.c_int, C.POINTER(DavidsonResultC)]),
     "b2g_davidson_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(DavidsonResultC)]),
+    "b2g_quanta_op": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_uint64,
+                                C.POINTER(C.c_uint64)]),
+    "b2g_state_tensor_product": (C.c_int, [C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_uint64, C.c_void_p]),
+    "b2g_state_connection": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "b2g_wfn_blocks": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_uint32,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                 C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
     "b2g_dm_truncate": (C.c_int, [C.c_void_p, C.POINTER(DmLayoutC), C.c_void_p, C.c_int, C.c_double,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.POINTER(DmResultC)]),

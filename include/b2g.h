@@ -323,6 +323,53 @@ int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *layout, const double 
                     double cutoff, double *eigvals, int32_t *kept, double *rotation,
                     double *wfn, b2g_dm_result *res);
 
+/* ---- Quantum-number bookkeeping (host only, bit-exact with the reference) ----
+ * Labels are the reference's packed 64-bit words: SZLongLong
+ * (src/core/symmetry.hpp:656, N | 2Sz | pg) and SU2LongLong
+ * (src/core/symmetry.hpp:1185, N | 2S_low | 2S | pg).  A StateInfo is n
+ * ascending labels with their state counts (src/core/state_info.hpp:60-200). */
+#define B2G_SYM_SZ 0
+#define B2G_SYM_SU2 1
+/* b2g_quanta_op operations (symmetry.hpp operator+, unary -, count, [k],
+ * get_ket, get_bra, combine): out = a + b | -a | a.count() | a[b] | a.get_ket()
+ * | a.get_bra(b) | a.combine(bra = b, ket = c) (a is the delta quantum). */
+#define B2G_QOP_ADD 0
+#define B2G_QOP_NEG 1
+#define B2G_QOP_COUNT 2
+#define B2G_QOP_ELEM 3
+#define B2G_QOP_KET 4
+#define B2G_QOP_BRA 5
+#define B2G_QOP_COMBINE 6
+typedef struct {
+    int32_t n;           /* labels (on output: count; on input of an output: capacity) */
+    uint64_t *quanta;    /* n packed labels, ascending */
+    uint32_t *n_states;  /* n state counts */
+} b2g_state_info;
+
+int b2g_quanta_op(int sym, int op, uint64_t a, uint64_t b, uint64_t c, uint64_t *out);
+/* StateInfo::tensor_product (state_info.hpp:231-276): every coupled label of
+ * a x b; with cref != NULL only labels of cref are kept (counts added into
+ * cref's slots), otherwise labels above target are dropped; counts saturate
+ * at ubond_max (65535 for the reference's default 16-bit ubond_t).  c->n is
+ * the capacity on entry and the label count on return. */
+int b2g_state_tensor_product(int sym, uint32_t ubond_max, const b2g_state_info *a,
+                             const b2g_state_info *b, const b2g_state_info *cref,
+                             uint64_t target, b2g_state_info *c);
+/* StateInfo::get_connection_info (state_info.hpp:280-307): for each label of
+ * c the (i, j) label pairs of a and b that couple to it; acc (c->n + 1)
+ * offsets into ij (pairs stored as i, j; capacity cap pairs). */
+int b2g_state_connection(int sym, const b2g_state_info *a, const b2g_state_info *b,
+                         const b2g_state_info *c, uint32_t *acc, uint32_t *ij, int64_t cap,
+                         int64_t *n_pairs);
+/* SparseMatrixInfo::initialize (sparse_matrix.hpp:727-757) of an operator
+ * (wfn = 0) or wavefunction (wfn = 1) with delta quantum dq between bra and
+ * ket, plus initialize_block_shifts / get_total_memory (sparse_matrix.hpp:
+ * 617-630, 804-820) with 32-bit offsets and blocks rounded up to align
+ * elements (1 unless the reference runs with an AlignTypes alignment). */
+int b2g_wfn_blocks(int sym, const b2g_state_info *bra, const b2g_state_info *ket, uint64_t dq,
+                   int wfn, uint32_t align, uint64_t *quanta, uint32_t *rows, uint32_t *cols,
+                   uint32_t *shifts, int cap, int *n_blocks, uint32_t *total);
+
 #ifdef __cplusplus
 }
 #endif

@@ -255,6 +255,54 @@ template <typename S> struct Dumper : CallbackKernel {
         }
         w.man.flush();
     }
+    // Quantum-number bookkeeping of the two-site wavefunction, as
+    // MovingEnvironment::contract_two_dot builds it (moving_environment.hpp:3376-3387):
+    // the input StateInfos, the two tensor products, the connection info of the
+    // left one, a target-filtered product, and the wavefunction's block list.
+    static void put_si(Writer &w, const string &name, const StateInfo<S> &si) {
+        vector<uint64_t> q(si.n);
+        vector<int32_t> n(si.n);
+        for (int i = 0; i < si.n; i++)
+            q[i] = si.quanta[i].data, n[i] = (int32_t)si.n_states[i];
+        w.vec(name + "_q", q, "u8");
+        w.vec(name + "_n", n, "i4");
+    }
+    void dump_quanta(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        Writer w(site_dir() + "/qn");
+        auto mi = d->me->ket->info;
+        const int c = d->me->center;
+        mi->load_left_dims(c);
+        mi->load_right_dims(c + 2);
+        StateInfo<S> l = *mi->left_dims[c], ml = *mi->basis[c], mr = *mi->basis[c + 1],
+                     r = *mi->right_dims[c + 2];
+        StateInfo<S> ll = StateInfo<S>::tensor_product(l, ml, *mi->left_dims_fci[c + 1]);
+        StateInfo<S> rr = StateInfo<S>::tensor_product(mr, r, *mi->right_dims_fci[c + 1]);
+        StateInfo<S> lt = StateInfo<S>::tensor_product(l, ml, mi->target);
+        auto lc = StateInfo<S>::get_connection_info(l, ml, ll);
+        put_si(w, "l", l), put_si(w, "ml", ml), put_si(w, "mr", mr), put_si(w, "r", r);
+        put_si(w, "lfci", *mi->left_dims_fci[c + 1]), put_si(w, "rfci", *mi->right_dims_fci[c + 1]);
+        put_si(w, "ll", ll), put_si(w, "rr", rr), put_si(w, "lt", lt);
+        vector<int32_t> acc(lc->acc_n_states.begin(), lc->acc_n_states.end()), ia, ib;
+        for (auto &x : lc->ij_indices)
+            ia.push_back((int32_t)x.first), ib.push_back((int32_t)x.second);
+        w.vec("lc_acc", acc, "i4"), w.vec("lc_i", ia, "i4"), w.vec("lc_j", ib, "i4");
+        auto info = h->ket->info;
+        vector<uint64_t> q(info->n), sh(info->n);
+        vector<int32_t> nb(info->n), nk(info->n);
+        for (int i = 0; i < info->n; i++)
+            q[i] = info->quanta[i].data, nb[i] = (int32_t)info->n_states_bra[i],
+            nk[i] = (int32_t)info->n_states_ket[i], sh[i] = info->block_shifts[i];
+        w.vec("wfn_q", q, "u8"), w.vec("wfn_rows", nb, "i4"), w.vec("wfn_cols", nk, "i4");
+        w.vec("wfn_shift", sh, "u8");
+        vector<uint64_t> dq{info->delta_quantum.data, mi->target.data};
+        w.vec("dq_target", dq, "u8");
+        w.scalar("is_wfn", info->is_wavefunction);
+        w.scalar("total_memory", (double)h->ket->total_memory);
+        w.scalar("su2", is_same<S, SU2>::value ? 1 : 0);
+        w.man.flush();
+        lc = nullptr;
+        lt.deallocate(), rr.deallocate(), ll.deallocate();
+    }
     void dump_post(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
         Writer w(site_dir() + "/post");
         const size_t nket = h->ket->total_memory, nbra = h->bra->total_memory;
@@ -353,8 +401,10 @@ template <typename S> struct Dumper : CallbackKernel {
     void compute(const string &name, int iprint) const override {
         if (d == nullptr || d->current_eff_ham == nullptr || !selected())
             return;
-        if (name == "DMRG::sweep::iter.eff_ham")
+        if (name == "DMRG::sweep::iter.eff_ham") {
             dump_pre(d->current_eff_ham);
+            dump_quanta(d->current_eff_ham);
+        }
         else if (name == "DMRG::sweep::iter.eff_ham.end") {
             dump_post(d->current_eff_ham);
             want_rotation = true;

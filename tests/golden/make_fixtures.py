@@ -76,7 +76,22 @@ def fcidump_for(tag, workdir):
     return path
 
 
-def run_case(name, args, desc):
+def write_qn(name, site_dir):
+    """NAME_qn.npz: the quantum-number bookkeeping of the two-site wavefunction
+    (input StateInfos, the reference's tensor products, connection info and
+    block list) from the harness's qn dump."""
+    qa, qs = read_dump(os.path.join(site_dir, "qn"))
+    qpath = os.path.join(HERE, name + "_qn.npz")
+    np.savez_compressed(
+        qpath, su2=np.int32(qs["su2"]), is_wfn=np.int32(qs["is_wfn"]),
+        total_memory=np.int64(qs["total_memory"]), **qa,
+        meta=np.array(json.dumps({"name": name + "_qn", "kind": "quanta",
+                                  "description": "two-site wavefunction bookkeeping at the site of " + name})))
+    print(f"{name}_qn: blocks={qa['wfn_q'].size} ll={qa['ll_q'].size} rr={qa['rr_q'].size} "
+          f"-> {os.path.getsize(qpath)} bytes")
+
+
+def run_case(name, args, desc, qn_only=False):
     out = os.path.join(RAW, name)
     if os.path.exists(out):
         shutil.rmtree(out)
@@ -95,6 +110,9 @@ def run_case(name, args, desc):
     res_a, res_s = read_dump(os.path.join(out, "result"))
     site_dirs = [d for d in os.listdir(out) if d.startswith("sweep")]
     assert len(site_dirs) == 1, site_dirs
+    write_qn(name, os.path.join(out, site_dirs[0]))
+    if qn_only:
+        return
     pre_a, pre_s = read_dump(os.path.join(out, site_dirs[0]))
     post_a, post_s = read_dump(os.path.join(out, site_dirs[0], "post"))
     pairs = {k: pre_a[k] for k in PAIR_FIELDS}
@@ -184,6 +202,7 @@ def dm_fixture_from_dump(site_dir, name, desc):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default=None)
+    ap.add_argument("--qn-only", action="store_true", help="write only the NAME_qn.npz fixtures")
     ap.add_argument("--dm-from-dump", nargs=2, metavar=("SITE_DIR", "NAME"), default=None,
                     help="write NAME_dm.npz (spectrum and discarded weight only) from a site dump")
     a = ap.parse_args()
@@ -197,7 +216,7 @@ def main():
     for name, (args, desc) in CASES.items():
         if a.only and name != a.only:
             continue
-        run_case(name, args, desc)
+        run_case(name, args, desc, qn_only=a.qn_only)
 
 
 if __name__ == "__main__":
