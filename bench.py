@@ -160,6 +160,8 @@ def run_ours(args, rank, local_rank, world, dist):
     ctx = b2g.Context(local_rank)
     heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
     st = heff.stats
+    # tile shapes of the tensor-core form picked by the autotuner (untimed setup)
+    tune = None if args.no_autotune else heff.autotune()
     flop = 2.0 * st["mnk"]
     a = prob.pairs
     flop0 = 2.0 * float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]))
@@ -366,6 +368,8 @@ def run_ours(args, rank, local_rank, world, dist):
                   "inputs larger than L2 (operator blob + work > 4x L2)",
             "parallelism": f"replicas x{world}",
             "wall_s_timed_region": t_wall,
+            "tile_shapes": heff.params,
+            "autotune": tune,
         },
         "forms": per_form,
         "roofline": {
@@ -386,7 +390,9 @@ def run_ours(args, rank, local_rank, world, dist):
             "d2h_bytes_per_step": 8 * prob.sigma_size,
             "ms_per_step": e2e_total / args.steps * 1e3,
         },
-        "gpu_launches": args.steps * 2,
+        # kernels of ours per apply: TF32x3 g0_pack_psi, two g0_kernel classes, g1_kernel,
+        # g1_reduce; FP64 simt_phase1, simt_phase2, simt_reduce; FP32 adds to_float
+        "gpu_launches": args.steps * {"tf32x3": 5, "fp64": 3, "fp32": 4}[head],
         "clocks": ck,
         "sigma_norm": nrm,
     }
@@ -487,6 +493,8 @@ def main():
     ap.add_argument("--workload", default=None)
     ap.add_argument("--form", default="tf32x3", choices=sorted(FORMS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tile shapes (no autotuner pass before timing)")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline form (no other forms, batched roots or Davidson "
                          "sections); for profiler runs")

@@ -62,6 +62,21 @@ class DavidsonResultC(C.Structure):
     ]
 
 
+class TuneResultC(C.Structure):
+    _fields_ = [
+        ("n_candidates", C.c_int32), ("best", C.c_int32), ("ms", C.c_float * 12),
+        ("g0_tile_cols", C.c_int32 * 12), ("g1_tile_cols", C.c_int32 * 12), ("g1_chunk", C.c_int32 * 12),
+        ("g1_wide_frac", C.c_double), ("g0_wide_frac", C.c_double),
+    ]
+
+    def as_dict(self):
+        n = self.n_candidates
+        return {"best": self.best,
+                "candidates": [{"g0_tile_cols": self.g0_tile_cols[i], "g1_tile_cols": self.g1_tile_cols[i],
+                                "g1_chunk": self.g1_chunk[i], "ms": float(self.ms[i])} for i in range(n)],
+                "g1_wide_frac": self.g1_wide_frac, "g0_wide_frac": self.g0_wide_frac}
+
+
 class DmLayoutC(C.Structure):
     _fields_ = [
         ("trace_right", C.c_int32), ("n_psi_blocks", C.c_int32), ("psi_dm", C.c_void_p),
@@ -114,6 +129,8 @@ SIGNATURES = {
     "b2g_heff_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "b2g_heff_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "b2g_heff_graph_count": (C.c_int, [C.c_void_p]),
+    "b2g_heff_autotune": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC), C.c_int, C.POINTER(TuneResultC)]),
+    "b2g_heff_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_heff_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,

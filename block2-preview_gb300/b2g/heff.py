@@ -126,6 +126,21 @@ class EffectiveHamiltonian:
         check(lib().b2g_heff_diag(self._h, _ptr(out)))
         return out
 
+    def autotune(self, form: int = TF32X3) -> dict:
+        """Time the candidate tile shapes of this H_eff (from its block-size
+        histogram) and keep the fastest plan; returns the candidates, their
+        median apply times (ms) and the index kept."""
+        res = capi.TuneResultC()
+        check(lib().b2g_heff_autotune(self._h, C.byref(self.seq.c), form, C.byref(res)))
+        return res.as_dict()
+
+    @property
+    def params(self) -> dict:
+        """Tile shapes of the installed plan."""
+        v = (C.c_int32 * 3)()
+        check(lib().b2g_heff_get_params(self._h, v))
+        return {"g0_tile_cols": v[0], "g1_tile_cols": v[1], "g1_chunk": v[2]}
+
     def set_graphs(self, enable: bool):
         """Replay repeated applies as CUDA graphs (default on); False drops them."""
         check(lib().b2g_heff_set_graphs(self._h, int(bool(enable))))

@@ -106,6 +106,47 @@ static int ensure_g1(b2g_heff *h, int nroots) {
     return B2G_OK;
 }
 
+// replace the device plan of h by hp: drops the captured graphs and every
+// plan-shaped buffer (images, partials), which the next apply rebuilds
+static int install_plan(b2g_heff *h, const HostPlan &hp) {
+    cudaStream_t s = h->ctx->stream;
+    B2G_CUDA_TRY(cudaStreamSynchronize(s));
+    clear_graphs(h);
+    free_plan(h->plan);
+    cudaFree(h->g1_aimg), cudaFree(h->g1_wimg), cudaFree(h->g1_part), cudaFree(h->g0_psi);
+    h->g1_aimg = nullptr, h->g1_wimg = nullptr, h->g1_part = nullptr, h->g0_psi = nullptr;
+    h->g1_roots = 0;
+    DevicePlan &p = h->plan;
+    int rc;
+    if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
+        (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
+        (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
+        (rc = upload(hp.t2multi, &p.t2multi, s)) ||
+        (rc = upload(hp.g0tile, &p.g0tile, s)) || (rc = upload(hp.g0col, &p.g0col, s)) ||
+        (rc = upload(hp.g1tile, &p.g1tile, s)) ||
+        (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
+        (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
+        (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
+        (rc = upload(hp.g0psi, &p.g0psi, s)) || (rc = upload(hp.region_cb, &p.region_cb, s)))
+        return rc;
+    p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
+    p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
+    p.n_g0psi = (int64_t)hp.g0psi.size(), p.g0_psi_floats = hp.g0_psi_floats;
+    p.n_g0wide = hp.g0_wide;
+    p.max_region_cells = 0;
+    for (const Region &r : hp.regions)
+        p.max_region_cells = std::max<int64_t>(p.max_region_cells, (int64_t)r.rows * r.cols);
+    p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
+    p.n_t2multi = (int64_t)hp.t2multi.size();
+    p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
+    p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
+    p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
+    h->params = hp.params;
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(B2G_ERR_CUDA, "plan upload failed");
+    return B2G_OK;
+}
+
 } // namespace b2g
 
 using namespace b2g;
@@ -204,31 +245,9 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
     }
     if (cudaMemsetAsync(h->err, 0, sizeof(int), s) != cudaSuccess)
         return bail(fail(B2G_ERR_CUDA, "error flag reset failed"));
-    DevicePlan &p = h->plan;
-    if ((rc = upload(hp.works, &p.works, s)) || (rc = upload(hp.contribs, &p.contribs, s)) ||
-        (rc = upload(hp.regions, &p.regions, s)) || (rc = upload(hp.t1, &p.t1, s)) ||
-        (rc = upload(hp.t2, &p.t2, s)) || (rc = upload(hp.lists, &p.lists, s)) ||
-        (rc = upload(hp.t2multi, &p.t2multi, s)) ||
-        (rc = upload(hp.g0tile, &p.g0tile, s)) || (rc = upload(hp.g0col, &p.g0col, s)) ||
-        (rc = upload(hp.g1tile, &p.g1tile, s)) ||
-        (rc = upload(hp.g1stage, &p.g1stage, s)) || (rc = upload(hp.g1task, &p.g1task, s)) ||
-        (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
-        (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
-        (rc = upload(hp.g0psi, &p.g0psi, s)) || (rc = upload(hp.region_cb, &p.region_cb, s)))
+    if ((rc = install_plan(h, hp)) != B2G_OK)
         return bail(rc);
-    p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
-    p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
-    p.n_g0psi = (int64_t)hp.g0psi.size(), p.g0_psi_floats = hp.g0_psi_floats;
-    p.n_g0wide = hp.g0_wide;
-    for (const Region &r : hp.regions)
-        p.max_region_cells = std::max<int64_t>(p.max_region_cells, (int64_t)r.rows * r.cols);
-    p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
-    p.n_t2multi = (int64_t)hp.t2multi.size();
-    p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
-    p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
-    p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
-    if (cudaStreamSynchronize(s) != cudaSuccess)
-        return bail(fail(B2G_ERR_CUDA, "plan upload failed"));
+    const DevicePlan &p = h->plan;
     b2g_heff_stats &st = h->stats;
     st.n_pairs = seq->n_pairs;
     st.n_work = p.n_works;
@@ -531,6 +550,134 @@ int b2g_heff_apply_batch(b2g_heff *h, const double *psi, double *sigma, int nroo
     if (h->graphs_on && !h->timing)
         return apply_graphed(h, psi, sigma, nroots, scale, form);
     return apply_launches(h, psi, sigma, nroots, scale, form);
+}
+
+// Autotuner of the tensor-core tile shapes.  The candidates come from the
+// block-size histogram of the installed plan: narrower GEMM1 tiles only when
+// some sigma rectangles are wider than 128 columns, narrower GEMM0 tiles only
+// when some right operators are shared by more than 128 psi rows, and two
+// split-K chunk lengths; each candidate plan is installed and timed (CUDA
+// events, L2 flushed between applies) and the fastest is kept.
+int b2g_heff_autotune(b2g_heff *h, const b2g_pair_seq *seq, int form, b2g_tune_result *res) {
+    if (h == nullptr || seq == nullptr || res == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_autotune: null argument");
+    if (form != B2G_TF32X3)
+        return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_autotune: only the TF32x3 form has tile shapes");
+    if (seq->n_pairs != h->stats.n_pairs)
+        return fail(B2G_ERR_ARG, "b2g_heff_autotune: not the pair sequence of this H_eff");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    cudaStream_t s = h->ctx->stream;
+    *res = b2g_tune_result{};
+    HostPlan hp;
+    int rc = build_plan(seq, h->ops_size, h->psi_size, h->sigma_size, hp, PlanParams());
+    if (rc != B2G_OK)
+        return rc;
+    if (hp.mnk != h->stats.mnk)
+        return fail(B2G_ERR_ARG, "b2g_heff_autotune: not the pair sequence of this H_eff");
+    // histogram: GEMM1 stage work in tiles wider than 128 columns, GEMM0 tiles
+    // with more than 128 stacked rows
+    double w1 = 0, w1_wide = 0;
+    for (const G1Task &k : hp.g1task) {
+        const G1Tile &tl = hp.g1tile[k.tile];
+        w1 += (double)k.n_stages * tl.n;
+        if (tl.n > 128)
+            w1_wide += (double)k.n_stages * tl.n;
+    }
+    int64_t g0_wide = 0;
+    for (const G0Tile &t : hp.g0tile)
+        g0_wide += t.ncol > 128;
+    res->g1_wide_frac = w1 > 0 ? w1_wide / w1 : 0.0;
+    res->g0_wide_frac = hp.g0tile.empty() ? 0.0 : (double)g0_wide / (double)hp.g0tile.size();
+    std::vector<PlanParams> cand;
+    for (int c1 : {256, 128})
+        for (int c0 : {256, 128})
+            for (int ch : {kTcMaxChunkStages, kG1ChunkLimit, kTcMaxChunkStages / 2}) {
+                if (c1 == 128 && w1_wide == 0)
+                    continue;
+                if (c0 == 128 && g0_wide == 0)
+                    continue;
+                PlanParams pp;
+                pp.g1_tile_cols = c1, pp.g0_tile_cols = c0, pp.g1_chunk = ch;
+                cand.push_back(pp);
+            }
+    // scratch: psi, sigma, and an L2 flush buffer larger than L2
+    const size_t kFlush = (size_t)256 << 20;
+    double *x = nullptr, *y = nullptr;
+    unsigned char *flush = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(x), cudaFree(y), cudaFree(flush);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (cudaMalloc(&x, sizeof(double) * std::max<uint64_t>(1, h->psi_size)) ||
+        cudaMalloc(&y, sizeof(double) * std::max<uint64_t>(1, h->sigma_size)) ||
+        cudaMalloc(&flush, kFlush) || cudaEventCreate(&e0) || cudaEventCreate(&e1)) {
+        cleanup();
+        return fail(B2G_ERR_NOMEM, "b2g_heff_autotune: scratch allocation failed");
+    }
+    const bool timing = h->timing;
+    h->timing = false;
+    int best = -1;
+    float best_ms = 0.f;
+    for (size_t i = 0; i < cand.size() && rc == B2G_OK; i++) {
+        HostPlan cp;
+        if ((rc = build_plan(seq, h->ops_size, h->psi_size, h->sigma_size, cp, cand[i])) != B2G_OK ||
+            (rc = install_plan(h, cp)) != B2G_OK || (rc = apply_prepare(h, 1, form)) != B2G_OK)
+            break;
+        if (cudaMemsetAsync(x, 0x3F, sizeof(double) * h->psi_size, s) != cudaSuccess) {
+            rc = fail(B2G_ERR_CUDA, "b2g_heff_autotune: scratch fill failed");
+            break;
+        }
+        std::vector<float> ms;
+        for (int rep = 0; rep < 7 && rc == B2G_OK; rep++) {
+            cudaMemsetAsync(flush, rep, kFlush, s);
+            cudaMemsetAsync(y, 0, sizeof(double) * h->sigma_size, s);
+            cudaEventRecord(e0, s);
+            rc = apply_launches(h, x, y, 1, 1.0, form);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = fail(B2G_ERR_CUDA, "b2g_heff_autotune: timed apply failed");
+                break;
+            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep >= 2)
+                ms.push_back(t);
+        }
+        if (rc != B2G_OK)
+            break;
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[ms.size() / 2];
+        if (i < 12) {
+            res->ms[i] = med;
+            res->g0_tile_cols[i] = cand[i].g0_tile_cols;
+            res->g1_tile_cols[i] = cand[i].g1_tile_cols;
+            res->g1_chunk[i] = cand[i].g1_chunk;
+        }
+        if (best < 0 || med < best_ms)
+            best = (int)i, best_ms = med;
+    }
+    res->n_candidates = (int32_t)std::min<size_t>(cand.size(), 12);
+    res->best = best;
+    if (rc == B2G_OK && best >= 0 && best + 1 != (int)cand.size()) {
+        HostPlan bp;
+        if ((rc = build_plan(seq, h->ops_size, h->psi_size, h->sigma_size, bp, cand[best])) == B2G_OK)
+            rc = install_plan(h, bp);
+    }
+    h->timing = timing;
+    if (rc == B2G_OK && b2g_heff_status(h) != B2G_OK)
+        rc = B2G_ERR_STATE;
+    cleanup();
+    return rc;
+}
+
+int b2g_heff_get_params(const b2g_heff *h, int32_t *params) {
+    if (h == nullptr || params == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_get_params: null argument");
+    params[0] = h->params.g0_tile_cols, params[1] = h->params.g1_tile_cols;
+    params[2] = h->params.g1_chunk;
+    return B2G_OK;
 }
 
 int b2g_heff_set_graphs(b2g_heff *h, int enable) {

@@ -33,7 +33,7 @@ constexpr int kG1Threads = 192;                 // warp 0 copies, warp 1 MMAs, w
 constexpr int kG1MaxRing = 6;
 constexpr uint32_t kG1ABytes = 128 * kG1SlabK * 4;   // one split part of the A slab (8 KB)
 constexpr uint32_t kG1RingBytes = 96 * 1024;         // two CTAs per SM
-constexpr int kG1MaxStages = 64;                     // stage table held in shared memory
+constexpr int kG1MaxStages = kG1ChunkLimit;          // stage table held in shared memory
 constexpr uint32_t kG1SmemBytes = kG1RingBytes + 1024;
 constexpr uint32_t kG1TmemCols = 256;
 

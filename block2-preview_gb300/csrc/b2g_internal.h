@@ -69,6 +69,7 @@ struct Tile2 {          // a phase-2 tile split over several chunks (reduced aft
 // sums the chunks.
 constexpr int kTcStageK = 16;
 constexpr int kTcMaxChunkStages = 32;
+constexpr int kG1ChunkLimit = 64;   // longest chunk the GEMM1 kernel's stage table holds
 
 // Tensor-core GEMM0 of the TF32x3 form, transposed: W_u^T = op(R)^T *
 // psi_u^T for the distinct products sharing one right operator block R.  A
@@ -147,7 +148,15 @@ struct G1Red {                  // reduction item: rows [r0, r1) of region g
 };
 constexpr int kG1SlabK = 16;
 
+// tile shapes of the tensor-core form (the autotuner's search space)
+struct PlanParams {
+    int32_t g0_tile_cols = 256;              // stacked psi rows per GEMM0 tile (128 or 256)
+    int32_t g1_tile_cols = 256;              // sigma columns per GEMM1 tile (128 or 256)
+    int32_t g1_chunk = kTcMaxChunkStages;    // K slabs per GEMM1 split-K chunk (<= kG1ChunkLimit)
+};
+
 struct HostPlan {
+    PlanParams params;
     std::vector<G0Tile> g0tile;
     std::vector<G0Col> g0col;
     std::vector<G0Psi> g0psi;
@@ -178,7 +187,7 @@ struct HostPlan {
 };
 
 int build_plan(const b2g_pair_seq *seq, uint64_t ops_size, uint64_t psi_size, uint64_t sigma_size,
-               HostPlan &plan);
+               HostPlan &plan, const PlanParams &params = PlanParams());
 
 struct DevicePlan {
     WorkDesc *works = nullptr;
@@ -289,6 +298,7 @@ struct b2g_heff {
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     int *err = nullptr;     // device flag: a bounded wait in a tensor-core kernel gave up
+    b2g::PlanParams params;  // tile shapes of the installed plan
     bool graphs_on = true;  // replay repeated applies as CUDA graphs
     std::vector<b2g::ApplyGraph> graphs;
     uint64_t graph_tick = 0;

@@ -61,11 +61,17 @@ static constexpr int kRowsPerTask = 4;    // warps per phase-2 CTA, one row each
 static constexpr int kColsPerTask = 256;  // 8 x 32 lanes
 
 int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint64_t sigma_size,
-               HostPlan &plan) {
+               HostPlan &plan, const PlanParams &params) {
     if (s == nullptr || s->n_pairs < 0)
         return fail(B2G_ERR_ARG, "b2g_heff_create: null or negative pair sequence");
+    if ((params.g0_tile_cols != 128 && params.g0_tile_cols != 256) ||
+        (params.g1_tile_cols != 128 && params.g1_tile_cols != 256) || params.g1_chunk < 1 ||
+        params.g1_chunk > kG1ChunkLimit)
+        return fail(B2G_ERR_ARG, "plan parameters outside the supported tile shapes");
     const int64_t np = s->n_pairs;
     plan = HostPlan();
+    plan.params = params;
+    const int32_t g1w = params.g1_tile_cols, g0w = params.g0_tile_cols;
     // ---- validation + GEMM0 de-duplication -------------------------------
     std::unordered_map<WorkKey, int32_t, WorkKeyHash> wmap;
     wmap.reserve((size_t)np * 2 + 1);
@@ -258,12 +264,12 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 const int32_t row0 = rkeys[z][0], m1 = rkeys[z][1], col0 = rkeys[z][2], n1 = rkeys[z][3];
                 const int32_t npad = (n1 + 15) / 16 * 16;
                 for (int32_t rp = 0; rp * 128 < m1; rp++)
-                    for (int32_t cp = 0; cp * 256 < npad; cp++) {
+                    for (int32_t cp = 0; cp * g1w < npad; cp++) {
                         G1Tile t;
-                        t.g = g, t.row0 = row0 + 128 * rp, t.col0 = col0 + 256 * cp;
+                        t.g = g, t.row0 = row0 + 128 * rp, t.col0 = col0 + g1w * cp;
                         t.rows = std::min(128, m1 - 128 * rp);
-                        t.n = std::min(256, npad - 256 * cp);
-                        t.ncols = std::min(t.n, n1 - 256 * cp);
+                        t.n = std::min(g1w, npad - g1w * cp);
+                        t.ncols = std::min(t.n, n1 - g1w * cp);
                         t.pad = 0;
                         t.n_chunks = 0;
                         t.part = (int64_t)plan.g1stage.size();  // first stage until chunking
@@ -364,7 +370,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             const int32_t npad = (w.n0 + 15) / 16 * 16;
             st.a = im.dst + (uint64_t)rp * 16384 * nsl + (uint64_t)sl * rows8 * 128;
             st.a_bytes = (uint32_t)rows8 * 64;
-            st.b = wdst[c.u] + (uint64_t)sl * npad * 128 + (uint64_t)cp * 256 * 64;
+            st.b = wdst[c.u] + (uint64_t)sl * npad * 128 + (uint64_t)cp * g1w * 64;
             st.b_lo = (uint32_t)npad * 64;
         }
         for (int32_t t = 0; t < (int32_t)plan.g1tile.size(); t++) {
@@ -373,10 +379,10 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             const int64_t se = t + 1 < (int32_t)plan.g1tile.size() ? plan.g1tile[t + 1].part
                                                                    : (int64_t)plan.g1stage.size();
             int32_t ch = 0;
-            for (int64_t st = sb; st < se; st += kTcMaxChunkStages, ch++) {
+            for (int64_t st = sb; st < se; st += params.g1_chunk, ch++) {
                 G1Task k;
                 k.tile = t, k.chunk = ch, k.st0 = st;
-                k.n_stages = (int32_t)std::min<int64_t>(kTcMaxChunkStages, se - st), k.pad = 0;
+                k.n_stages = (int32_t)std::min<int64_t>(params.g1_chunk, se - st), k.pad = 0;
                 plan.g1task.push_back(k);
             }
             tl.n_chunks = ch;
@@ -456,8 +462,8 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 }
             }
             const int32_t npad = (w0.n0 + 15) / 16 * 16;
-            for (size_t c0 = 0; c0 < cols.size(); c0 += 256) {
-                const int32_t nc = (int32_t)std::min<size_t>(256, cols.size() - c0);
+            for (size_t c0 = 0; c0 < cols.size(); c0 += (size_t)g0w) {
+                const int32_t nc = (int32_t)std::min<size_t>((size_t)g0w, cols.size() - c0);
                 const int64_t cb = (int64_t)plan.g0col.size();
                 plan.g0col.insert(plan.g0col.end(), cols.begin() + c0, cols.begin() + c0 + nc);
                 for (int32_t rp = 0; rp * 128 < w0.n0; rp++) {

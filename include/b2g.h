@@ -225,6 +225,27 @@ int b2g_heff_set_graphs(b2g_heff *h, int enable);
 /* number of captured graphs held (-1 for a null handle) */
 int b2g_heff_graph_count(const b2g_heff *h);
 
+/* Autotuner of the tensor-core tile shapes (no reference counterpart: the
+ * reference's BatchGEMMSeq replays fixed MKL calls).  From the block-size
+ * histogram of this H_eff's plan it lists candidate shapes -- GEMM0 tiles of
+ * 256 or 128 stacked psi rows (128 only tried when some right operator is
+ * shared by more rows), GEMM1 tiles of 256 or 128 sigma columns (128 only
+ * when some rectangle is wider), split-K chunks of 32, 64 or 16 K slabs -- times
+ * one TF32x3 apply of each (median of 5 after 2 warm-ups, L2 flushed between
+ * applies) and keeps the fastest plan installed.  seq must be the sequence
+ * the H_eff was created from.  Only form = B2G_TF32X3 has tile shapes. */
+typedef struct {
+    int32_t n_candidates, best;     /* candidates timed; index of the kept one */
+    float ms[12];                   /* median apply time per candidate */
+    int32_t g0_tile_cols[12], g1_tile_cols[12], g1_chunk[12];
+    double g1_wide_frac;            /* GEMM1 stage work in tiles wider than 128 columns */
+    double g0_wide_frac;            /* GEMM0 tiles with more than 128 stacked rows */
+} b2g_tune_result;
+int b2g_heff_autotune(b2g_heff *h, const b2g_pair_seq *seq, int form, b2g_tune_result *res);
+/* tile shapes of the installed plan: params[0] GEMM0 tile rows, params[1]
+ * GEMM1 tile columns, params[2] split-K chunk length */
+int b2g_heff_get_params(const b2g_heff *h, int32_t *params);
+
 /* Measured compute ceiling of one arithmetic form on this device (a
  * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as
  * the roofline denominator where no measured peak exists (FP64). */
