@@ -161,7 +161,11 @@ def run_ours(args, rank, local_rank, world, dist):
     heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
     st = heff.stats
     # tile shapes of the tensor-core form picked by the autotuner (untimed setup)
-    tune = None if args.no_autotune else heff.autotune()
+    if args.tiles:
+        heff.set_params(*[int(x) for x in args.tiles.split(",")])
+        tune = None
+    else:
+        tune = None if args.no_autotune else heff.autotune()
     flop = 2.0 * st["mnk"]
     a = prob.pairs
     flop0 = 2.0 * float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]))
@@ -433,7 +437,7 @@ def run_ours(args, rank, local_rank, world, dist):
     return result
 
 
-def truncation_section(ctx):
+def truncation_section(ctx, cpu=True):
 
     from b2g.truncation import DensityMatrixLayout, split_density_matrix
     path = os.path.join(ROOT, "tests", "golden", "syn24_su2_M1000_dm.npz")
@@ -456,6 +460,8 @@ def truncation_section(ctx):
            "gpu_ms": 1e3 * statistics.median(ts), "kept": res.n_kept,
            "error": res.error, "reference_error": float(z["error"]),
            "max_abs_eig_err_vs_reference": float(np.abs(eig - eig_ref).max())}
+    if not cpu:
+        return out
     from oracle import oracle as _oracle
     t0 = time.perf_counter()
     _oracle.dm_truncate(bool(z["trace_right"]), z["psi_dm"], z["psi_rows"], z["psi_cols"], z["psi_off"],
@@ -495,6 +501,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile shapes (no autotuner pass before timing)")
+    ap.add_argument("--tiles", default=None,
+                    help="tile shapes g0_rows,g1_cols,chunk installed instead of autotuning "
+                         "(profiler runs: the autotuner would time candidates under the profiler)")
+    ap.add_argument("--truncation-only", action="store_true",
+                    help="run only the density-matrix truncation section (GPU, no CPU leg); "
+                         "for profiler runs")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline form (no other forms, batched roots or Davidson "
                          "sections); for profiler runs")
@@ -508,6 +520,11 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.truncation_only:
+        import b2g
+        print(json.dumps({"section": "truncation", **truncation_section(b2g.Context(local_rank), cpu=False)}),
+              flush=True)
         return
     dist = None
     if world > 1:

@@ -131,6 +131,7 @@ SIGNATURES = {
     "b2g_heff_graph_count": (C.c_int, [C.c_void_p]),
     "b2g_heff_autotune": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC), C.c_int, C.POINTER(TuneResultC)]),
     "b2g_heff_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "b2g_heff_set_params": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC), C.c_void_p]),
     "b2g_heff_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,

@@ -141,6 +141,11 @@ class EffectiveHamiltonian:
         check(lib().b2g_heff_get_params(self._h, v))
         return {"g0_tile_cols": v[0], "g1_tile_cols": v[1], "g1_chunk": v[2]}
 
+    def set_params(self, g0_tile_cols: int, g1_tile_cols: int, g1_chunk: int):
+        """Install the plan with these tile shapes (no timing)."""
+        v = (C.c_int32 * 3)(g0_tile_cols, g1_tile_cols, g1_chunk)
+        check(lib().b2g_heff_set_params(self._h, C.byref(self.seq.c), v))
+
     def set_graphs(self, enable: bool):
         """Replay repeated applies as CUDA graphs (default on); False drops them."""
         check(lib().b2g_heff_set_graphs(self._h, int(bool(enable))))

@@ -672,6 +672,23 @@ int b2g_heff_autotune(b2g_heff *h, const b2g_pair_seq *seq, int form, b2g_tune_r
     return rc;
 }
 
+int b2g_heff_set_params(b2g_heff *h, const b2g_pair_seq *seq, const int32_t *params) {
+    if (h == nullptr || seq == nullptr || params == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_heff_set_params: null argument");
+    if (seq->n_pairs != h->stats.n_pairs)
+        return fail(B2G_ERR_ARG, "b2g_heff_set_params: not the pair sequence of this H_eff");
+    B2G_CUDA_TRY(cudaSetDevice(h->ctx->device));
+    PlanParams pp;
+    pp.g0_tile_cols = params[0], pp.g1_tile_cols = params[1], pp.g1_chunk = params[2];
+    HostPlan hp;
+    int rc = build_plan(seq, h->ops_size, h->psi_size, h->sigma_size, hp, pp);
+    if (rc != B2G_OK)
+        return rc;
+    if (hp.mnk != h->stats.mnk)
+        return fail(B2G_ERR_ARG, "b2g_heff_set_params: not the pair sequence of this H_eff");
+    return install_plan(h, hp);
+}
+
 int b2g_heff_get_params(const b2g_heff *h, int32_t *params) {
     if (h == nullptr || params == nullptr)
         return fail(B2G_ERR_ARG, "b2g_heff_get_params: null argument");

@@ -245,6 +245,9 @@ int b2g_heff_autotune(b2g_heff *h, const b2g_pair_seq *seq, int form, b2g_tune_r
 /* tile shapes of the installed plan: params[0] GEMM0 tile rows, params[1]
  * GEMM1 tile columns, params[2] split-K chunk length */
 int b2g_heff_get_params(const b2g_heff *h, int32_t *params);
+/* install the plan with the given tile shapes (same meaning; 128 or 256, 128
+ * or 256, 1..64) without timing, e.g. shapes an earlier autotune kept */
+int b2g_heff_set_params(b2g_heff *h, const b2g_pair_seq *seq, const int32_t *params);
 
 /* Measured compute ceiling of one arithmetic form on this device (a
  * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as

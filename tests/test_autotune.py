@@ -69,3 +69,25 @@ def test_autotune_rejects_other_forms_and_sequences(problems, ctx):
             h.autotune()
     finally:
         h.close()
+
+
+def test_set_params_installs_given_shapes(problems, ctx):
+    p = problems["hub16_su2_M250"]
+    h = b2g.EffectiveHamiltonian(ctx, p.seq(), p.ops, p.psi_size, p.sigma_size)
+    try:
+        psi = torch.from_numpy(p.psi).cuda()
+        for shapes in ((128, 128, 16), (256, 128, 64), (256, 256, 32)):
+            h.set_params(*shapes)
+            assert h.params == dict(zip(("g0_tile_cols", "g1_tile_cols", "g1_chunk"), shapes))
+            sig = torch.zeros(p.sigma_size, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            h(psi, sig, 1.0, b2g.TF32X3)
+            ctx.synchronize()
+            h.status()
+            assert rel(sig.cpu().numpy(), p.sigma) <= RTOL_TF32X3
+        with pytest.raises(b2g.B2GError):
+            h.set_params(64, 256, 32)
+        with pytest.raises(b2g.B2GError):
+            h.set_params(256, 256, 65)
+    finally:
+        h.close()
