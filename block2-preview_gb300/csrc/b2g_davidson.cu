@@ -46,45 +46,88 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// partial[j * gridDim.x + block] = sum over this block's slice of X_j . y
-// X_j = X + j * ldx (j < nv)
-__global__ void __launch_bounds__(kRedThreads) multidot_partial(const double *__restrict__ X,
-                                                                uint64_t ldx, int nv,
-                                                                const double *__restrict__ y,
-                                                                uint64_t n, double *partial) {
-    __shared__ double red[kRedThreads / 32];
+// out[j] = X_j . y for j < nv (X_j = X + j * ldx), one launch: every block
+// sums its grid-stride slice for up to kDotBatch vectors at a time (independent
+// FP64 chains, interleaved reductions) into partial[j * gridDim.x + block];
+// the last block to finish (a counter, reset by that block) adds the
+// partials of each j in block order.  Deterministic: fixed slices, fixed
+// reduction trees, fixed final order.
+constexpr int kDotBatch = 8;
+// NB vectors j0 .. j0+NB-1 of this block's slice into partial; exact NB so the
+// narrow FP64 pipe issues no predicated-off FMA or add
+template <int NB>
+__device__ __forceinline__ void multidot_chunk(const double *__restrict__ X, uint64_t ldx, int j0,
+                                               const double *__restrict__ y, uint64_t n,
+                                               double *partial, double (*red)[kDotBatch]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (int j = 0; j < nv; j++) {
-        const double *x = X + (uint64_t)j * ldx;
-        double s = 0.0;
-        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-            s = fma(x[i], y[i], s);
-        s = warp_sum(s);
-        if ((threadIdx.x & 31) == 0)
-            red[threadIdx.x >> 5] = s;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            double v = threadIdx.x < kRedThreads / 32 ? red[threadIdx.x] : 0.0;
-            v = warp_sum(v);
-            if (threadIdx.x == 0)
-                partial[(uint64_t)j * gridDim.x + blockIdx.x] = v;
-        }
-        __syncthreads();
+    double s[NB];
+#pragma unroll
+    for (int jj = 0; jj < NB; jj++)
+        s[jj] = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double yi = y[i];
+#pragma unroll
+        for (int jj = 0; jj < NB; jj++)
+            s[jj] = fma(X[(uint64_t)(j0 + jj) * ldx + i], yi, s[jj]);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int jj = 0; jj < NB; jj++)
+            s[jj] += __shfl_down_sync(0xffffffffu, s[jj], o);
+    if (lane == 0)
+#pragma unroll
+        for (int jj = 0; jj < NB; jj++)
+            red[warp][jj] = s[jj];
+    __syncthreads();
+    if (threadIdx.x < NB) {
+        const int jj = threadIdx.x;
+        static_assert(kRedThreads / 32 == 8, "tree below sums 8 warps");
+        const double v = ((red[0][jj] + red[1][jj]) + (red[2][jj] + red[3][jj])) +
+                         ((red[4][jj] + red[5][jj]) + (red[6][jj] + red[7][jj]));
+        partial[(uint64_t)(j0 + jj) * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
 }
 
-// out[j] = sum_b partial[j * nb + b] (fixed order), one warp per j
-__global__ void multidot_final(const double *__restrict__ partial, int nb, int nv, double *out) {
-    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (j >= nv)
+__global__ void __launch_bounds__(kRedThreads) multidot(const double *__restrict__ X, uint64_t ldx,
+                                                        int nv, const double *__restrict__ y,
+                                                        uint64_t n, double *partial,
+                                                        unsigned *counter, double *out) {
+    __shared__ double red[kRedThreads / 32][kDotBatch];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j0 = 0; j0 < nv; j0 += kDotBatch) {
+        switch (min(kDotBatch, nv - j0)) {
+        case 1: multidot_chunk<1>(X, ldx, j0, y, n, partial, red); break;
+        case 2: multidot_chunk<2>(X, ldx, j0, y, n, partial, red); break;
+        case 3: multidot_chunk<3>(X, ldx, j0, y, n, partial, red); break;
+        case 4: multidot_chunk<4>(X, ldx, j0, y, n, partial, red); break;
+        case 5: multidot_chunk<5>(X, ldx, j0, y, n, partial, red); break;
+        case 6: multidot_chunk<6>(X, ldx, j0, y, n, partial, red); break;
+        case 7: multidot_chunk<7>(X, ldx, j0, y, n, partial, red); break;
+        default: multidot_chunk<8>(X, ldx, j0, y, n, partial, red); break;
+        }
+    }
+    // the last block adds the partials
+    __threadfence();
+    if (threadIdx.x == 0)
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last)
         return;
-    double s = 0.0;
-    for (int b = lane; b < nb; b += 32)
-        s += partial[(uint64_t)j * nb + b];
-    s = warp_sum(s);
-    if (lane == 0)
-        out[j] = s;
+    __threadfence();
+    for (int j = warp; j < nv; j += kRedThreads / 32) {
+        double v = 0.0;
+        for (int bb = lane; bb < (int)gridDim.x; bb += 32)
+            v += __ldcg(partial + (uint64_t)j * gridDim.x + bb);
+        v = warp_sum(v);
+        if (lane == 0)
+            out[j] = v;
+    }
+    if (threadIdx.x == 0)
+        *counter = 0u;
 }
 
 // y = beta * y + sum_j coef[j] * X_j   (coef on device, optionally negated)
@@ -394,7 +437,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
         cudaMalloc(&Q, sizeof(double) * n * k) || cudaMalloc(&t, sizeof(double) * n) ||
         cudaMalloc(&R, sizeof(double) * n * def_min) || cudaMalloc(&D, sizeof(double) * n) ||
         cudaMalloc(&small, sizeof(double) * nsmall) ||
-        cudaMalloc(&partial, sizeof(double) * kRedBlocks * kMaxSub)) {
+        cudaMalloc(&partial, sizeof(double) * (kRedBlocks * kMaxSub + 1))) {
         cleanup();
         return fail(B2G_ERR_NOMEM, "b2g_davidson: device workspace allocation failed");
     }
@@ -408,9 +451,11 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     double *qqd = dots + kMaxSub;               // kMaxSub residual norms
     double *sc = qqd + kMaxSub;                 // scratch scalars
     double *coef = sc + 16;                     // kMaxSub coefficients
+    unsigned *dot_counter = (unsigned *)(partial + (size_t)kRedBlocks * kMaxSub);
+    // about four elements per thread: short per-thread FP64 chains and few partials
+    const int dot_blocks = (int)std::min<uint64_t>(kRedBlocks, std::max<uint64_t>(1, (n + 1023) / 1024));
     auto dot_many = [&](const double *Xv, int nv, const double *y, double *out) {
-        multidot_partial<<<kRedBlocks, kRedThreads, 0, st>>>(Xv, n, nv, y, n, partial);
-        multidot_final<<<(nv + 7) / 8, 256, 0, st>>>(partial, kRedBlocks, nv, out);
+        multidot<<<dot_blocks, kRedThreads, 0, st>>>(Xv, n, nv, y, n, partial, dot_counter, out);
     };
     std::vector<double> lam(kMaxSub), qq(kMaxSub);
     int rc = B2G_OK;
@@ -493,7 +538,8 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     // ---- initial basis: the k guesses, orthonormalised
     if (!cuda_ok(cudaMemcpyAsync(D, diag, sizeof(double) * n, cudaMemcpyHostToDevice, st), "diag") ||
         !cuda_ok(cudaMemcpyAsync(Q, psi, sizeof(double) * n * k, cudaMemcpyHostToDevice, st), "psi") ||
-        !cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A"))
+        !cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A") ||
+        !cuda_ok(cudaMemsetAsync(dot_counter, 0, sizeof(unsigned), st), "counter"))
         goto done;
     for (int i = 0; i < k; i++) {
         const int r = append(Q + (uint64_t)i * n);
