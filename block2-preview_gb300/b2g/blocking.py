@@ -48,3 +48,17 @@ def contract(ctx, seq, env, site, tmp_size: int, out_size: int) -> np.ndarray:
     check(lib().b2g_block_contract(ctx.handle, C.byref(seq.c), env.ctypes.data, env.size, site.ctypes.data,
                                    site.size, int(tmp_size), out.ctypes.data, int(out_size)))
     return out[:int(out_size)]
+
+
+def contract_device(ctx, seq, env, site, tmp_size: int, out):
+    """Device-resident blocking: env, site and out are contiguous float64 CUDA
+    tensors (out holds out.numel() doubles and is overwritten)."""
+    if not isinstance(seq, BlockSeq):
+        seq = BlockSeq(seq)
+    for t in (env, site, out):
+        if not (t.is_cuda and t.is_contiguous()):
+            raise TypeError("env, site and out must be contiguous CUDA tensors")
+    check(lib().b2g_block_contract_device(ctx.handle, C.byref(seq.c), env.data_ptr(), env.numel(),
+                                          site.data_ptr(), site.numel(), int(tmp_size), out.data_ptr(),
+                                          out.numel()))
+    return out

@@ -123,6 +123,8 @@ SIGNATURES = {
     "b2g_heff_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_block_contract": (C.c_int, [C.c_void_p, C.POINTER(BlockSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                      C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64]),
+    "b2g_block_contract_device": (C.c_int, [C.c_void_p, C.POINTER(BlockSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
+                                     C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64]),
     "b2g_heff_diag_host": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),

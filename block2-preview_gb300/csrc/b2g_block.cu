@@ -120,9 +120,9 @@ void group_overlapping(int64_t n, Span span, std::vector<int64_t> &order, std::v
 
 using namespace b2g;
 
-extern "C" int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
-                                  uint64_t env_size, const double *site, uint64_t site_size,
-                                  uint64_t tmp_size, double *out, uint64_t out_size) {
+static int block_contract(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
+                          uint64_t env_size, const double *site, uint64_t site_size,
+                          uint64_t tmp_size, double *out, uint64_t out_size, bool on_device) {
     if (ctx == nullptr || seq == nullptr || out == nullptr || (env_size && env == nullptr) ||
         (site_size && site == nullptr) || seq->n_iadd < 0 || seq->n_kron < 0)
         return fail(B2G_ERR_ARG, "b2g_block_contract: null or negative argument");
@@ -176,17 +176,26 @@ extern "C" int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, co
         kr_s[p] = kr[kr_order[p]];
     B2G_CUDA_TRY(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    double *d_env = nullptr, *d_site = nullptr, *d_tmp = nullptr, *d_out = nullptr;
+    // device operands: the caller's (on_device) or staged copies of the host
+    // buffers; scratch from the stream-ordered pool (no synchronisation)
+    double *d_env = on_device ? const_cast<double *>(env) : nullptr;
+    double *d_site = on_device ? const_cast<double *>(site) : nullptr;
+    double *d_out = on_device ? out : nullptr, *d_tmp = nullptr;
     BlkIadd *d_ia = nullptr;
     BlkKron *d_kr = nullptr;
     int64_t *d_iag = nullptr, *d_krg = nullptr;
     auto cleanup = [&]() {
-        cudaFree(d_env), cudaFree(d_site), cudaFree(d_tmp), cudaFree(d_out);
-        cudaFree(d_ia), cudaFree(d_kr), cudaFree(d_iag), cudaFree(d_krg);
+        if (!on_device) {
+            cudaFreeAsync(d_env, s), cudaFreeAsync(d_site, s), cudaFreeAsync(d_out, s);
+        }
+        cudaFreeAsync(d_tmp, s);
+        cudaFreeAsync(d_ia, s), cudaFreeAsync(d_kr, s), cudaFreeAsync(d_iag, s), cudaFreeAsync(d_krg, s);
     };
-    auto dmalloc = [](void **p, size_t bytes) { return cudaMalloc(p, std::max<size_t>(bytes, 16)); };
-    if (dmalloc((void **)&d_env, sizeof(double) * env_size) || dmalloc((void **)&d_site, sizeof(double) * site_size) ||
-        dmalloc((void **)&d_tmp, sizeof(double) * tmp_size) || dmalloc((void **)&d_out, sizeof(double) * out_size) ||
+    auto dmalloc = [&](void **p, size_t bytes) { return cudaMallocAsync(p, std::max<size_t>(bytes, 16), s); };
+    if ((!on_device && (dmalloc((void **)&d_env, sizeof(double) * env_size) ||
+                        dmalloc((void **)&d_site, sizeof(double) * site_size) ||
+                        dmalloc((void **)&d_out, sizeof(double) * out_size))) ||
+        dmalloc((void **)&d_tmp, sizeof(double) * tmp_size) ||
         dmalloc((void **)&d_ia, sizeof(BlkIadd) * ia_s.size()) || dmalloc((void **)&d_kr, sizeof(BlkKron) * kr_s.size()) ||
         dmalloc((void **)&d_iag, sizeof(int64_t) * ia_grp.size()) ||
         dmalloc((void **)&d_krg, sizeof(int64_t) * kr_grp.size())) {
@@ -198,10 +207,13 @@ extern "C" int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, co
         if (e == cudaSuccess)
             e = x;
     };
-    step(cudaMemcpyAsync(d_env, env, sizeof(double) * env_size, cudaMemcpyHostToDevice, s));
-    step(cudaMemcpyAsync(d_site, site, sizeof(double) * site_size, cudaMemcpyHostToDevice, s));
+    if (!on_device) {
+        step(cudaMemcpyAsync(d_env, env, sizeof(double) * env_size, cudaMemcpyHostToDevice, s));
+        step(cudaMemcpyAsync(d_site, site, sizeof(double) * site_size, cudaMemcpyHostToDevice, s));
+    }
     step(cudaMemsetAsync(d_tmp, 0, sizeof(double) * std::max<uint64_t>(tmp_size, 1), s));
-    step(cudaMemsetAsync(d_out, 0, sizeof(double) * std::max<uint64_t>(out_size, 1), s));
+    if (out_size)
+        step(cudaMemsetAsync(d_out, 0, sizeof(double) * out_size, s));
     if (!ia_s.empty()) {
         step(cudaMemcpyAsync(d_ia, ia_s.data(), sizeof(BlkIadd) * ia_s.size(), cudaMemcpyHostToDevice, s));
         step(cudaMemcpyAsync(d_iag, ia_grp.data(), sizeof(int64_t) * ia_grp.size(), cudaMemcpyHostToDevice, s));
@@ -218,11 +230,24 @@ extern "C" int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, co
             step(cudaGetLastError());
         }
     }
-    if (out_size)
+    if (!on_device && out_size)
         step(cudaMemcpyAsync(out, d_out, sizeof(double) * out_size, cudaMemcpyDeviceToHost, s));
+    // the record tables live in host vectors of this call: finish before returning
     step(cudaStreamSynchronize(s));
     cleanup();
     if (e != cudaSuccess)
         return fail(B2G_ERR_CUDA, std::string("b2g_block_contract: ") + cudaGetErrorString(e));
     return B2G_OK;
+}
+
+extern "C" int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
+                                  uint64_t env_size, const double *site, uint64_t site_size,
+                                  uint64_t tmp_size, double *out, uint64_t out_size) {
+    return block_contract(ctx, seq, env, env_size, site, site_size, tmp_size, out, out_size, false);
+}
+
+extern "C" int b2g_block_contract_device(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
+                                         uint64_t env_size, const double *site, uint64_t site_size,
+                                         uint64_t tmp_size, double *out, uint64_t out_size) {
+    return block_contract(ctx, seq, env, env_size, site, site_size, tmp_size, out, out_size, true);
 }

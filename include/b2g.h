@@ -189,6 +189,12 @@ typedef struct {
 int b2g_block_contract(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
                        uint64_t env_size, const double *site, uint64_t site_size,
                        uint64_t tmp_size, double *out, uint64_t out_size);
+/* The same with env, site and out as DEVICE pointers (the environment stays
+ * resident between sites: the output can feed b2g_heff_create with
+ * ops_on_device = 1 or the next blocking without a host round trip). */
+int b2g_block_contract_device(b2g_context *ctx, const b2g_block_seq *seq, const double *env,
+                              uint64_t env_size, const double *site, uint64_t site_size,
+                              uint64_t tmp_size, double *out, uint64_t out_size);
 
 /*
  * sigma += scale * H_eff * psi in plain FP64 without allocating anything.

@@ -60,3 +60,22 @@ def test_gpu_blocking_matches_reference(ctx, path):
     # reproducible bit for bit
     out2 = contract(ctx, d, d["env"], d["site"], int(d["tmp_size"]), d["out"].size)
     assert np.array_equal(out, out2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", BLK, ids=IDS)
+def test_gpu_blocking_device_resident(ctx, path):
+    """b2g_block_contract_device (operands and output stay on the device) gives
+    the host entry's result bit for bit; the output then serves as an
+    operator blob on the device without a host round trip."""
+    torch = pytest.importorskip("torch")
+    from b2g.blocking import contract, contract_device
+    d = load(path)
+    host = contract(ctx, d, d["env"], d["site"], int(d["tmp_size"]), d["out"].size)
+    env = torch.from_numpy(np.ascontiguousarray(d["env"], dtype=np.float64)).cuda()
+    site = torch.from_numpy(np.ascontiguousarray(d["site"], dtype=np.float64)).cuda()
+    out = torch.full((max(d["out"].size, 1),), 7.0, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    contract_device(ctx, d, env, site, int(d["tmp_size"]), out)
+    ctx.synchronize()
+    assert np.array_equal(out.cpu().numpy()[:d["out"].size], host)
