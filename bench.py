@@ -417,6 +417,24 @@ def run_ours(args, rank, local_rank, world, dist):
                                                                - dprob.meta["davidson_energy"]),
                      "iterations": ndav, "fp64_products": r.n_apply_fp64,
                      "reduced_products": r.n_apply_mixed, "seconds": tdav}
+    # eight state-averaged roots (the batching form's root count): block
+    # Davidson, all new basis vectors of an iteration in one batched product
+    if not args.headline_only:
+        rng = np.random.default_rng(8)
+        g0 = np.ascontiguousarray(rng.standard_normal((8, dprob.psi_size)))
+        g0[0] = dprob.psi
+        multi = {}
+        for name in ("fp64", "tf32x3"):
+            g = g0.copy()
+            e8, ndav, nfl, tdav = dh.eigs_multi(dprob.diag, g, conv_thrd=dprob.meta["conv_thrd"], def_min=8,
+                                                def_max=48, form=FORMS[name])
+            r = dh.last_davidson
+            multi[name] = {"energies": [float(v) for v in e8], "iterations": ndav,
+                           "fp64_products": r.n_apply_fp64, "reduced_products": r.n_apply_mixed,
+                           "seconds": tdav}
+        multi["max_abs_root_diff_tf32x3_vs_fp64"] = float(
+            np.max(np.abs(np.array(multi["tf32x3"]["energies"]) - np.array(multi["fp64"]["energies"]))))
+        dav["eight_roots"] = multi
     dh.close()
     result["davidson"] = dav
     # ---- density-matrix truncation of the reference's converged psi at the

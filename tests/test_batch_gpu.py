@@ -77,3 +77,25 @@ def test_block_davidson_four_roots(problems, ctx, name, form):
         hx = oracle.replay(p.seq(), p.ops, guesses[i], p.sigma_size)
         assert np.linalg.norm(hx - e[i] * guesses[i]) ** 2 < 1e-9
     h.close()
+
+
+@pytest.mark.parametrize("name", ["hub16_su2_M250"])
+def test_eight_state_averaged_roots_mixed_vs_fp64(problems, ctx, name):
+    """Eight roots (the batching form's root count) on the reference's own
+    M=250 Hubbard H_eff: the TF32x3 block Davidson with FP64 defect
+    correction gives every root energy within 1e-8 of the FP64 block Davidson."""
+    p = problems[name]
+    h = b2g.EffectiveHamiltonian(ctx, p.seq(), p.ops, p.psi_size, p.sigma_size)
+    k = 8
+    rng = np.random.default_rng(8)
+    g0 = np.ascontiguousarray(rng.standard_normal((k, p.psi_size)))
+    g0[0] = p.psi
+    res = {}
+    for form in (b2g.FP64, b2g.TF32X3):
+        g = g0.copy()
+        e, ndav, nflop, tdav = h.eigs_multi(p.diag, g, conv_thrd=1e-10, def_min=k, def_max=48, form=form)
+        res[form] = (e, g)
+    e64, etf = res[b2g.FP64][0], res[b2g.TF32X3][0]
+    assert np.all(np.diff(e64) >= -1e-12)
+    assert np.max(np.abs(etf - e64)) <= 1e-8, (etf, e64)
+    h.close()
