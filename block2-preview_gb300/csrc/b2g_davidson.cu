@@ -189,7 +189,8 @@ __global__ void olsen_update(double *__restrict__ q, const double *__restrict__ 
 // y = x / sqrt(d[0])
 __global__ void normalize_into(double *__restrict__ y, const double *__restrict__ x,
                                const double *__restrict__ d, uint64_t n) {
-    const double f = 1.0 / sqrt(d[0]);
+    // a (numerically) zero vector becomes zero: the host drops it afterwards
+    const double f = d[0] > 1e-28 ? 1.0 / sqrt(d[0]) : 0.0;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         y[i] = x[i] * f;
@@ -595,21 +596,45 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             m = msig = def_min;
             vw = 0;
         }
-        // ---- Olsen corrections of the unconverged roots
-        int added = 0;
+        // ---- Olsen corrections of the unconverged roots, appended in order
+        // (Gram-Schmidt twice against the basis including the corrections
+        // appended before them) without a host round trip per root: each norm
+        // lands in dots[], a numerically zero correction is stored as a zero
+        // vector, and one read of the norms afterwards drops those
+        int added = 0, mp = m;
         for (int i = 0; i < k; i++) {
             const double thr = reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i]) : conv_thrd;
-            if (qq[i] < thr || m >= def_max)
+            if (qq[i] < thr || mp >= def_max)
                 continue;
             double *q = Q + (uint64_t)i * n, *x = X + (uint64_t)i * n;
             residual_olsen<<<g, 256, 0, st>>>(q, t, SX + (uint64_t)i * n, x, D, w + i, n, 1);
             dot_many(q, 1, x, sc + 2);
             dot_many(t, 1, x, sc + 3);
             olsen_update<<<g, 256, 0, st>>>(q, t, sc + 2, n);
-            const int r = append(q);
-            if (r < 0)
+            for (int pass = 0; pass < 2 && mp > 0; pass++) {
+                dot_many(B, mp, q, coef);
+                combine<<<g, 256, 0, st>>>(q, 1.0, B, n, mp, coef, -1.0, n);
+            }
+            dot_many(q, 1, q, dots + (mp - m));
+            normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)mp * n, q, dots + (mp - m), n);
+            mp++;
+        }
+        if (mp > m) {
+            std::vector<double> nr(mp - m);
+            if (!cuda_ok(cudaMemcpyAsync(nr.data(), dots, sizeof(double) * (mp - m), cudaMemcpyDeviceToHost, st),
+                         "norms") ||
+                !cuda_ok(cudaStreamSynchronize(st), "sync"))
                 goto done;
-            added += r;
+            for (int j = 0; j < mp - m; j++) {
+                if (!(nr[j] > 1e-28))
+                    continue;  // dropped (stored as zeros, never used)
+                if (m + added != m + j &&
+                    !cuda_ok(cudaMemcpyAsync(B + (uint64_t)(m + added) * n, B + (uint64_t)(m + j) * n,
+                                             sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "compact"))
+                    goto done;
+                added++;
+            }
+            m += added;
         }
         if (added == 0 && msig == m)
             break;  // no new direction: stagnated
