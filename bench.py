@@ -437,6 +437,10 @@ def run_ours(args, rank, local_rank, world, dist):
         dav["eight_roots"] = multi
     dh.close()
     result["davidson"] = dav
+    # ---- differentiation form: one adjoint (operator and ket gradients of
+    # <x|H_eff|y>, FP64) on this workload, next to the FP64 product
+    if not args.headline_only:
+        result["adjoint"] = adjoint_section(heff, prob, stream, dev, do_flush, args)
     # ---- density-matrix truncation of the reference's converged psi at the
     # n=24 M=1000 middle site (28 blocks, 2827 states): GPU vs the oracle's
     # numpy/LAPACK restatement, spectrum and discarded weight vs the reference
@@ -453,6 +457,44 @@ def run_ours(args, rank, local_rank, world, dist):
     heff.close()
     ctx.close()
     return result
+
+
+def adjoint_section(heff, prob, stream, dev, do_flush, args):
+    """Time b2g_heff_adjoint (both gradients) and the FP64 product on the same
+    H_eff with CUDA events on the library's stream (L2 flushed before each)."""
+    import torch
+
+    import b2g
+    rng = np.random.default_rng(12)
+    x = torch.from_numpy(rng.standard_normal(prob.sigma_size)).to(dev)
+    y = torch.from_numpy(prob.psi).to(dev)
+    gops = torch.zeros(prob.ops.size, dtype=torch.float64, device=dev)
+    gpsi = torch.zeros(prob.psi_size, dtype=torch.float64, device=dev)
+    sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+    nflop = heff.adjoint_nflop
+    torch.cuda.synchronize()
+    reps = max(2, min(args.steps, 5))
+
+    def timed(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            do_flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    ms_adj = timed(lambda: heff.adjoint(x, y, gops, gpsi))
+    ms_fwd = timed(lambda: heff.apply_ptr(y.data_ptr(), sig.data_ptr(), 1.0, b2g.FP64))
+    return {"form": "fp64", "ms": ms_adj, "tflops": nflop / ms_adj / 1e9,
+            "flop": nflop, "fp64_product_ms": ms_fwd,
+            "ratio_to_product": ms_adj / ms_fwd,
+            "note": "operator gradient + ket gradient of <x|H_eff|y>; median of "
+                    f"{reps} after one warm-up, L2 flushed; FP64 DFMA (GB300 has no FP64 tensor path)"}
 
 
 def truncation_section(ctx, cpu=True):

@@ -128,6 +128,11 @@ SIGNATURES = {
     "b2g_heff_diag_host": (C.c_int, [C.c_void_p, C.c_void_p]),
     "b2g_heff_apply_noalloc": (C.c_int, [C.POINTER(PairSeqC), C.c_void_p, C.c_uint64, C.c_void_p,
                                          C.c_uint64, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p]),
+    "b2g_heff_set_ops": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "b2g_heff_adjoint_prepare": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC)]),
+    "b2g_heff_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                   C.c_void_p]),
+    "b2g_heff_adjoint_mnk": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "b2g_heff_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "b2g_heff_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "b2g_heff_graph_count": (C.c_int, [C.c_void_p]),

@@ -74,6 +74,8 @@ class EffectiveHamiltonian:
         self.seq = seq
         ops = np.ascontiguousarray(ops, dtype=np.float64)
         self.psi_size, self.sigma_size = int(psi_size), int(sigma_size)
+        self.ops_size = int(ops.size)
+        self._adjoint_ready = False
         self._h = C.c_void_p()
         check(lib().b2g_heff_create(ctx.handle, C.byref(seq.c), ops.ctypes.data, ops.size, 0,
                                     self.psi_size, self.sigma_size, C.byref(self._h)))
@@ -200,6 +202,53 @@ class EffectiveHamiltonian:
         check(rc)
         self.last_davidson = res
         return energies, res.n_iter, self.nflop * (res.n_apply_fp64 + res.n_apply_mixed), tdav
+
+    # ---- differentiation form (no reference counterpart; see b2g.autodiff) ----
+    def set_ops(self, ops):
+        """Replace the operator values (same layout and size): a float64 numpy
+        array (host, synchronous) or a contiguous float64 CUDA tensor (copied on
+        the context stream)."""
+        if isinstance(ops, np.ndarray):
+            ops = np.ascontiguousarray(ops, dtype=np.float64)
+            if ops.size != self.ops_size:
+                raise ValueError("operator blob size does not match the effective Hamiltonian")
+            check(lib().b2g_heff_set_ops(self._h, ops.ctypes.data, 0))
+        else:
+            if ops.numel() != self.ops_size:
+                raise ValueError("operator blob size does not match the effective Hamiltonian")
+            if not (ops.is_cuda and ops.is_contiguous()):
+                raise TypeError("ops must be a contiguous CUDA tensor")
+            check(lib().b2g_heff_set_ops(self._h, _ptr(ops), 1))
+
+    def adjoint(self, x, y, grad_ops=None, grad_psi=None, scale: float = 1.0):
+        """Gradients of f = <x| H_eff |y> (CUDA tensors, FP64):
+        grad_ops += scale * df/dops, grad_psi += scale * H_eff^T x.  Either
+        output may be None.  Asynchronous on the context stream."""
+        if not self._adjoint_ready:
+            check(lib().b2g_heff_adjoint_prepare(self._h, C.byref(self.seq.c)))
+            self._adjoint_ready = True
+        if x.numel() != self.sigma_size or (y is not None and y.numel() != self.psi_size):
+            raise ValueError("bra/ket sizes do not match the effective Hamiltonian")
+        if grad_ops is not None and grad_ops.numel() != self.ops_size:
+            raise ValueError("grad_ops must hold ops_size doubles")
+        if grad_psi is not None and grad_psi.numel() != self.psi_size:
+            raise ValueError("grad_psi must hold psi_size doubles")
+        for t in (x, y, grad_ops, grad_psi):
+            if t is not None and not (t.is_cuda and t.is_contiguous()):
+                raise TypeError("adjoint buffers must be contiguous CUDA tensors")
+        check(lib().b2g_heff_adjoint(self._h, _ptr(x), None if y is None else _ptr(y), scale,
+                                     None if grad_ops is None else _ptr(grad_ops),
+                                     None if grad_psi is None else _ptr(grad_psi)))
+
+    @property
+    def adjoint_nflop(self) -> float:
+        """FLOP of one adjoint with both gradients (2 x multiply-adds)."""
+        if not self._adjoint_ready:
+            check(lib().b2g_heff_adjoint_prepare(self._h, C.byref(self.seq.c)))
+            self._adjoint_ready = True
+        v = C.c_double()
+        check(lib().b2g_heff_adjoint_mnk(self._h, C.byref(v)))
+        return 2.0 * v.value
 
     def close(self):
         if self._h:

@@ -286,6 +286,7 @@ int b2g_heff_destroy(b2g_heff *h) {
     cudaSetDevice(h->ctx->device);
     cudaStreamSynchronize(h->ctx->stream);
     clear_graphs(h);
+    free_adjoint(h);
     free_plan(h->plan);
     cudaFree(h->ops), cudaFree(h->ops32), cudaFree(h->psi32), cudaFree(h->work);
     cudaFree(h->simt_part);

@@ -274,6 +274,7 @@ struct ApplyGraph {
     uint64_t last = 0;    // LRU tick
 };
 constexpr size_t kMaxApplyGraphs = 64;
+struct AdjointPlan;   // the adjoint's schedule and work matrices (b2g_adjoint.cu)
 } // namespace b2g
 
 struct b2g_heff {
@@ -302,4 +303,9 @@ struct b2g_heff {
     bool graphs_on = true;  // replay repeated applies as CUDA graphs
     std::vector<b2g::ApplyGraph> graphs;
     uint64_t graph_tick = 0;
+    b2g::AdjointPlan *adj = nullptr;  // made by b2g_heff_adjoint_prepare
 };
+
+namespace b2g {
+void free_adjoint(b2g_heff *h);
+} // namespace b2g

@@ -214,6 +214,32 @@ int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops, uint64_t 
                            const double *psi, uint64_t psi_size, double *sigma,
                            uint64_t sigma_size, double scale, void *stream);
 
+/*
+ * Differentiation form (the adjoint of H_eff*psi).  No counterpart in the
+ * reference, which obtains energy derivatives only as reduced density
+ * matrices from its expectation sweeps (src/dmrg/sweep_algorithm.hpp,
+ * class Expect); the adjoint follows the pair semantics of
+ * BatchGEMMSeq::rotate (src/core/batch_gemm.hpp:893-902).
+ *
+ * b2g_heff_set_ops: replace the operator values of an H_eff (same layout and
+ *   size as created; host pointer when ops_on_device == 0, else a device
+ *   pointer that is copied).  The reduced-precision copies follow.
+ * b2g_heff_adjoint_prepare: build the adjoint schedule from the sequence the
+ *   H_eff was created from (host work, device tables and work matrices).
+ * b2g_heff_adjoint: for bra x (sigma_size) and ket y (psi_size), DEVICE
+ *   pointers, with f = <x| H_eff(ops) |y>:
+ *     grad_ops[i] += scale * df/dops[i]   (ops_size doubles, may be NULL)
+ *     grad_psi[j] += scale * df/dy[j] = scale * (H_eff^T x)[j]  (psi_size, may be NULL)
+ *   FP64, deterministic (no atomics), asynchronous on the context stream.
+ *   The gradient buffers must not overlap x, y or each other.
+ * b2g_heff_adjoint_mnk: multiply-adds of one adjoint with both gradients.
+ */
+int b2g_heff_set_ops(b2g_heff *h, const double *ops, int ops_on_device);
+int b2g_heff_adjoint_prepare(b2g_heff *h, const b2g_pair_seq *seq);
+int b2g_heff_adjoint(b2g_heff *h, const double *x, const double *y, double scale, double *grad_ops,
+                     double *grad_psi);
+int b2g_heff_adjoint_mnk(const b2g_heff *h, double *mnk);
+
 /* Per-kernel timing of b2g_heff_apply (CUDA events recorded on the context
  * stream around each phase when enabled; no work is skipped).  ms[0] =
  * GEMM0 phase, ms[1] = GEMM1 phase of the most recent apply (synchronizes). */

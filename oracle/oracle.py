@@ -199,3 +199,43 @@ def block_contract(rec, env, site, tmp_size, out_size):
         for r in range(rows):
             out[c + r * cn:c + r * cn + cols] += K[r]
     return out
+
+
+def _view_idx(off, rows, cols, ld):
+    return int(off) + np.arange(rows)[:, None] * int(ld) + np.arange(cols)[None, :]
+
+
+def adjoint(seq: PairSeq, ops, x, y):
+    """Gradients of f = <x| H_eff(ops) |y> in numpy (the checker of b2g_heff_adjoint).
+
+    H_eff(ops) y is the replay above: per pair, W = alpha0 y[a0:] op_b0(ops[b0:])
+    and sigma[c1:] += alpha1 op_a1(ops[a1:]) W (BatchGEMMSeq::rotate,
+    src/core/batch_gemm.hpp:893-902).  Differentiating f pair by pair gives
+    df/dA' = c x_p (y_p B')^T, df/dB' = c y_p^T (A'^T x_p), df/dy_p = c A'^T x_p B'^T
+    with c = alpha0 alpha1, A' = op_a1(A), B' = op_b0(B).  Returns (grad_ops, grad_y)."""
+    a = seq.arrays
+    ops = np.asarray(ops, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    gops = np.zeros_like(ops)
+    gy = np.zeros_like(y)
+    for p in range(seq.n):
+        m0, n0, k0 = int(a["m0"][p]), int(a["n0"][p]), int(a["k0"][p])
+        m1, n1, k1 = int(a["m1"][p]), int(a["n1"][p]), int(a["k1"][p])
+        c = float(a["alpha0"][p]) * float(a["alpha1"][p])
+        iy = _view_idx(a["a0"][p], m0, k0, a["lda0"][p])
+        ix = _view_idx(a["c1"][p], m1, n1, a["ldc1"][p])
+        tb, ta = int(a["tb0"][p]), int(a["ta1"][p])
+        ib = _view_idx(a["b0"][p], n0, k0, a["ldb0"][p]) if tb else _view_idx(a["b0"][p], k0, n0, a["ldb0"][p])
+        ia = _view_idx(a["a1"][p], k1, m1, a["lda1"][p]) if ta else _view_idx(a["a1"][p], m1, k1, a["lda1"][p])
+        Bp = ops[ib].T if tb else ops[ib]
+        Ap = ops[ia].T if ta else ops[ia]
+        yp, xp = y[iy], x[ix]
+        W = yp @ Bp
+        T = Ap.T @ xp
+        dA = c * (xp @ W.T)
+        dB = c * (yp.T @ T)
+        np.add.at(gops, ia, dA.T if ta else dA)
+        np.add.at(gops, ib, dB.T if tb else dB)
+        np.add.at(gy, iy, c * (T @ Bp.T))
+    return gops, gy
