@@ -118,3 +118,14 @@ def converged_energy(heff: EffectiveHamiltonian, ops, psi0, conv_thrd: float = 1
     """(E, psi) of the lowest eigenpair of H_eff(ops); E is differentiable in ops.
     psi0: host float64 initial guess (not modified)."""
     return ConvergedEnergy.apply(ops, heff, psi0, conv_thrd, max_iter)
+
+
+def chain_to_parameters(grad_ops, jac_idx, jac_val, jac_ptr):
+    """dE/dtheta_k = sum_i dE/dops_i dops_i/dtheta_k for Jacobian columns stored
+    sparse (column k: entries [jac_ptr[k], jac_ptr[k + 1]) of jac_idx / jac_val),
+    e.g. the integral -> operator Jacobian of the MPO and environment
+    construction at fixed MPS.  Returns a float64 numpy array (summed on the
+    host in column order: deterministic)."""
+    g = grad_ops.detach().cpu().numpy() if hasattr(grad_ops, "detach") else np.asarray(grad_ops)
+    jac_idx, jac_val, jac_ptr = np.asarray(jac_idx), np.asarray(jac_val), np.asarray(jac_ptr)
+    return np.array([float(g[jac_idx[a:b]] @ jac_val[a:b]) for a, b in zip(jac_ptr[:-1], jac_ptr[1:])])

@@ -64,6 +64,40 @@ def test_heff_is_symmetric(problems, name):
     assert rel(gy, hx) <= 1e-12
 
 
+def _grad_fixture():
+    import json
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "syn8_su2_s0_grad.npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    return z, meta
+
+
+RTOL_INTEGRAL = 1e-6   # dE/dh_pq, dE/d(pq|rs) vs the reference's own central differences
+
+
+def _check_integral_gradient(dE, z, meta):
+    fd = (z["e_plus"] - z["e_minus"]) / (2 * meta["delta"])
+    err = np.abs(dE - fd) / np.abs(fd)
+    assert err.max() <= RTOL_INTEGRAL, list(zip(meta["labels"], err))
+
+
+def test_oracle_integral_gradient_matches_reference_differences():
+    """dE/dtheta for one-electron h_pq and two-electron (pq|rs) elements at the
+    first site of the first sweep: the numpy adjoint at the reference's
+    converged eigenvector, chained through the reference's integral -> operator
+    Jacobian, equals the reference's central differences of its own energies."""
+    from b2g.autodiff import chain_to_parameters
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture()
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    v = z["psi_final"] / np.linalg.norm(z["psi_final"])
+    g, _ = oracle.adjoint(seq, z["ops"], v, v)
+    dE = chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"])
+    _check_integral_gradient(dE, z, meta)
+
+
 # ---------------------------------------------------------------- GPU
 
 torch = pytest.importorskip("torch")
@@ -213,4 +247,25 @@ def test_converged_energy_gradient_matches_finite_differences(problems, ctx, nam
         an = torch.dot(g, d).item()
         worst = max(worst, abs(an - fd) / max(abs(fd), 1e-12))
     assert worst <= RTOL_FD_EIG, worst
+    h.close()
+
+
+@pytest.mark.gpu
+def test_gpu_integral_gradient_matches_reference_differences(ctx):
+    """The same through the product path: device Davidson (FP64) for the site
+    energy, the adjoint kernel for dE/dops via torch.autograd, chained to the
+    integrals; against the reference's central differences (<= 1e-6)."""
+    from b2g.autodiff import chain_to_parameters, converged_energy
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture()
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    n = int(z["psi_size"])
+    h = b2g.EffectiveHamiltonian(ctx, seq, z["ops"], n, int(z["sigma_size"]))
+    ops = torch.from_numpy(np.array(z["ops"])).cuda().requires_grad_(True)
+    e, _ = converged_energy(h, ops, z["psi"], conv_thrd=1e-20)
+    e.backward()
+    assert e.item() == pytest.approx(meta["energy"], abs=1e-10)
+    dE = chain_to_parameters(ops.grad, z["jac_idx"], z["jac_val"], z["jac_ptr"])
+    _check_integral_gradient(dE, z, meta)
     h.close()
