@@ -44,6 +44,11 @@ struct Opts {
     int dump_site = -1;       // -1: middle site (n/2-1); -2: all sites
     bool with_data = true;    // false: structure only (no operator blob)
     bool dump_dm = true;      // density-matrix / split data after Davidson
+    // after the run: the reference's 1-/2-PDM of the final MPS, and for each
+    // listed FCIDUMP the H_eff at the final MPS's centre with that Hamiltonian
+    // (first site of one sweep on a copy of the final MPS: fixed MPS)
+    bool pdm = false;
+    vector<string> perturb;
 };
 
 static void mkdirs(const string &p) {
@@ -730,6 +735,83 @@ template <typename S> struct RecordingTF : TensorFunctions<S, double> {
     }
 };
 
+template <typename S>
+shared_ptr<MPO<S, double>> qc_mpo(const shared_ptr<HamiltonianQC<S, double>> &hamil) {
+    shared_ptr<MPO<S, double>> mpo = make_shared<MPOQC<S, double>>(hamil, QCTypes::Conventional, "HQC");
+    return make_shared<SimplifiedMPO<S, double>>(mpo, make_shared<RuleQC<S, double>>(), true, true,
+                                                 OpNamesSet({OpNames::R, OpNames::RD}));
+}
+
+// The reference's 1-/2-PDM of the final MPS (Expect with PDM1MPOQC /
+// PDM2MPOQC, the pattern of unit_test/test_npdm_n2_sto3g.cpp), and, per
+// perturbed Hamiltonian, the H_eff of the final MPS's centre built with it
+// (dumped by the first site of one sweep on a copy of the final MPS, before
+// its Davidson changes anything).
+template <typename S>
+void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>> &hamil,
+                       const shared_ptr<MPS<S, double>> &mps, int n) {
+    typedef double FL;
+    if (o.pdm) {
+        Writer w(o.out + "/pdm");
+        for (int k = 1; k <= 2; k++) {
+            shared_ptr<MPO<S, FL>> pmpo;
+            if (k == 1)
+                pmpo = make_shared<PDM1MPOQC<S, FL>>(hamil);
+            else
+                pmpo = make_shared<PDM2MPOQC<S, FL>>(hamil);
+            pmpo = make_shared<SimplifiedMPO<S, FL>>(pmpo, make_shared<RuleQC<S, FL>>(), true, true,
+                                                    OpNamesSet({OpNames::R, OpNames::RD}));
+            auto pme = make_shared<MovingEnvironment<S, FL, FL>>(pmpo, mps, mps, k == 1 ? "1PDM" : "2PDM");
+            pme->init_environments(false);
+            auto ex = make_shared<Expect<S, FL, FL>>(pme, (ubond_t)o.M, (ubond_t)o.M);
+            ex->solve(true, mps->center == 0);
+            if (k == 1) {
+                GMatrix<FL> dm = ex->get_1pdm_spatial();
+                vector<double> v(dm.data, dm.data + (size_t)n * n);
+                w.vec("dm1", v, "f8");
+                dm.deallocate();
+            } else {
+                shared_ptr<GTensor<FL>> dm2 = ex->get_2pdm_spatial();
+                w.vec("dm2", *dm2->data, "f8");
+            }
+            pmpo->deallocate();
+            pme->remove_partition_files();
+        }
+        w.scalar("n", n);
+        w.man.flush();
+    }
+    mps->save_data();
+    for (size_t k = 0; k < o.perturb.size(); k++) {
+        auto fd = make_shared<FCIDUMP<FL>>();
+        fd->read(o.perturb[k]);
+        vector<uint8_t> orbsym(n, 0);
+        auto ham2 = make_shared<HamiltonianQC<S, FL>>(hamil->vacuum, n, orbsym, fd);
+        shared_ptr<MPO<S, FL>> mpo2 = qc_mpo<S>(ham2);
+        auto xmps = mps->deep_copy("PT" + to_string(k));
+        auto dumper = make_shared<Dumper<S>>();
+        dumper->o = o;
+        dumper->o.dump_sweep = 0;
+        dumper->o.dump_site = xmps->center;
+        dumper->o.dump_dm = false;
+        dumper->o.out = o.out + "/perturb" + to_string(k);
+        auto me2 = make_shared<MovingEnvironment<S, FL, FL>>(mpo2, xmps, xmps, "PT" + to_string(k));
+        me2->init_environments(false);
+        me2->delayed_contraction = OpNamesSet::normal_ops();
+        me2->cached_contraction = true;
+        vector<ubond_t> bdims = {(ubond_t)o.M};
+        auto dmrg2 = make_shared<DMRG<S, FL, FL>>(me2, bdims, vector<FL>{0.0});
+        dmrg2->davidson_conv_thrds = o.dav_thrds;
+        dmrg2->noise_type = NoiseTypes::DensityMatrix;
+        dmrg2->iprint = 0;
+        dumper->d = dmrg2.get();
+        callback_() = dumper;
+        dmrg2->solve(1, xmps->center == 0, 0.0);
+        callback_() = make_shared<CallbackKernel>();
+        mpo2->deallocate();
+        me2->remove_partition_files();
+    }
+}
+
 template <typename S> int run(const Opts &o) {
     typedef double FL;
     Random::rand_seed(o.seed);
@@ -800,6 +882,8 @@ template <typename S> int run(const Opts &o) {
     w.vec("sweep_energies", es, "f8");
     w.vec("discarded_weights", dws, "f8");
     cout << setprecision(12) << "FINAL E = " << e << " T = " << tt << endl;
+    if (o.pdm || !o.perturb.empty())
+        fixed_mps_outputs<S>(o, hamil, mps, n);
     mps_info->deallocate();
     mpo->deallocate();
     me->remove_partition_files();
@@ -837,6 +921,13 @@ int main(int argc, char **argv) {
         else if (k == "--dump-sweep") o.dump_sweep = atoi(v.c_str());
         else if (k == "--dump-site") o.dump_site = atoi(v.c_str());
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
+        else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
+        else if (k == "--perturb") {
+            stringstream ss(v);
+            string x;
+            while (getline(ss, x, ','))
+                o.perturb.push_back(x);
+        }
         else {
             cerr << "unknown option " << k << endl;
             return 2;

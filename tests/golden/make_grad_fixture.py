@@ -20,6 +20,10 @@ The check (tests/test_adjoint.py): dE/dtheta_k = <dE/dops, jac_k> with dE/dops
 from the adjoint kernel (Hellmann-Feynman) equals the reference's central
 difference (e_plus_k - e_minus_k) / (2 delta).
 
+A second fixture, syn8_su2_conv_grad.npz, does the same at the converged MPS
+of a full run and pins the derivatives to the reference's own 1-/2-PDM
+(converged(), below).
+
 Usage (needs the reference harness; not run on GPU machines):
     python tests/golden/make_grad_fixture.py
 """
@@ -98,7 +102,20 @@ def run(tag, h, eri, ec):
     return pre_a, pre_s, post_a, post_s
 
 
-def main():
+def perturbed(h0, eri0, kind, idx, sgn):
+    h, eri = h0.copy(), eri0.copy()
+    if kind == "h":
+        p, q = idx
+        h[p, q] += sgn * DELTA
+        if p != q:
+            h[q, p] += sgn * DELTA
+    else:
+        for t in eri_orbit(*idx):
+            eri[t] += sgn * DELTA
+    return h, eri
+
+
+def first_site():
     h0, eri0, ec = synthetic_integrals(N, seed=0)
     base_a, base_s, base_post, base_post_s = run("base", h0, eri0, ec)
     labels, jac_idx, jac_val, jac_ptr, e_plus, e_minus = [], [], [], [0], [], []
@@ -107,15 +124,7 @@ def main():
     for kind, idx in params:
         runs = []
         for sgn in (+1, -1):
-            h, eri = h0.copy(), eri0.copy()
-            if kind == "h":
-                p, q = idx
-                h[p, q] += sgn * DELTA
-                if p != q:
-                    h[q, p] += sgn * DELTA
-            else:
-                for t in eri_orbit(*idx):
-                    eri[t] += sgn * DELTA
+            h, eri = perturbed(h0, eri0, kind, idx, sgn)
             tag = f"{kind}_{'_'.join(map(str, idx))}_{'p' if sgn > 0 else 'm'}"
             a, s, pa, ps = run(tag, h, eri, ec)
             for k in PAIR_FIELDS:
@@ -159,5 +168,109 @@ def main():
           f"linearity worst {lin_worst:.1e}")
 
 
+CONV_ARGS = ["--M", "60", "--sym", "su2", "--sweeps", "8", "--seed", "1234", "--dav", "1e-14",
+             "--dump-sweep", "99", "--pdm", "1"]
+
+
+def converged():
+    """syn8_su2_conv_grad.npz: at the converged MPS of an 8-sweep run, the
+    reference's 1-/2-PDM (Expect) and, for each parameter, the H_eff of the MPS
+    centre built with the perturbed integrals at that same (fixed) MPS.  The
+    energy derivative at fixed MPS is <Psi|dH/dtheta|Psi>, i.e. the PDM
+    element; the chain adjoint x Jacobian must reproduce it."""
+    h0, eri0, ec = synthetic_integrals(N, seed=0)
+    out = os.path.join(RAW, "grad", "conv")
+    if os.path.exists(out):
+        shutil.rmtree(out)
+    os.makedirs(out)
+    params = [("h", p) for p in H_PARAMS] + [("eri", p) for p in ERI_PARAMS]
+    dumps = [os.path.join(out, "base.FCIDUMP")]
+    write_fcidump(dumps[0], h0, eri0, ec, nelec=N)
+    for kind, idx in params:
+        for sgn in (+1, -1):
+            h, eri = perturbed(h0, eri0, kind, idx, sgn)
+            path = os.path.join(out, f"{kind}_{'_'.join(map(str, idx))}_{'p' if sgn > 0 else 'm'}.FCIDUMP")
+            write_fcidump(path, h, eri, ec, nelec=N)
+            dumps.append(path)
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
+    cmd = [HARNESS, "--ham", dumps[0], *CONV_ARGS, "--perturb", ",".join(dumps), "--threads", "1",
+           "--out", out]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    res_a, res_s = read_dump(os.path.join(out, "result"))
+    pdm_a, _ = read_dump(os.path.join(out, "pdm"))
+    dm1 = pdm_a["dm1"].reshape(N, N)
+    dm2 = pdm_a["dm2"].reshape(N, N, N, N)
+
+    def site(k):
+        d = os.path.join(out, f"perturb{k}")
+        (sd,) = [x for x in os.listdir(d) if x.startswith("sweep")]
+        return read_dump(os.path.join(d, sd))
+
+    base_a, base_s = site(0)
+    # the energy of the fixed MPS: the Rayleigh quotient of its centre tensor
+    # with the centre's H_eff (the reference's replay, restated by the oracle)
+    sys.path.insert(0, ROOT)
+    from b2g.capi import PairSeq
+    from oracle import oracle
+    psi = base_a["psi"]
+    sig = oracle.replay(PairSeq({k: base_a[k] for k in PAIR_FIELDS}), base_a["ops"], psi,
+                        int(base_s["sigma_size"]))
+    e_state = float(psi @ sig / (psi @ psi)) + ec
+    # energy identity fixes the 2-PDM convention: E = sum h dm1 + 1/2 sum (ij|kl) dm2[i,k,l,j]
+    e1 = float(np.einsum("ij,ij->", h0, dm1))
+    e2 = 0.5 * float(np.einsum("ijkl,iklj->", eri0, dm2))
+    print(f"E(MPS)={e_state:.12f}  sum h dm1 + 1/2 sum v dm2 = {e1 + e2 + ec:.12f} "
+          f"(last sweep energy {float(res_s['energy']):.12f})")
+    if abs(e1 + e2 + ec - e_state) > 1e-10:
+        raise RuntimeError("PDM energy identity does not hold with the assumed convention")
+    e_final = e_state
+    labels, jac_idx, jac_val, jac_ptr, expect = [], [], [], [0], []
+    lin_worst = 0.0
+    base_ops = to_base_layout(base_a, base_a)
+    for i, (kind, idx) in enumerate(params):
+        (ap, _), (am, _) = site(1 + 2 * i), site(2 + 2 * i)
+        for a in (ap, am):
+            for k in PAIR_FIELDS:
+                if k not in ("b0", "a1") and not np.array_equal(a[k], base_a[k]):
+                    raise RuntimeError(f"{kind}{idx}: pair structure differs ({k})")
+        op_p, op_m = to_base_layout(base_a, ap), to_base_layout(base_a, am)
+        d = (op_p - op_m) / (2 * DELTA)
+        lin = np.linalg.norm((op_p - base_ops) - (base_ops - op_m)) / max(np.linalg.norm(op_p - op_m), 1e-300)
+        lin_worst = max(lin_worst, lin)
+        nz = np.nonzero(np.abs(d) > 1e-9 * np.abs(d).max())[0]
+        if kind == "h":
+            p, q = idx
+            ex = dm1[p, q] + (dm1[q, p] if p != q else 0.0)
+        else:
+            ex = 0.5 * sum(dm2[i_, k_, l_, j_] for (i_, j_, k_, l_) in eri_orbit(*idx))
+        labels.append(f"{kind}{list(idx)}")
+        jac_idx.append(nz.astype(np.int64))
+        jac_val.append(d[nz])
+        jac_ptr.append(jac_ptr[-1] + nz.size)
+        expect.append(ex)
+        print(f"{labels[-1]}: jac nnz={nz.size} PDM derivative={ex:.12f} linearity {lin:.1e}")
+    meta = {"name": "syn8_su2_conv_grad", "kind": "integral_gradient_pdm",
+            "description": "synthetic ab initio n=8 N=8 (seed 0), SU(2), M=60, converged 8-sweep MPS "
+                           "(harness seed 1234): H_eff of the MPS centre, integral -> operator Jacobian "
+                           "at that fixed MPS, and the reference's 1-/2-PDM (Expect)",
+            "harness_args": CONV_ARGS, "delta": DELTA, "labels": labels, "energy": e_final,
+            "linearity_worst": lin_worst,
+            "pdm_convention": "E = sum_ij h_ij dm1[i,j] + 1/2 sum_ijkl (ij|kl) dm2[i,k,l,j] + E_core "
+                              "(spin-summed spatial PDMs of Expect::get_1pdm_spatial / get_2pdm_spatial)",
+            "param_convention": "h[p,q]: h_pq and h_qp move together; eri[p,q,r,s]: all eight "
+                                "symmetry-equivalent entries move together"}
+    path = os.path.join(HERE, "syn8_su2_conv_grad.npz")
+    np.savez_compressed(
+        path, **{k: base_a[k] for k in PAIR_FIELDS}, ops=base_ops, psi=base_a["psi"],
+        psi_size=np.int64(base_s["psi_size"]), sigma_size=np.int64(base_s["sigma_size"]),
+        jac_idx=np.concatenate(jac_idx), jac_val=np.concatenate(jac_val),
+        jac_ptr=np.array(jac_ptr, dtype=np.int64), pdm_derivative=np.array(expect), dm1=dm1, dm2=dm2,
+        meta=np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8))
+    print(f"-> {path} ({os.path.getsize(path)} bytes), linearity worst {lin_worst:.1e}")
+
+
 if __name__ == "__main__":
-    main()
+    first_site()
+    converged()

@@ -64,11 +64,11 @@ def test_heff_is_symmetric(problems, name):
     assert rel(gy, hx) <= 1e-12
 
 
-def _grad_fixture():
+def _grad_fixture(name="syn8_su2_s0_grad"):
     import json
     import os
     from conftest import GOLDEN
-    z = np.load(os.path.join(GOLDEN, "syn8_su2_s0_grad.npz"))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
     meta = json.loads(bytes(z["meta"]).decode())
     return z, meta
 
@@ -96,6 +96,28 @@ def test_oracle_integral_gradient_matches_reference_differences():
     g, _ = oracle.adjoint(seq, z["ops"], v, v)
     dE = chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"])
     _check_integral_gradient(dE, z, meta)
+
+
+def _check_pdm_derivative(dE, z, meta):
+    ref = z["pdm_derivative"]
+    err = np.abs(dE - ref) / np.abs(ref)
+    assert err.max() <= RTOL_INTEGRAL, list(zip(meta["labels"], err))
+
+
+def test_oracle_integral_gradient_matches_reference_pdm():
+    """At a converged MPS (fixed), dE/dh_pq and dE/d(pq|rs) from the numpy
+    adjoint at the MPS centre, chained through the reference's integral ->
+    operator Jacobian at that MPS, equal the reference's own 1-/2-PDM elements
+    (Expect; E = sum h dm1 + 1/2 sum (ij|kl) dm2[i,k,l,j], checked when the
+    fixture was made)."""
+    from b2g.autodiff import chain_to_parameters
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture("syn8_su2_conv_grad")
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    v = z["psi"] / np.linalg.norm(z["psi"])
+    g, _ = oracle.adjoint(seq, z["ops"], v, v)
+    _check_pdm_derivative(chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"]), z, meta)
 
 
 # ---------------------------------------------------------------- GPU
@@ -268,4 +290,23 @@ def test_gpu_integral_gradient_matches_reference_differences(ctx):
     assert e.item() == pytest.approx(meta["energy"], abs=1e-10)
     dE = chain_to_parameters(ops.grad, z["jac_idx"], z["jac_val"], z["jac_ptr"])
     _check_integral_gradient(dE, z, meta)
+    h.close()
+
+
+@pytest.mark.gpu
+def test_gpu_integral_gradient_matches_reference_pdm(ctx):
+    """The adjoint kernel at the converged MPS centre, chained to the integrals,
+    against the reference's 1-/2-PDM (<= 1e-6)."""
+    from b2g.autodiff import chain_to_parameters
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture("syn8_su2_conv_grad")
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    h = b2g.EffectiveHamiltonian(ctx, seq, z["ops"], int(z["psi_size"]), int(z["sigma_size"]))
+    v = torch.from_numpy(z["psi"] / np.linalg.norm(z["psi"])).cuda()
+    g = torch.zeros(z["ops"].size, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    h.adjoint(v, v, g, None)
+    ctx.synchronize()
+    _check_pdm_derivative(chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"]), z, meta)
     h.close()
