@@ -497,6 +497,28 @@ def adjoint_section(heff, prob, stream, dev, do_flush, args):
                     f"{reps} after one warm-up, L2 flushed; FP64 DFMA (GB300 has no FP64 tensor path)"}
 
 
+def adjoint_only(args, local_rank):
+    import torch
+
+    import b2g
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    prob = load_workload(args.workload)
+    ctx = b2g.Context(local_rank)
+    heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
+    flush = torch.empty(4 * L2_BYTES, dtype=torch.uint8, device=dev)
+
+    def do_flush():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    res = adjoint_section(heff, prob, stream, dev, do_flush, args)
+    heff.close()
+    ctx.close()
+    return res
+
+
 def truncation_section(ctx, cpu=True):
 
     from b2g.truncation import DensityMatrixLayout, split_density_matrix
@@ -567,6 +589,9 @@ def main():
     ap.add_argument("--truncation-only", action="store_true",
                     help="run only the density-matrix truncation section (GPU, no CPU leg); "
                          "for profiler runs")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the differentiation-form section (one FP64 adjoint and one FP64 "
+                         "product on the workload); for profiler runs")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline form (no other forms, batched roots or Davidson "
                          "sections); for profiler runs")
@@ -585,6 +610,10 @@ def main():
         import b2g
         print(json.dumps({"section": "truncation", **truncation_section(b2g.Context(local_rank), cpu=False)}),
               flush=True)
+        return
+    if args.adjoint_only:
+        print(json.dumps({"section": "adjoint", "workload": args.workload,
+                          **adjoint_only(args, local_rank)}), flush=True)
         return
     dist = None
     if world > 1:

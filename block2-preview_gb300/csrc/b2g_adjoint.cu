@@ -12,13 +12,18 @@
 //
 //   df/dA'_p = c_p x_p W'_p^T,   df/dB'_p = c_p y_p^T T_p,   df/dy_p = c_p T_p B'_p^T.
 //
-// The last is (H_eff^T x) restricted to block p.  Every term is a small dense
-// product C += coef op(A) op(B); four launches of one FP64 kernel compute the
-// distinct W' (GEMM0 products, de-duplicated as in the forward plan), the
-// distinct T, then the operator and ket gradients.  Destinations that overlap
-// in memory form one group, processed in a fixed order by one CTA (large
-// groups are first cut into disjoint destination tiles): the gradients are
-// deterministic and need no atomics.
+// The last is (H_eff^T x) restricted to block p.  The operator gradient is a
+// list of small dense products C += coef op(A) op(B); three launches of one
+// FP64 kernel compute the distinct W' (GEMM0 products, de-duplicated as in
+// the forward plan), the distinct T, then the operator gradient.
+// Destinations that overlap in memory form one group, processed in a fixed
+// order by one CTA (large groups are first cut into disjoint destination
+// tiles): deterministic, no atomics.  The ket gradient H_eff^T x is itself a
+// forward product, of the transposed pairs
+//   W'' = x_p op_b0(B)^T (m1 x k0),  grad_y[a0:] += c_p op_a1(A)^T W''
+// (GEMM0 reads x at c1, GEMM1 writes at a0, both operator flags flipped), so
+// it runs on the forward FP64 plan and kernels (simt_phase1/2: de-duplicated
+// GEMM0, owner-computes sigma regions, deterministic split-K).
 #include <algorithm>
 #include <map>
 #include <string>
@@ -51,11 +56,15 @@ struct AdjStage {
 };
 
 struct AdjointPlan {
-    AdjStage st[4];           // W', T, operator gradient, ket gradient
+    AdjStage st[3];           // W', T, operator gradient
     double *wbuf = nullptr, *tbuf = nullptr;
     uint64_t wsize = 0, tsize = 0;
     uint64_t ops_size = 0, psi_size = 0, sigma_size = 0;
     double mnk = 0;           // multiply-adds of one adjoint (both gradients)
+    // ket gradient H_eff^T x: the forward FP64 engine on the transposed pairs
+    DevicePlan tplan;
+    double *twork = nullptr, *tpart = nullptr;
+    uint64_t twork_size = 0, tpart_size = 0;
 };
 
 struct AdjSrc {
@@ -103,7 +112,9 @@ __global__ void __launch_bounds__(256) adj_items(const AdjItem *__restrict__ ite
                             }
                         }
                         __syncthreads();
-                        const int kn = min(kAT, e.K - k0);
+                        // a warp owns rows [4 w, 4 w + 4) of the tile: warps past the
+                        // item's last row skip the products (warp-uniform)
+                        const int kn = (i0 + (ti & ~3) < e.i1) ? min(kAT, e.K - k0) : 0;
                         for (int k = 0; k < kn; k++) {
                             const double a = As[k][ti];
                             acc0 = fma(a, Bs[k][tj], acc0);
@@ -196,13 +207,36 @@ void overlap_groups(HostStage &s, double max_mnk) {
         std::sort(g.begin(), g.end());
         double work = 0;
         bool frame = true;
-        const uint64_t base = lo[ord[i]];
         const int32_t ld = s.items[g[0]].ldc;
         for (size_t k : g) {
-            const AdjItem &e = s.items[k];
-            work += item_mnk(e);
-            if (e.ldc != ld || (e.c - base) % (uint64_t)ld + (uint64_t)e.N > (uint64_t)ld)
-                frame = false;
+            work += item_mnk(s.items[k]);
+            frame = frame && s.items[k].ldc == ld;
+        }
+        // the frame's row start: the lowest item need not start a row, so try
+        // the shifts that put some item's first column at column 0
+        uint64_t base = lo[ord[i]];
+        if (frame && work > max_mnk && g.size() >= 2) {
+            std::vector<uint64_t> shifts(1, 0);
+            for (size_t k : g)
+                shifts.push_back(((uint64_t)ld - (s.items[k].c - base) % (uint64_t)ld) % (uint64_t)ld);
+            std::sort(shifts.begin(), shifts.end());
+            shifts.erase(std::unique(shifts.begin(), shifts.end()), shifts.end());
+            frame = false;
+            for (uint64_t sh : shifts) {
+                if (sh > base)
+                    continue;
+                bool ok = true;
+                for (size_t k : g)
+                    if ((s.items[k].c - (base - sh)) % (uint64_t)ld + (uint64_t)s.items[k].N > (uint64_t)ld) {
+                        ok = false;
+                        break;
+                    }
+                if (ok) {
+                    base -= sh;
+                    frame = true;
+                    break;
+                }
+            }
         }
         if (!frame || work <= max_mnk || g.size() < 2) {
             for (size_t k : g)
@@ -251,6 +285,33 @@ int upload_stage(const HostStage &h, AdjStage &d, cudaStream_t s) {
     return B2G_OK;
 }
 
+template <typename T> int upload_vec(const std::vector<T> &v, T **dst, cudaStream_t s) {
+    *dst = nullptr;
+    if (v.empty())
+        return B2G_OK;
+    if (cudaMalloc((void **)dst, sizeof(T) * v.size()) != cudaSuccess) {
+        *dst = nullptr;
+        return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the adjoint's transposed plan");
+    }
+    B2G_CUDA_TRY(cudaMemcpyAsync(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return B2G_OK;
+}
+
+// the FP64 (CUDA-core) tables of a forward plan
+int upload_simt_plan(const HostPlan &hp, DevicePlan &p, cudaStream_t s) {
+    int rc;
+    if ((rc = upload_vec(hp.works, &p.works, s)) || (rc = upload_vec(hp.contribs, &p.contribs, s)) ||
+        (rc = upload_vec(hp.regions, &p.regions, s)) || (rc = upload_vec(hp.t1, &p.t1, s)) ||
+        (rc = upload_vec(hp.t2, &p.t2, s)) || (rc = upload_vec(hp.lists, &p.lists, s)) ||
+        (rc = upload_vec(hp.t2multi, &p.t2multi, s)))
+        return rc;
+    p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();
+    p.n_regions = (int64_t)hp.regions.size(), p.n_t1 = (int64_t)hp.t1.size();
+    p.n_t2 = (int64_t)hp.t2.size(), p.n_lists = (int64_t)hp.lists.size();
+    p.n_t2multi = (int64_t)hp.t2multi.size();
+    return B2G_OK;
+}
+
 cudaError_t launch_stage(const AdjStage &st, const AdjSrc &src, double *dst, double scale,
                          cudaStream_t s) {
     if (st.n_groups == 0)
@@ -269,6 +330,10 @@ void free_adjoint(b2g_heff *h) {
     for (AdjStage &s : p->st)
         cudaFree(s.items), cudaFree(s.grp);
     cudaFree(p->wbuf), cudaFree(p->tbuf);
+    DevicePlan &t = p->tplan;
+    cudaFree(t.works), cudaFree(t.contribs), cudaFree(t.regions), cudaFree(t.t1), cudaFree(t.t2);
+    cudaFree(t.lists), cudaFree(t.t2multi);
+    cudaFree(p->twork), cudaFree(p->tpart);
     delete p;
     h->adj = nullptr;
 }
@@ -309,7 +374,7 @@ int b2g_heff_adjoint_prepare(b2g_heff *h, const b2g_pair_seq *seq) {
     B2G_CUDA_TRY(cudaStreamSynchronize(s));
     free_adjoint(h);
     const int64_t n = seq->n_pairs;
-    HostStage hw, ht, hg, hy;
+    HostStage hw, ht, hg;
     std::map<std::tuple<uint64_t, uint64_t, int, int, int, int, int, int>, uint64_t> wkey;
     std::map<std::tuple<uint64_t, uint64_t, int, int, int, int, int, int>, uint64_t> tkey;
     uint64_t wsize = 0, tsize = 0;
@@ -376,20 +441,36 @@ int b2g_heff_adjoint_prepare(b2g_heff *h, const b2g_pair_seq *seq) {
         }
         b.i0 = 0, b.i1 = b.M, b.j0 = 0, b.j1 = b.N;
         hg.items.push_back(b);
-        AdjItem y{};   // ket gradient dy_p (m0 x k0) = T op_b0(B)^T
-        y.coef = coef, y.c = seq->a0[p], y.ldc = seq->lda0[p];
-        y.M = m0, y.N = k0, y.K = n0;
-        y.a = toff[p], y.lda = n0, y.ta = 0, y.asrc = kSrcT;
-        y.b = seq->b0[p], y.ldb = seq->ldb0[p], y.tb = seq->tb0[p] ? 0 : 1, y.bsrc = kSrcOps;
-        y.i0 = 0, y.i1 = y.M, y.j0 = 0, y.j1 = y.N;
-        hy.items.push_back(y);
-        mnk += (double)m1 * k1 * n1 + (double)k0 * n0 * m0 + (double)m0 * k0 * n0;
+        mnk += (double)m1 * k1 * n1 + (double)k0 * n0 * m0;
     }
+    // the transposed pairs (ket gradient = forward product of these with psi := x)
+    std::vector<int32_t> t_tb0(n), t_m0(n), t_n0(n), t_k0(n), t_lda0(n), t_ldb0(n);
+    std::vector<int32_t> t_ta1(n), t_m1(n), t_n1(n), t_k1(n), t_lda1(n), t_ldc1(n);
+    std::vector<double> t_al0(n), t_al1(n);
+    std::vector<uint64_t> t_a0(n), t_b0(n), t_a1(n), t_c1(n);
+    for (int64_t p = 0; p < n; p++) {
+        t_tb0[p] = seq->tb0[p] ? 0 : 1, t_m0[p] = seq->m1[p], t_k0[p] = seq->n1[p], t_n0[p] = seq->k0[p];
+        t_lda0[p] = seq->ldc1[p], t_ldb0[p] = seq->ldb0[p], t_a0[p] = seq->c1[p], t_b0[p] = seq->b0[p];
+        t_ta1[p] = seq->ta1[p] ? 0 : 1, t_m1[p] = seq->m0[p], t_k1[p] = seq->m1[p], t_n1[p] = seq->k0[p];
+        t_lda1[p] = seq->lda1[p], t_ldc1[p] = seq->lda0[p], t_a1[p] = seq->a1[p], t_c1[p] = seq->a0[p];
+        t_al0[p] = seq->alpha0[p], t_al1[p] = seq->alpha1[p];
+    }
+    b2g_pair_seq tseq;
+    tseq.n_pairs = n;
+    tseq.tb0 = t_tb0.data(), tseq.m0 = t_m0.data(), tseq.n0 = t_n0.data(), tseq.k0 = t_k0.data();
+    tseq.lda0 = t_lda0.data(), tseq.ldb0 = t_ldb0.data(), tseq.ta1 = t_ta1.data(), tseq.m1 = t_m1.data();
+    tseq.n1 = t_n1.data(), tseq.k1 = t_k1.data(), tseq.lda1 = t_lda1.data(), tseq.ldc1 = t_ldc1.data();
+    tseq.alpha0 = t_al0.data(), tseq.alpha1 = t_al1.data();
+    tseq.a0 = t_a0.data(), tseq.b0 = t_b0.data(), tseq.a1 = t_a1.data(), tseq.c1 = t_c1.data();
+    HostPlan thp;
+    int trc = build_plan(&tseq, h->ops_size, h->sigma_size, h->psi_size, thp);
+    if (trc != B2G_OK)
+        return trc;
+    mnk += thp.mnk_exec;
     // every operand of every item inside its buffer (nothing reaches the GPU unchecked)
     const uint64_t sizes[kNumSrc] = {h->ops_size, h->psi_size, h->sigma_size, wsize, tsize};
-    const struct { const HostStage *s; uint64_t dst; const char *name; } checks[4] = {
-        {&hw, wsize, "W"}, {&ht, tsize, "T"}, {&hg, h->ops_size, "operator gradient"},
-        {&hy, h->psi_size, "ket gradient"}};
+    const struct { const HostStage *s; uint64_t dst; const char *name; } checks[3] = {
+        {&hw, wsize, "W"}, {&ht, tsize, "T"}, {&hg, h->ops_size, "operator gradient"}};
     for (const auto &c : checks)
         for (size_t i = 0; i < c.s->items.size(); i++)
             if (!item_ok(c.s->items[i], sizes, c.dst))
@@ -399,25 +480,26 @@ int b2g_heff_adjoint_prepare(b2g_heff *h, const b2g_pair_seq *seq) {
     single_groups(ht);
     // no group above 1/4096 of a stage's work (2 CTAs on each of 152 SMs,
     // about 13 groups each) unless its items cannot be tiled
-    double wg = 0, wy = 0;
+    double wg = 0;
     for (const AdjItem &e : hg.items)
         wg += item_mnk(e);
-    for (const AdjItem &e : hy.items)
-        wy += item_mnk(e);
     overlap_groups(hg, wg / 4096.0);
-    overlap_groups(hy, wy / 4096.0);
     AdjointPlan *ap = new AdjointPlan();
     h->adj = ap;
     ap->wsize = wsize, ap->tsize = tsize, ap->mnk = mnk;
     ap->ops_size = h->ops_size, ap->psi_size = h->psi_size, ap->sigma_size = h->sigma_size;
     int rc;
     if ((rc = upload_stage(hw, ap->st[0], s)) || (rc = upload_stage(ht, ap->st[1], s)) ||
-        (rc = upload_stage(hg, ap->st[2], s)) || (rc = upload_stage(hy, ap->st[3], s))) {
+        (rc = upload_stage(hg, ap->st[2], s)) || (rc = upload_simt_plan(thp, ap->tplan, s))) {
         free_adjoint(h);
         return rc;
     }
+    ap->twork_size = thp.work_size;
+    ap->tpart_size = (uint64_t)4 * 256 * thp.t2_part_tiles;
     if ((wsize && cudaMalloc(&ap->wbuf, sizeof(double) * wsize) != cudaSuccess) ||
-        (tsize && cudaMalloc(&ap->tbuf, sizeof(double) * tsize) != cudaSuccess)) {
+        (tsize && cudaMalloc(&ap->tbuf, sizeof(double) * tsize) != cudaSuccess) ||
+        (ap->twork_size && cudaMalloc(&ap->twork, sizeof(double) * ap->twork_size) != cudaSuccess) ||
+        (ap->tpart_size && cudaMalloc(&ap->tpart, sizeof(double) * ap->tpart_size) != cudaSuccess)) {
         free_adjoint(h);
         return fail(B2G_ERR_NOMEM, "cudaMalloc failed for the adjoint work matrices");
     }
@@ -440,19 +522,24 @@ int b2g_heff_adjoint(b2g_heff *h, const double *x, const double *y, double scale
     const AdjointPlan &p = *h->adj;
     cudaStream_t s = h->ctx->stream;
     AdjSrc src{{h->ops, y, x, p.wbuf, p.tbuf}};
-    if (p.tsize) {
-        B2G_CUDA_TRY(cudaMemsetAsync(p.tbuf, 0, sizeof(double) * p.tsize, s));
-        B2G_CUDA_TRY(launch_stage(p.st[1], src, p.tbuf, 1.0, s));
-    }
     if (grad_ops != nullptr) {
+        if (p.tsize) {
+            B2G_CUDA_TRY(cudaMemsetAsync(p.tbuf, 0, sizeof(double) * p.tsize, s));
+            B2G_CUDA_TRY(launch_stage(p.st[1], src, p.tbuf, 1.0, s));
+        }
         if (p.wsize) {
             B2G_CUDA_TRY(cudaMemsetAsync(p.wbuf, 0, sizeof(double) * p.wsize, s));
             B2G_CUDA_TRY(launch_stage(p.st[0], src, p.wbuf, 1.0, s));
         }
         B2G_CUDA_TRY(launch_stage(p.st[2], src, grad_ops, scale, s));
     }
-    if (grad_psi != nullptr)
-        B2G_CUDA_TRY(launch_stage(p.st[3], src, grad_psi, scale, s));
+    if (grad_psi != nullptr) {
+        RootStrides rs;
+        rs.nroots = 1, rs.psi = p.sigma_size, rs.sigma = p.psi_size;
+        rs.work = p.twork_size, rs.part = p.tpart_size;
+        B2G_CUDA_TRY(launch_simt_phase1<double>(p.tplan, h->ops, x, p.twork, rs, s));
+        B2G_CUDA_TRY(launch_simt_phase2<double>(p.tplan, h->ops, p.twork, grad_psi, p.tpart, scale, rs, s));
+    }
     return B2G_OK;
 }
 
