@@ -49,6 +49,7 @@ struct Opts {
     // (first site of one sweep on a copy of the final MPS: fixed MPS)
     bool pdm = false;
     vector<string> perturb;
+    int perturb_site = -1;    // centre moved here first (-1: n/2 - 1)
 };
 
 static void mkdirs(const string &p) {
@@ -742,15 +743,54 @@ shared_ptr<MPO<S, double>> qc_mpo(const shared_ptr<HamiltonianQC<S, double>> &ha
                                                  OpNamesSet({OpNames::R, OpNames::RD}));
 }
 
-// The reference's 1-/2-PDM of the final MPS (Expect with PDM1MPOQC /
-// PDM2MPOQC, the pattern of unit_test/test_npdm_n2_sto3g.cpp), and, per
-// perturbed Hamiltonian, the H_eff of the final MPS's centre built with it
-// (dumped by the first site of one sweep on a copy of the final MPS, before
-// its Davidson changes anything).
+// Per perturbed Hamiltonian, the H_eff at one site of the final MPS built with
+// it (a copy of the final MPS with its canonical centre moved to that site,
+// dumped by a one-site sweep before its Davidson changes anything); then the
+// reference's 1-/2-PDM of the final MPS (Expect with PDM1MPOQC / PDM2MPOQC,
+// the pattern of unit_test/test_npdm_n2_sto3g.cpp).
 template <typename S>
 void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>> &hamil,
                        const shared_ptr<MPS<S, double>> &mps, int n) {
     typedef double FL;
+    mps->save_data();
+    for (size_t k = 0; k < o.perturb.size(); k++) {
+        auto fd = make_shared<FCIDUMP<FL>>();
+        fd->read(o.perturb[k]);
+        vector<uint8_t> orbsym(n, 0);
+        auto ham2 = make_shared<HamiltonianQC<S, FL>>(hamil->vacuum, n, orbsym, fd);
+        shared_ptr<MPO<S, FL>> mpo2 = qc_mpo<S>(ham2);
+        auto xmps = mps->deep_copy("PT" + to_string(k));
+        // walk the centre from the left end to the requested site with a
+        // sweep whose Davidson stops at its initial guess (the current
+        // two-site wavefunction): each split keeps every state (the MPS is
+        // already truncated to M), so the state stays the converged one
+        const int target = o.perturb_site >= 0 ? o.perturb_site : n / 2 - 1;
+        if (xmps->center != 0)
+            throw runtime_error("fixed-MPS perturbation expects the final MPS centre at site 0");
+        auto dumper = make_shared<Dumper<S>>();
+        dumper->o = o;
+        dumper->o.dump_sweep = 0;
+        dumper->o.dump_site = target;
+        dumper->o.dump_dm = false;
+        dumper->o.out = o.out + "/perturb" + to_string(k);
+        auto me2 = make_shared<MovingEnvironment<S, FL, FL>>(mpo2, xmps, xmps, "PT" + to_string(k));
+        me2->init_environments(false);
+        me2->delayed_contraction = OpNamesSet::normal_ops();
+        me2->cached_contraction = true;
+        vector<ubond_t> bdims = {(ubond_t)o.M};
+        auto dmrg2 = make_shared<DMRG<S, FL, FL>>(me2, bdims, vector<FL>{0.0});
+        dmrg2->davidson_conv_thrds = vector<FL>{1e10};
+        dmrg2->noise_type = NoiseTypes::DensityMatrix;
+        dmrg2->iprint = 0;
+        dmrg2->sweep_start_site = 0;
+        dmrg2->sweep_end_site = target + 2;
+        dumper->d = dmrg2.get();
+        callback_() = dumper;
+        dmrg2->solve(1, true, 0.0);
+        callback_() = make_shared<CallbackKernel>();
+        mpo2->deallocate();
+        me2->remove_partition_files();
+    }
     if (o.pdm) {
         Writer w(o.out + "/pdm");
         for (int k = 1; k <= 2; k++) {
@@ -779,36 +819,6 @@ void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>>
         }
         w.scalar("n", n);
         w.man.flush();
-    }
-    mps->save_data();
-    for (size_t k = 0; k < o.perturb.size(); k++) {
-        auto fd = make_shared<FCIDUMP<FL>>();
-        fd->read(o.perturb[k]);
-        vector<uint8_t> orbsym(n, 0);
-        auto ham2 = make_shared<HamiltonianQC<S, FL>>(hamil->vacuum, n, orbsym, fd);
-        shared_ptr<MPO<S, FL>> mpo2 = qc_mpo<S>(ham2);
-        auto xmps = mps->deep_copy("PT" + to_string(k));
-        auto dumper = make_shared<Dumper<S>>();
-        dumper->o = o;
-        dumper->o.dump_sweep = 0;
-        dumper->o.dump_site = xmps->center;
-        dumper->o.dump_dm = false;
-        dumper->o.out = o.out + "/perturb" + to_string(k);
-        auto me2 = make_shared<MovingEnvironment<S, FL, FL>>(mpo2, xmps, xmps, "PT" + to_string(k));
-        me2->init_environments(false);
-        me2->delayed_contraction = OpNamesSet::normal_ops();
-        me2->cached_contraction = true;
-        vector<ubond_t> bdims = {(ubond_t)o.M};
-        auto dmrg2 = make_shared<DMRG<S, FL, FL>>(me2, bdims, vector<FL>{0.0});
-        dmrg2->davidson_conv_thrds = o.dav_thrds;
-        dmrg2->noise_type = NoiseTypes::DensityMatrix;
-        dmrg2->iprint = 0;
-        dumper->d = dmrg2.get();
-        callback_() = dumper;
-        dmrg2->solve(1, xmps->center == 0, 0.0);
-        callback_() = make_shared<CallbackKernel>();
-        mpo2->deallocate();
-        me2->remove_partition_files();
     }
 }
 
@@ -922,6 +932,7 @@ int main(int argc, char **argv) {
         else if (k == "--dump-site") o.dump_site = atoi(v.c_str());
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
         else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
+        else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
         else if (k == "--perturb") {
             stringstream ss(v);
             string x;

@@ -169,13 +169,15 @@ def first_site():
 
 
 CONV_ARGS = ["--M", "60", "--sym", "su2", "--sweeps", "8", "--seed", "1234", "--dav", "1e-14",
-             "--dump-sweep", "99", "--pdm", "1"]
+             "--dump-sweep", "99", "--pdm", "1", "--perturb-site", "3"]
 
 
 def converged():
     """syn8_su2_conv_grad.npz: at the converged MPS of an 8-sweep run, the
-    reference's 1-/2-PDM (Expect) and, for each parameter, the H_eff of the MPS
-    centre built with the perturbed integrals at that same (fixed) MPS.  The
+    reference's 1-/2-PDM (Expect) and, for each parameter, the H_eff of the
+    middle site (sites 3-4) built with the perturbed integrals at that same
+    (fixed) MPS -- the harness walks the canonical centre there with a sweep
+    whose Davidson keeps its initial guess.  The
     energy derivative at fixed MPS is <Psi|dH/dtheta|Psi>, i.e. the PDM
     element; the chain adjoint x Jacobian must reproduce it."""
     h0, eri0, ec = synthetic_integrals(N, seed=0)
@@ -253,7 +255,7 @@ def converged():
         print(f"{labels[-1]}: jac nnz={nz.size} PDM derivative={ex:.12f} linearity {lin:.1e}")
     meta = {"name": "syn8_su2_conv_grad", "kind": "integral_gradient_pdm",
             "description": "synthetic ab initio n=8 N=8 (seed 0), SU(2), M=60, converged 8-sweep MPS "
-                           "(harness seed 1234): H_eff of the MPS centre, integral -> operator Jacobian "
+                           "(harness seed 1234): H_eff of the middle site (3-4), integral -> operator Jacobian "
                            "at that fixed MPS, and the reference's 1-/2-PDM (Expect)",
             "harness_args": CONV_ARGS, "delta": DELTA, "labels": labels, "energy": e_final,
             "linearity_worst": lin_worst,
