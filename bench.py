@@ -494,7 +494,35 @@ def adjoint_section(heff, prob, stream, dev, do_flush, args):
             "flop": nflop, "fp64_product_ms": ms_fwd,
             "ratio_to_product": ms_adj / ms_fwd,
             "note": "operator gradient + ket gradient of <x|H_eff|y>; median of "
-                    f"{reps} after one warm-up, L2 flushed; FP64 DFMA (GB300 has no FP64 tensor path)"}
+                    f"{reps} after one warm-up, L2 flushed; FP64 DFMA (GB300 has no FP64 tensor path)",
+            "integral_gradient": integral_gradient_check(heff.ctx, dev)}
+
+
+def integral_gradient_check(ctx, dev):
+    """dE/dh_pq and dE/d(pq|rs) at the middle site of a converged n=8 SU(2) MPS:
+    the adjoint kernel at the site wavefunction, chained through the
+    reference's integral -> operator Jacobian at that MPS, against the
+    reference's own 1-/2-PDM elements (fixture made by the reference harness)."""
+    import torch
+
+    import b2g
+    from b2g.autodiff import chain_to_parameters
+    from b2g.problem import PAIR_FIELDS
+    z = np.load(os.path.join(ROOT, "tests", "golden", "syn8_su2_conv_grad.npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    h = b2g.EffectiveHamiltonian(ctx, b2g.PairSeq({k: z[k] for k in PAIR_FIELDS}), z["ops"],
+                                 int(z["psi_size"]), int(z["sigma_size"]))
+    v = torch.from_numpy(z["psi"] / np.linalg.norm(z["psi"])).to(dev)
+    g = torch.zeros(z["ops"].size, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    h.adjoint(v, v, g, None)
+    ctx.synchronize()
+    dE = chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"])
+    h.close()
+    err = np.abs(dE - z["pdm_derivative"]) / np.abs(z["pdm_derivative"])
+    return {"workload": "syn8_su2_conv_grad (n=8 SU(2) M=60, middle site, 3250 pairs)",
+            "parameters": meta["labels"], "max_rel_err_vs_reference_pdm": float(err.max()),
+            "bound": 1e-6}
 
 
 def adjoint_only(args, local_rank):
