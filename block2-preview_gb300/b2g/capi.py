@@ -154,6 +154,10 @@ SIGNATURES = {
     "b2g_wfn_blocks": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_uint32,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                  C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
+    "b2g_wfn_connection": (C.c_int, [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "b2g_dm_truncate": (C.c_int, [C.c_void_p, C.POINTER(DmLayoutC), C.c_void_p, C.c_int, C.c_double,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.POINTER(DmResultC)]),

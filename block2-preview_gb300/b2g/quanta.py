@@ -105,3 +105,48 @@ def wavefunction_blocks(sym, bra, ket, dq, wfn=True, align=1):
                                C.byref(nb), C.byref(tot)))
     n = nb.value
     return q[:n].copy(), r[:n].copy(), c[:n].copy(), sh[:n].copy(), tot.value
+
+
+class OpInfosC(C.Structure):
+    _fields_ = [("n", C.c_int32), ("dq", C.c_void_p), ("fermion", C.c_void_p), ("start", C.c_void_p),
+                ("quanta", C.c_void_p)]
+
+
+def _ops(dq, fermion, start, q):
+    arrs = (np.ascontiguousarray(dq, dtype=np.uint64), np.ascontiguousarray(fermion, dtype=np.int32),
+            np.ascontiguousarray(start, dtype=np.int32), np.ascontiguousarray(q, dtype=np.uint64))
+    if arrs[2].size != arrs[0].size + 1 or arrs[1].size != arrs[0].size:
+        raise ValueError("operator infos: start must have n + 1 entries and fermion n")
+    return OpInfosC(arrs[0].size, *(a.ctypes.data for a in arrs)), arrs
+
+
+def wfn_connection(sym, cdq, vdq, opdq, sub_conj, sub_q, left, right, ket_q, bra_q):
+    """ConnectionInfo::initialize_wfn (sparse_matrix.hpp:163-292) through
+    b2g_wfn_connection.  left / right: (dq, fermion, start, quanta) arrays of
+    the operator infos.  Returns a dict n (5), idx, stride, factor, ia, ib, ic."""
+    sc = np.ascontiguousarray(sub_conj, dtype=np.int32)
+    sq = np.ascontiguousarray(sub_q, dtype=np.uint64)
+    kq = np.ascontiguousarray(ket_q, dtype=np.uint64)
+    bq = np.ascontiguousarray(bra_q, dtype=np.uint64)
+    lo, keep_l = _ops(*left)
+    ro, keep_r = _ops(*right)
+    n5 = np.zeros(5, dtype=np.int32)
+    idx = np.zeros(max(1, sc.size), dtype=np.uint32)
+    nc = C.c_int64()
+    cap = 0
+    while True:
+        stride = np.zeros(max(1, cap), dtype=np.uint64)
+        factor = np.zeros(max(1, cap))
+        ia, ib, ic = (np.zeros(max(1, cap), dtype=np.uint32) for _ in range(3))
+        rc = lib().b2g_wfn_connection(sym, C.c_uint64(cdq), C.c_uint64(vdq), C.c_uint64(opdq), sc.size,
+                                      sc.ctypes.data, sq.ctypes.data, C.byref(lo), C.byref(ro), kq.size,
+                                      kq.ctypes.data, bq.size, bq.ctypes.data, n5.ctypes.data,
+                                      idx.ctypes.data, stride.ctypes.data, factor.ctypes.data,
+                                      ia.ctypes.data, ib.ctypes.data, ic.ctypes.data, cap, C.byref(nc))
+        if rc != 0 and nc.value > cap:
+            cap = nc.value
+            continue
+        check(rc)
+        m = nc.value
+        return {"n": n5, "idx": idx[:sc.size], "stride": stride[:m], "factor": factor[:m],
+                "ia": ia[:m], "ib": ib[:m], "ic": ic[:m]}

@@ -8,7 +8,11 @@
 //     (src/core/state_info.hpp:160-310);
 //   * SparseMatrixInfo::initialize for an operator or a wavefunction and
 //     initialize_block_shifts / get_total_memory
-//     (src/core/sparse_matrix.hpp:617-630, 727-757, 804-820).
+//     (src/core/sparse_matrix.hpp:617-630, 727-757, 804-820);
+//   * the wavefunction connection info of an effective Hamiltonian
+//     (ConnectionInfo::initialize_wfn, src/core/sparse_matrix.hpp:163-292)
+//     with SU(2) recoupling factors (9j symbols from Racah's 6j formula,
+//     transposition factors) computed in long double.
 // The label layouts and the carry/borrow behaviour of the packed arithmetic
 // are part of the reference's data format (labels are compared as raw 64-bit
 // words and stored in block lists), so the word-level operations are the
@@ -186,6 +190,161 @@ int blocks(const b2g_state_info *bra, const b2g_state_info *ket, uint64_t dq, bo
     return B2G_OK;
 }
 
+// ---- SU(2) recoupling coefficients (spins given as 2j), in long double
+struct Recoupling {
+    long double fact[200];
+    Recoupling() {
+        fact[0] = 1.0L;
+        for (int i = 1; i < 200; i++)
+            fact[i] = fact[i - 1] * (long double)i;
+    }
+    static bool tri(int a, int b, int c) {
+        return !((a + b + c) & 1) && c <= a + b && c >= (a > b ? a - b : b - a);
+    }
+    // triangle coefficient Delta(abc) = sqrt((a+b-c)! (a-b+c)! (-a+b+c)! / (a+b+c+1)!)
+    long double delta(int a, int b, int c) const {
+        return sqrtl(fact[(a + b - c) / 2] * fact[(a - b + c) / 2] * fact[(-a + b + c) / 2] /
+                     fact[(a + b + c) / 2 + 1]);
+    }
+    // 6j symbol {a b c; d e f} by Racah's single-sum formula
+    long double sixj(int a, int b, int c, int d, int e, int f) const {
+        if (!tri(a, b, c) || !tri(a, e, f) || !tri(d, b, f) || !tri(d, e, c))
+            return 0.0L;
+        const int t1 = (a + b + c) / 2, t2 = (a + e + f) / 2, t3 = (d + b + f) / 2, t4 = (d + e + c) / 2;
+        const int u1 = (a + b + d + e) / 2, u2 = (b + c + e + f) / 2, u3 = (a + c + d + f) / 2;
+        const int lo = std::max(std::max(t1, t2), std::max(t3, t4)), hi = std::min(u1, std::min(u2, u3));
+        long double sum = 0.0L;
+        for (int t = lo; t <= hi; t++) {
+            const long double term = fact[t + 1] / (fact[t - t1] * fact[t - t2] * fact[t - t3] * fact[t - t4] *
+                                                    fact[u1 - t] * fact[u2 - t] * fact[u3 - t]);
+            sum += (t & 1) ? -term : term;
+        }
+        return delta(a, b, c) * delta(a, e, f) * delta(d, b, f) * delta(d, e, c) * sum;
+    }
+    // 9j symbol {a b c; d e f; g h i} as sum_x (-1)^(2x) (2x+1) {a b c; f i x}
+    // {d e f; b x h} {g h i; x a d} (Messiah, Quantum Mechanics, App. C)
+    long double ninej(int a, int b, int c, int d, int e, int f, int g, int h, int i) const {
+        if (!tri(a, b, c) || !tri(d, e, f) || !tri(g, h, i) || !tri(a, d, g) || !tri(b, e, h) ||
+            !tri(c, f, i))
+            return 0.0L;
+        const int lo = std::max(std::abs(a - i), std::max(std::abs(d - h), std::abs(b - f)));
+        const int hi = std::min(a + i, std::min(d + h, b + f));
+        long double sum = 0.0L;
+        for (int x = lo; x <= hi; x += 2) {
+            const long double t = (long double)(x + 1) * sixj(a, b, c, f, i, x) * sixj(d, e, f, b, x, h) *
+                                  sixj(g, h, i, x, a, d);
+            sum += (x & 1) ? -t : t;
+        }
+        return sum;
+    }
+    // factor of an SU(2) operator block used transposed: delta spin d, row /
+    // column spins l / r (the reference's sign and normalisation convention)
+    static long double transpose(int d, int l, int r) {
+        const long double sign = ((d + l - r) & 2) ? -1.0L : 1.0L;
+        return sign * sqrtl((long double)(r + 1)) / sqrtl((long double)(l + 1));
+    }
+};
+
+struct OpInfos {
+    const b2g_op_infos *p;
+    int find_info(uint64_t dq) const {  // exact delta quantum or -1
+        return find(p->dq, p->n, dq);
+    }
+    int find_block(int info, uint64_t q) const {
+        const int s = p->start[info], e = p->start[info + 1];
+        const int k = find(p->quanta + s, e - s, q);
+        return k;
+    }
+};
+
+struct CEntry {
+    double f;
+    uint64_t iv;
+    uint32_t ia, ib, ic;
+};
+
+// ConnectionInfo::initialize_wfn (src/core/sparse_matrix.hpp:163-292): for
+// every sub-label k (conj type, label) and every bra block iv, the coupled
+// (left op block ia, right op block ib, ket block ic) with their factor; the
+// j-th entry found for each iv goes to round j, and rounds are emitted in
+// order (so the first entry of every bra block comes first).
+template <class L, bool kSu2>
+int wfn_connection(uint64_t cdq, uint64_t vdq, uint64_t opdq, int n_sub, const int32_t *sub_conj,
+                   const uint64_t *sub_q, const OpInfos &A, const OpInfos &B, int n_ket,
+                   const uint64_t *ket_q, int n_bra, const uint64_t *bra_q, int32_t *n5,
+                   std::vector<uint32_t> &idx, std::vector<CEntry> &out) {
+    static const Recoupling rc;
+    auto tw = [](uint64_t a) { return (int)((a >> 16) & 0xFFFFULL); };
+    auto mult = [&](uint64_t a) { return kSu2 ? tw(a) + 1 : 1; };
+    auto fermion = [](uint64_t a) { return ((a >> 48) & 1ULL) != 0; };
+    for (int t = 0; t < 5; t++)
+        n5[t] = -1;
+    idx.assign(n_sub, 0);
+    for (int k = 0; k < n_sub; k++) {
+        const int ct = sub_conj[k];
+        if (ct < 0 || ct > 3)
+            return fail(B2G_ERR_ARG, "b2g_wfn_connection: conj type outside 0..3");
+        if (n5[ct] == -1)
+            n5[ct] = k;
+        const bool cja = ct & 1, cjb = (ct & 2) != 0;
+        idx[k] = (uint32_t)out.size();
+        const uint64_t sq = sub_q[k];
+        const uint64_t adq = cja ? L::neg(L::bra(sq, opdq)) : L::bra(sq, opdq);
+        const uint64_t bdq = cjb ? L::ket(sq) : L::neg(L::ket(sq));
+        const int ai = A.find_info(adq), bi = B.find_info(bdq);
+        if (ai < 0 || bi < 0)
+            return fail(B2G_ERR_ARG, "b2g_wfn_connection: no operator info for a sub-label");
+        const bool bferm = B.p->fermion[bi] != 0;
+        std::vector<std::vector<CEntry>> rounds;
+        for (int iv = 0; iv < n_bra; iv++) {
+            size_t ip = 0;
+            const uint64_t lq = L::bra(bra_q[iv], vdq);
+            const uint64_t rq = L::neg(L::ket(bra_q[iv]));
+            const uint64_t rqs = cjb ? L::add(rq, bdq) : L::add(rq, L::neg(bdq));
+            for (int r = 0; r < L::count(rqs); r++) {
+                const uint64_t rqp = L::elem(rqs, r);
+                const int ib = B.find_block(bi, cjb ? L::combine(bdq, rqp, rq) : L::combine(bdq, rq, rqp));
+                if (ib < 0)
+                    continue;
+                const uint64_t lqs = L::add(cdq, L::neg(rqp));
+                for (int l = 0; l < L::count(lqs); l++) {
+                    const uint64_t lqp = L::elem(lqs, l);
+                    const int ia = A.find_block(ai, cja ? L::combine(adq, lqp, lq) : L::combine(adq, lq, lqp));
+                    const int ic = find(ket_q, n_ket, L::combine(cdq, lqp, L::neg(rqp)));
+                    if (ia < 0 || ic < 0)
+                        continue;
+                    long double x = 1.0L;
+                    if (kSu2) {
+                        x = sqrtl((long double)mult(cdq) * mult(opdq) * mult(lq) * mult(rq)) *
+                            rc.ninej(tw(lqp), tw(rqp), tw(cdq), tw(adq), tw(bdq), tw(opdq), tw(lq), tw(rq),
+                                     tw(vdq));
+                        if (cja)
+                            x *= Recoupling::transpose(tw(adq), tw(lq), tw(lqp));
+                        if (cjb)
+                            x *= Recoupling::transpose(tw(bdq), tw(rq), tw(rqp));
+                    }
+                    double f = (double)x;
+                    if (bferm && fermion(lqp))
+                        f = -f;
+                    if (std::fabs(f) >= 1e-20) {
+                        if (rounds.size() <= ip)
+                            rounds.emplace_back();
+                        rounds[ip].push_back(CEntry{f, (uint64_t)iv, (uint32_t)ia, (uint32_t)ib, (uint32_t)ic});
+                        ip++;
+                    }
+                }
+            }
+        }
+        for (auto &rd : rounds)
+            out.insert(out.end(), rd.begin(), rd.end());
+    }
+    n5[4] = n_sub;
+    for (int t = 3; t >= 0; t--)
+        if (n5[t] == -1)
+            n5[t] = n5[t + 1];
+    return B2G_OK;
+}
+
 bool bad_info(const b2g_state_info *s) {
     return s == nullptr || s->n < 0 || (s->n > 0 && (s->quanta == nullptr || s->n_states == nullptr));
 }
@@ -277,6 +436,42 @@ int b2g_wfn_blocks(int sym, const b2g_state_info *bra, const b2g_state_info *ket
         off = off + (x + align - 1) / align * align;
     }
     *total = off;
+    return B2G_OK;
+}
+
+int b2g_wfn_connection(int sym, uint64_t cdq, uint64_t vdq, uint64_t opdq, int32_t n_sub,
+                       const int32_t *sub_conj, const uint64_t *sub_q, const b2g_op_infos *left,
+                       const b2g_op_infos *right, int32_t n_ket, const uint64_t *ket_q, int32_t n_bra,
+                       const uint64_t *bra_q, int32_t *n5, uint32_t *idx, uint64_t *stride,
+                       double *factor, uint32_t *ia, uint32_t *ib, uint32_t *ic, int64_t cap,
+                       int64_t *nc) {
+    auto bad_ops = [](const b2g_op_infos *o) {
+        return o == nullptr || o->n < 0 ||
+               (o->n > 0 && (o->dq == nullptr || o->fermion == nullptr || o->start == nullptr ||
+                             (o->start[o->n] > 0 && o->quanta == nullptr)));
+    };
+    if ((sym != B2G_SYM_SZ && sym != B2G_SYM_SU2) || n_sub < 0 || (n_sub > 0 && (sub_conj == nullptr ||
+        sub_q == nullptr)) || bad_ops(left) || bad_ops(right) || n_ket < 0 || n_bra < 0 ||
+        (n_ket > 0 && ket_q == nullptr) || (n_bra > 0 && bra_q == nullptr) || n5 == nullptr ||
+        nc == nullptr || (n_sub > 0 && idx == nullptr))
+        return fail(B2G_ERR_ARG, "b2g_wfn_connection: bad argument");
+    std::vector<uint32_t> vi;
+    std::vector<CEntry> out;
+    const OpInfos A{left}, B{right};
+    const int rc = sym == B2G_SYM_SU2
+                       ? wfn_connection<Su2, true>(cdq, vdq, opdq, n_sub, sub_conj, sub_q, A, B, n_ket, ket_q,
+                                                   n_bra, bra_q, n5, vi, out)
+                       : wfn_connection<Sz, false>(cdq, vdq, opdq, n_sub, sub_conj, sub_q, A, B, n_ket, ket_q,
+                                                   n_bra, bra_q, n5, vi, out);
+    if (rc != B2G_OK)
+        return rc;
+    *nc = (int64_t)out.size();
+    if (*nc > cap || (*nc > 0 && (stride == nullptr || factor == nullptr || ia == nullptr ||
+                                  ib == nullptr || ic == nullptr)))
+        return fail(B2G_ERR_ARG, "b2g_wfn_connection: output capacity too small");
+    std::copy(vi.begin(), vi.end(), idx);
+    for (size_t j = 0; j < out.size(); j++)
+        stride[j] = out[j].iv, factor[j] = out[j].f, ia[j] = out[j].ia, ib[j] = out[j].ib, ic[j] = out[j].ic;
     return B2G_OK;
 }
 

@@ -426,6 +426,32 @@ int b2g_wfn_blocks(int sym, const b2g_state_info *bra, const b2g_state_info *ket
                    int wfn, uint32_t align, uint64_t *quanta, uint32_t *rows, uint32_t *cols,
                    uint32_t *shifts, int cap, int *n_blocks, uint32_t *total);
 
+/* Operator infos of one side of an H_eff (left_op_infos / right_op_infos of
+ * the EffectiveHamiltonian constructor): n infos sorted by delta quantum, each
+ * with its fermion flag and its ascending block labels quanta[start[i] ..
+ * start[i + 1]). */
+typedef struct {
+    int32_t n;
+    const uint64_t *dq;
+    const int32_t *fermion;
+    const int32_t *start;
+    const uint64_t *quanta;
+} b2g_op_infos;
+/* ConnectionInfo::initialize_wfn (sparse_matrix.hpp:163-292), as the
+ * EffectiveHamiltonian constructor calls it (effective_hamiltonian.hpp:208-216):
+ * for each sub-label k (sub_conj[k] in 0..3: bit 0 left operator transposed,
+ * bit 1 right; sub_q[k] its label) and each bra block, the coupled (left op
+ * block, right op block, ket block) triples with their Clebsch-Gordan factor
+ * (SU(2): 9j symbol x transposition factors x fermion sign; SZ: sign only).
+ * Outputs: n5 (5 conj-type boundaries), idx (n_sub starts), and nc entries of
+ * stride (bra block), factor, ia, ib, ic (capacity cap). */
+int b2g_wfn_connection(int sym, uint64_t cdq, uint64_t vdq, uint64_t opdq, int32_t n_sub,
+                       const int32_t *sub_conj, const uint64_t *sub_q, const b2g_op_infos *left,
+                       const b2g_op_infos *right, int32_t n_ket, const uint64_t *ket_q, int32_t n_bra,
+                       const uint64_t *bra_q, int32_t *n5, uint32_t *idx, uint64_t *stride,
+                       double *factor, uint32_t *ia, uint32_t *ib, uint32_t *ic, int64_t cap,
+                       int64_t *nc);
+
 #ifdef __cplusplus
 }
 #endif

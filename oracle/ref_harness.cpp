@@ -305,9 +305,63 @@ template <typename S> struct Dumper : CallbackKernel {
         w.scalar("is_wfn", info->is_wavefunction);
         w.scalar("total_memory", (double)h->ket->total_memory);
         w.scalar("su2", is_same<S, SU2>::value ? 1 : 0);
+        dump_wfn_cinfo(w, h);
         w.man.flush();
         lc = nullptr;
         lt.deallocate(), rr.deallocate(), ll.deallocate();
+    }
+    // The H_eff's wavefunction connection infos (ConnectionInfo::initialize_wfn,
+    // src/core/sparse_matrix.hpp:163-292, built in the EffectiveHamiltonian
+    // constructor, src/dmrg/effective_hamiltonian.hpp:208-216) with their
+    // inputs: the left/right operator infos, ket/bra infos and labels.
+    static void put_op_infos(Writer &w, const string &name,
+                             const vector<pair<S, shared_ptr<SparseMatrixInfo<S>>>> &infos) {
+        vector<uint64_t> dq, q;
+        vector<int32_t> ferm, start;
+        for (auto &p : infos) {
+            dq.push_back(p.first.data);
+            ferm.push_back(p.second->is_fermion ? 1 : 0);
+            start.push_back((int32_t)q.size());
+            for (int i = 0; i < p.second->n; i++)
+                q.push_back(p.second->quanta[i].data);
+        }
+        start.push_back((int32_t)q.size());
+        w.vec(name + "_dq", dq, "u8"), w.vec(name + "_ferm", ferm, "i4");
+        w.vec(name + "_start", start, "i4"), w.vec(name + "_q", q, "u8");
+    }
+    void dump_wfn_cinfo(Writer &w, const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        put_op_infos(w, "lop", h->left_op_infos);
+        put_op_infos(w, "rop", h->right_op_infos);
+        vector<uint64_t> bq(h->bra->info->n);
+        for (int i = 0; i < h->bra->info->n; i++)
+            bq[i] = h->bra->info->quanta[i].data;
+        w.vec("bra_q", bq, "u8");
+        vector<uint64_t> lab{h->ket->info->delta_quantum.data, h->bra->info->delta_quantum.data};
+        vector<uint64_t> opq, cq, cstride;
+        vector<int32_t> cn, cidx, cia, cib, cic, cstart, cqstart;
+        vector<double> cf;
+        for (size_t i = 0; i < h->wfn_infos.size(); i++) {
+            auto ci = h->wfn_infos[i];
+            if (ci == nullptr)
+                continue;
+            opq.push_back(h->operator_quanta[i].data);
+            for (int t = 0; t < 5; t++)
+                cn.push_back(ci->n[t]);
+            cqstart.push_back((int32_t)cq.size());
+            for (int k = 0; k < ci->n[4]; k++)
+                cq.push_back(ci->quanta[k].data), cidx.push_back((int32_t)ci->idx[k]);
+            cstart.push_back((int32_t)cstride.size());
+            for (int j = 0; j < ci->nc; j++) {
+                cstride.push_back(ci->stride[j]), cf.push_back(ci->factor[j]);
+                cia.push_back((int32_t)ci->ia[j]), cib.push_back((int32_t)ci->ib[j]);
+                cic.push_back((int32_t)ci->ic[j]);
+            }
+        }
+        cqstart.push_back((int32_t)cq.size()), cstart.push_back((int32_t)cstride.size());
+        w.vec("cdq_vdq", lab, "u8"), w.vec("ci_opdq", opq, "u8"), w.vec("ci_n", cn, "i4");
+        w.vec("ci_q", cq, "u8"), w.vec("ci_qstart", cqstart, "i4"), w.vec("ci_idx", cidx, "i4");
+        w.vec("ci_start", cstart, "i4"), w.vec("ci_stride", cstride, "u8"), w.vec("ci_factor", cf, "f8");
+        w.vec("ci_ia", cia, "i4"), w.vec("ci_ib", cib, "i4"), w.vec("ci_ic", cic, "i4");
     }
     void dump_post(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
         Writer w(site_dir() + "/post");
