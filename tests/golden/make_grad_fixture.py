@@ -22,7 +22,8 @@ difference (e_plus_k - e_minus_k) / (2 delta).
 
 A second fixture, syn8_su2_conv_grad.npz, does the same at the converged MPS
 of a full run and pins the derivatives to the reference's own 1-/2-PDM
-(converged(), below).
+(converged(), below); a third, syn8_su2_conv_fullgrad.npz, holds the Jacobian
+for every independent integral there (full_gradient()).
 
 Usage (needs the reference harness; not run on GPU machines):
     python tests/golden/make_grad_fixture.py
@@ -273,6 +274,86 @@ def converged():
     print(f"-> {path} ({os.path.getsize(path)} bytes), linearity worst {lin_worst:.1e}")
 
 
+def unique_params(n):
+    """Every independent integral: h_pq (p >= q) and (pq|rs) (p >= q, r >= s, pq >= rs)."""
+    pairs = [(i, j) for i in range(n) for j in range(i + 1)]
+    hs = [("h", p) for p in pairs]
+    es = [("eri", pairs[a] + pairs[b]) for a in range(len(pairs)) for b in range(a + 1)]
+    return hs + es
+
+
+def full_gradient():
+    """syn8_su2_conv_fullgrad.npz: the integral -> operator Jacobian of the
+    middle-site H_eff at the converged MPS (the run of converged()) for every
+    independent integral, by one-sided differences (the blob is linear in the
+    integrals at fixed MPS), with the reference's full 1-/2-PDM."""
+    h0, eri0, ec = synthetic_integrals(N, seed=0)
+    out = os.path.join(RAW, "grad", "full")
+    if os.path.exists(out):
+        shutil.rmtree(out)
+    os.makedirs(out)
+    params = unique_params(N)
+    dumps = [os.path.join(out, "base.FCIDUMP")]
+    write_fcidump(dumps[0], h0, eri0, ec, nelec=N)
+    for k, (kind, idx) in enumerate(params):
+        h, eri = perturbed(h0, eri0, kind, idx, +1)
+        dumps.append(os.path.join(out, f"p{k}.FCIDUMP"))
+        write_fcidump(dumps[-1], h, eri, ec, nelec=N)
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
+    cmd = [HARNESS, "--ham", dumps[0], *CONV_ARGS, "--perturb", ",".join(dumps), "--threads", "1",
+           "--out", out]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    pdm_a, _ = read_dump(os.path.join(out, "pdm"))
+    dm1 = pdm_a["dm1"].reshape(N, N)
+    dm2 = pdm_a["dm2"].reshape(N, N, N, N)
+
+    def site(k):
+        d = os.path.join(out, f"perturb{k}")
+        (sd,) = [x for x in os.listdir(d) if x.startswith("sweep")]
+        return read_dump(os.path.join(d, sd))
+
+    base_a, base_s = site(0)
+    base_ops = to_base_layout(base_a, base_a)
+    jac_idx, jac_val, jac_ptr, expect, labels = [], [], [0], [], []
+    for k, (kind, idx) in enumerate(params):
+        a, _ = site(k + 1)
+        for key in PAIR_FIELDS:
+            if key not in ("b0", "a1") and not np.array_equal(a[key], base_a[key]):
+                raise RuntimeError(f"{kind}{idx}: pair structure differs ({key})")
+        d = (to_base_layout(base_a, a) - base_ops) / DELTA
+        nz = np.nonzero(np.abs(d) > 1e-9 * max(np.abs(d).max(), 1e-300))[0]
+        jac_idx.append(nz.astype(np.int32))
+        jac_val.append(d[nz])
+        jac_ptr.append(jac_ptr[-1] + nz.size)
+        if kind == "h":
+            p, q = idx
+            expect.append(dm1[p, q] + (dm1[q, p] if p != q else 0.0))
+        else:
+            expect.append(0.5 * sum(dm2[i_, k_, l_, j_] for (i_, j_, k_, l_) in eri_orbit(*idx)))
+        labels.append(f"{kind}{list(idx)}")
+    meta = {"name": "syn8_su2_conv_fullgrad", "kind": "integral_gradient_full",
+            "description": "synthetic ab initio n=8 N=8 (seed 0), SU(2), M=60, converged 8-sweep MPS "
+                           "(harness seed 1234): middle-site (3-4) H_eff and its integral -> operator "
+                           "Jacobian for every independent integral (one-sided, step delta), with the "
+                           "reference's 1-/2-PDM",
+            "harness_args": CONV_ARGS, "delta": DELTA, "labels": labels,
+            "pdm_convention": "E = sum_ij h_ij dm1[i,j] + 1/2 sum_ijkl (ij|kl) dm2[i,k,l,j] + E_core",
+            "param_convention": "h[p,q] (p >= q): h_pq and h_qp move together; eri[p,q,r,s] "
+                                "(p >= q, r >= s, pq >= rs): all eight symmetry-equivalent entries move together"}
+    path = os.path.join(HERE, "syn8_su2_conv_fullgrad.npz")
+    np.savez_compressed(
+        path, **{k: base_a[k] for k in PAIR_FIELDS}, ops=base_ops, psi=base_a["psi"],
+        psi_size=np.int64(base_s["psi_size"]), sigma_size=np.int64(base_s["sigma_size"]),
+        jac_idx=np.concatenate(jac_idx), jac_val=np.concatenate(jac_val),
+        jac_ptr=np.array(jac_ptr, dtype=np.int64), pdm_derivative=np.array(expect), dm1=dm1, dm2=dm2,
+        meta=np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8))
+    print(f"-> {path} ({os.path.getsize(path)} bytes), {len(params)} parameters, "
+          f"{jac_ptr[-1]} Jacobian entries")
+
+
 if __name__ == "__main__":
     first_site()
     converged()
+    full_gradient()

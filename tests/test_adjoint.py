@@ -120,6 +120,39 @@ def test_oracle_integral_gradient_matches_reference_pdm():
     _check_pdm_derivative(chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"]), z, meta)
 
 
+def _check_full_gradient(dE, ref):
+    """Every independent integral: per-element relative error <= 1e-6 where the
+    PDM element exceeds 1e-3, absolute <= 1e-9 elsewhere."""
+    big = np.abs(ref) > 1e-3
+    assert np.all(np.abs(dE - ref)[big] / np.abs(ref[big]) <= RTOL_INTEGRAL)
+    assert np.all(np.abs(dE - ref)[~big] <= 1e-9)
+
+
+def _jac_times(z, d):
+    """sum_k d_k dops/dtheta_k (the blob is linear in the integrals)."""
+    ptr = z["jac_ptr"]
+    col = np.repeat(np.arange(ptr.size - 1), np.diff(ptr))
+    out = np.zeros(z["ops"].size)
+    np.add.at(out, z["jac_idx"], z["jac_val"] * d[col])
+    return out
+
+
+def test_oracle_full_integral_gradient_matches_reference_pdm():
+    """dE/dh_pq and dE/d(pq|rs) for every independent integral (36 + 666 at n=8)
+    at the converged MPS: numpy adjoint chained through the reference's full
+    Jacobian, against the reference's 1-/2-PDM."""
+    from b2g.autodiff import chain_to_parameters
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture("syn8_su2_conv_fullgrad")
+    assert len(meta["labels"]) == 702
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    v = z["psi"] / np.linalg.norm(z["psi"])
+    g, _ = oracle.adjoint(seq, z["ops"], v, v)
+    _check_full_gradient(chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"]),
+                         z["pdm_derivative"])
+
+
 # ---------------------------------------------------------------- GPU
 
 torch = pytest.importorskip("torch")
@@ -309,4 +342,45 @@ def test_gpu_integral_gradient_matches_reference_pdm(ctx):
     h.adjoint(v, v, g, None)
     ctx.synchronize()
     _check_pdm_derivative(chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"]), z, meta)
+    h.close()
+
+
+@pytest.mark.gpu
+def test_gpu_full_integral_gradient_and_random_directions(ctx):
+    """The full integral gradient from the adjoint kernel against the
+    reference's 1-/2-PDM, and in 20 random directions D of integral space
+    against central differences (step 1e-5) of the energy of the fixed MPS,
+    <psi|H_eff(ops(theta + t D))|psi>, computed with the GPU product."""
+    from b2g.autodiff import chain_to_parameters
+    from b2g.capi import PairSeq
+    from b2g.problem import PAIR_FIELDS
+    z, meta = _grad_fixture("syn8_su2_conv_fullgrad")
+    seq = PairSeq({k: z[k] for k in PAIR_FIELDS})
+    n = int(z["psi_size"])
+    h = b2g.EffectiveHamiltonian(ctx, seq, z["ops"], n, int(z["sigma_size"]))
+    v = torch.from_numpy(z["psi"] / np.linalg.norm(z["psi"])).cuda()
+    g = torch.zeros(z["ops"].size, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    h.adjoint(v, v, g, None)
+    ctx.synchronize()
+    dE = chain_to_parameters(g, z["jac_idx"], z["jac_val"], z["jac_ptr"])
+    _check_full_gradient(dE, z["pdm_derivative"])
+
+    def energy(ops):
+        h.set_ops(np.ascontiguousarray(ops))
+        s = torch.zeros(n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        h(v, s)
+        ctx.synchronize()
+        return float(torch.dot(v, s))
+
+    rng = np.random.default_rng(21)
+    eps, worst = 1e-5, 0.0
+    for _ in range(20):
+        d = rng.standard_normal(dE.size)
+        jd = _jac_times(z, d)
+        fd = (energy(z["ops"] + eps * jd) - energy(z["ops"] - eps * jd)) / (2 * eps)
+        worst = max(worst, abs(float(dE @ d) - fd) / abs(fd))
+        assert float(z["pdm_derivative"] @ d) == pytest.approx(fd, rel=1e-6)
+    assert worst <= 1e-6, worst
     h.close()
