@@ -437,6 +437,11 @@ def run_ours(args, rank, local_rank, world, dist):
         dav["eight_roots"] = multi
     dh.close()
     result["davidson"] = dav
+    # ---- full-size site solve: Davidson FP64 vs TF32x3 + FP64 defect correction
+    # on the symmetrised n=24 M=1000 sweep-0 site (200 iterations at most)
+    if not args.headline_only:
+        result["site_solve"] = {"site": "heff_syn24_su2_M1000_sweep0",
+                                **site_solve_section(ctx, load_workload("heff_syn24_su2_M1000_sweep0"))}
     # ---- differentiation form: one adjoint (operator and ket gradients of
     # <x|H_eff|y>, FP64) on this workload, next to the FP64 product
     if not args.headline_only:
@@ -529,6 +534,61 @@ def integral_gradient_check(ctx, dev):
             "bound": 1e-6}
 
 
+def site_solve_section(ctx, prob, max_iter=200, conv_thrd=1e-9):
+    """Davidson on the full-size site: FP64 against TF32x3 with FP64 defect
+    correction.  The recorded structure carries seeded synthetic operator
+    values, whose H_eff is not symmetric; the solve runs on (H_eff + H_eff^T)/2,
+    one pair sequence of both (b2g PairSeq.symmetrized: the transposed pairs of
+    the same blob), so both forms solve the same symmetric problem of the
+    site's block structure (twice the pairs of one product)."""
+    import b2g
+    seq = prob.seq().symmetrized()
+    h = b2g.EffectiveHamiltonian(ctx, seq, prob.ops, prob.psi_size, prob.sigma_size)
+    h.set_params(256, 256, 64)
+    diag = h.diag()
+    out = {"workload": "(H + H^T)/2 of the bench workload's H_eff", "pairs": int(seq.n),
+           "conv_thrd": conv_thrd, "max_iter": max_iter}
+    for name, form in (("fp64", b2g.FP64), ("tf32x3", b2g.TF32X3)):
+        x = np.array(prob.psi, copy=True)
+        converged = True
+        try:
+            h.eigs(diag, x, conv_thrd=conv_thrd, max_iter=max_iter, form=form)
+        except b2g.B2GError as err:
+            if err.code != 5:   # B2G_ERR_NOT_CONVERGED: report the solve as it stopped
+                raise
+            converged = False
+        r = h.last_davidson
+        out[name] = {"energy": r.energy, "iterations": r.n_iter, "converged": converged,
+                     "fp64_products": r.n_apply_fp64, "reduced_products": r.n_apply_mixed,
+                     "seconds": h.last_tdav, "residual_norm2": r.residual_norm2}
+    out["abs_energy_diff"] = abs(out["tf32x3"]["energy"] - out["fp64"]["energy"])
+    out["speedup_tf32x3_vs_fp64"] = out["fp64"]["seconds"] / out["tf32x3"]["seconds"]
+    h.close()
+    return out
+
+
+def adjoint_only(args, local_rank):
+    import torch
+
+    import b2g
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    prob = load_workload(args.workload)
+    ctx = b2g.Context(local_rank)
+    heff = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
+    flush = torch.empty(4 * L2_BYTES, dtype=torch.uint8, device=dev)
+
+    def do_flush():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    res = adjoint_section(heff, prob, stream, dev, do_flush, args)
+    heff.close()
+    ctx.close()
+    return res
+
+
 def truncation_section(ctx, cpu=True):
 
     from b2g.truncation import DensityMatrixLayout, split_density_matrix
@@ -599,6 +659,9 @@ def main():
     ap.add_argument("--truncation-only", action="store_true",
                     help="run only the density-matrix truncation section (GPU, no CPU leg); "
                          "for profiler runs")
+    ap.add_argument("--site-solve-only", action="store_true",
+                    help="run only the full-size Davidson comparison (FP64 vs TF32x3) on the "
+                         "symmetrised workload H_eff")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the differentiation-form section (one FP64 adjoint and one FP64 "
                          "product on the workload); for profiler runs")
@@ -619,6 +682,12 @@ def main():
     if args.truncation_only:
         import b2g
         print(json.dumps({"section": "truncation", **truncation_section(b2g.Context(local_rank), cpu=False)}),
+              flush=True)
+        return
+    if args.site_solve_only:
+        import b2g
+        print(json.dumps({"section": "site_solve",
+                          **site_solve_section(b2g.Context(local_rank), load_workload(args.workload))}),
               flush=True)
         return
     if args.adjoint_only:

@@ -235,6 +235,24 @@ class PairSeq:
         idx = np.asarray(idx, dtype=np.int64)
         return PairSeq({k: v[idx] for k, v in self.arrays.items()})
 
+    def transposed(self) -> "PairSeq":
+        """The pairs of H_eff^T: pair i becomes W = x[c1:] op_b0(ops[b0:])^T,
+        out[a0:] += alpha op_a1(ops[a1:])^T W (both operator flags flipped, the
+        psi and sigma roles swapped), so applying it to x gives H_eff^T x."""
+        a = self.arrays
+        return PairSeq({"tb0": 1 - a["tb0"], "m0": a["m1"], "k0": a["n1"], "n0": a["k0"],
+                        "lda0": a["ldc1"], "ldb0": a["ldb0"], "a0": a["c1"], "b0": a["b0"],
+                        "ta1": 1 - a["ta1"], "m1": a["m0"], "k1": a["m1"], "n1": a["k0"],
+                        "lda1": a["lda1"], "ldc1": a["lda0"], "a1": a["a1"], "c1": a["a0"],
+                        "alpha0": a["alpha0"], "alpha1": a["alpha1"]})
+
+    def symmetrized(self) -> "PairSeq":
+        """The pairs of (H_eff + H_eff^T) / 2 (square H_eff only)."""
+        t = self.transposed()
+        both = {k: np.concatenate([self.arrays[k], t.arrays[k]]) for k in self.arrays}
+        both["alpha1"] = both["alpha1"] * 0.5
+        return PairSeq(both)
+
     def mnk(self) -> float:
         a = self.arrays
         return float(np.sum(a["m0"].astype(np.float64) * a["n0"] * a["k0"]

@@ -178,8 +178,9 @@ class EffectiveHamiltonian:
         rc = lib().b2g_davidson(self._h, diag.ctypes.data, psi.ctypes.data, conv_thrd, max_iter,
                                 def_min, def_max, form, C.byref(res))
         tdav = time.perf_counter() - t0
+        self.last_davidson = res   # also when the solve stops unconverged (max_iter)
+        self.last_tdav = tdav
         check(rc)
-        self.last_davidson = res
         nflop = self.nflop * (res.n_apply_fp64 + res.n_apply_mixed)
         return res.energy, res.n_iter, nflop, tdav
 
