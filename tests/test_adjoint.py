@@ -52,6 +52,22 @@ def test_oracle_adjoint_is_the_derivative_of_the_replay(problems, name):
         assert float(gy @ d_y) == pytest.approx(f_y, rel=RTOL_FD_LINEAR, abs=1e-12)
 
 
+@pytest.mark.parametrize("name", fixture_ids() + rotation_ids())
+def test_transposed_pairs_apply_the_transpose(problems, name):
+    """PairSeq.transposed(): its replay is H^T x (the adjoint's ket gradient);
+    symmetrized() replays (H + H^T)/2 (square problems)."""
+    p = problems[name]
+    seq = p.seq()
+    rng = np.random.default_rng(4)
+    x, y = _rand_like(rng, p.sigma_size), _rand_like(rng, p.psi_size)
+    _, gy = oracle.adjoint(seq, p.ops, x, y)
+    assert rel(oracle.replay(seq.transposed(), p.ops, x, p.psi_size), gy) <= 1e-12
+    if p.psi_size == p.sigma_size:
+        hs = oracle.replay(seq.symmetrized(), p.ops, x, p.sigma_size)
+        ref = 0.5 * (oracle.replay(seq, p.ops, x, p.sigma_size) + gy)
+        assert rel(hs, ref) <= 1e-12
+
+
 @pytest.mark.parametrize("name", fixture_ids())
 def test_heff_is_symmetric(problems, name):
     """<x|H y> = <H x|y> on every recorded H_eff (the adjoint's ket gradient is H^T x)."""
