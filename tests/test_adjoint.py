@@ -400,3 +400,20 @@ def test_gpu_full_integral_gradient_and_random_directions(ctx):
         assert float(z["pdm_derivative"] @ d) == pytest.approx(fd, rel=1e-6)
     assert worst <= 1e-6, worst
     h.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_argument_errors(problems, ctx):
+    p = problems["hub8_su2"]
+    h = _heff(ctx, p)
+    x = torch.zeros(p.sigma_size, dtype=torch.float64, device="cuda")
+    g = torch.zeros(p.ops.size, dtype=torch.float64, device="cuda")
+    from b2g import capi
+    # the C entry before its schedule exists: a state error, nothing launched
+    rc = capi.lib().b2g_heff_adjoint(h._h, x.data_ptr(), x.data_ptr(), 1.0, g.data_ptr(), None)
+    assert rc == capi.B2G_ERR_STATE
+    with pytest.raises(ValueError):
+        h.set_ops(np.zeros(p.ops.size + 1))
+    with pytest.raises(ValueError):
+        h.adjoint(x, x, torch.zeros(3, dtype=torch.float64, device="cuda"), None)
+    h.close()

@@ -58,3 +58,17 @@ def test_recoupling_identities():
     r = quanta.wfn_connection(quanta.SU2, s0, s0, s0, np.array([0]), np.array([s0], np.uint64), left, right,
                               np.array([s0], np.uint64), np.array([s0], np.uint64))
     assert r["stride"].size == 1 and r["factor"][0] == pytest.approx(1.0, abs=1e-15)
+
+
+def test_wfn_connection_rejects_bad_input():
+    s0 = quanta.su2_label(0, 0)
+    ops = (np.array([s0], np.uint64), np.array([0]), np.array([0, 1]), np.array([s0], np.uint64))
+    q = np.array([s0], np.uint64)
+    with pytest.raises(Exception):
+        quanta.wfn_connection(7, s0, s0, s0, np.array([0]), q, ops, ops, q, q)   # unknown symmetry
+    with pytest.raises(Exception):
+        quanta.wfn_connection(quanta.SU2, s0, s0, s0, np.array([5]), q, ops, ops, q, q)   # conj type 5
+    # a sub-label whose operator delta quantum has no operator info
+    s2 = quanta.su2_label(0, 2)
+    with pytest.raises(Exception):
+        quanta.wfn_connection(quanta.SU2, s0, s0, s2, np.array([0]), np.array([s2], np.uint64), ops, ops, q, q)
