@@ -86,6 +86,34 @@ class ShardedEffectiveHamiltonian:
             c.add_(part)
         return c
 
+    def adjoint(self, x, y, grad_ops=None, grad_psi=None, scale: float = 1.0):
+        """Gradients of <x|H_eff|y> summed over the ranks: each rank
+        differentiates its own pairs into zeroed buffers, one all_reduce per
+        gradient, then grad += the sum (every rank gets it).  Host numpy
+        arrays (gloo) or CUDA tensors (NCCL), matching the engine."""
+        import torch
+        import torch.distributed as dist
+
+        host = isinstance(x, np.ndarray)
+        parts = []
+        for g in (grad_ops, grad_psi):
+            if g is None:
+                parts.append(None)
+            else:
+                parts.append(np.zeros_like(g) if host else torch.zeros_like(g))
+        self.local.adjoint(x, y, parts[0], parts[1], scale)
+        if not host and hasattr(self.local, "ctx"):
+            self.local.ctx.synchronize()
+        for g, part in zip((grad_ops, grad_psi), parts):
+            if g is None:
+                continue
+            t = torch.from_numpy(part) if host else part
+            dist.all_reduce(t, group=self.group)
+            if host:
+                g += part
+            else:
+                g.add_(part)
+
     def close(self):
         if hasattr(self.local, "close"):
             self.local.close()

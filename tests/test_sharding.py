@@ -90,6 +90,13 @@ class OracleShare:
         oracle.replay(self.seq, self.ops, b, self.sigma_size, scale, sigma=c)
         return c
 
+    def adjoint(self, x, y, grad_ops, grad_psi, scale=1.0):
+        go, gy = oracle.adjoint(self.seq, self.ops, x, y)
+        if grad_ops is not None:
+            grad_ops += scale * go
+        if grad_psi is not None:
+            grad_psi += scale * gy
+
 
 def _free_port():
     with socket.socket() as s:
@@ -112,6 +119,12 @@ def _gloo_rank(rank, world, port, name, out_dir):
         c = np.full(p.sigma_size, 0.25)   # c += scale * H psi keeps what c held
         h(p.psi, c, scale=0.5)
         np.save(os.path.join(out_dir, f"sigma{rank}.npy"), c)
+        # the adjoint of the sharded product: one all_reduce per gradient
+        x = np.random.default_rng(2).standard_normal(p.sigma_size)
+        go, gy = np.zeros(p.ops.size), np.ones(p.psi_size)
+        h.adjoint(x, p.psi, go, gy, scale=2.0)
+        np.save(os.path.join(out_dir, f"gops{rank}.npy"), go)
+        np.save(os.path.join(out_dir, f"gpsi{rank}.npy"), gy)
         np.save(os.path.join(out_dir, f"npairs{rank}.npy"), np.array([h.local_seq.n]))
     finally:
         dist.destroy_process_group()
@@ -130,6 +143,11 @@ def test_gloo_two_ranks_sum_sigma(problems, name, tmp_path):
     assert npairs == p.seq().n
     assert np.array_equal(got[0], got[1])
     assert rel(got[0], want) <= RTOL
+    x = np.random.default_rng(2).standard_normal(p.sigma_size)
+    go, gy = oracle.adjoint(p.seq(), p.ops, x, p.psi)
+    for r in range(2):
+        assert rel(np.load(tmp_path / f"gops{r}.npy"), 2.0 * go) <= RTOL
+        assert rel(np.load(tmp_path / f"gpsi{r}.npy"), 1.0 + 2.0 * gy) <= RTOL
 
 
 @pytest.mark.gpu
@@ -153,3 +171,30 @@ def test_gpu_rank_shares_sum_to_reference(problems, name):
         assert rel(total.cpu().numpy(), p.sigma) <= RTOL
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hub8_su2", "syn8_sz"])
+def test_gpu_rank_adjoint_shares_sum_to_full_adjoint(problems, name):
+    """The adjoint of each rank's pairs (two shares built and run one after the
+    other on one GPU) sums to the adjoint of the whole H_eff."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    p = problems[name]
+    seq = p.seq()
+    ctx = b2g.Context(0)
+    x = np.random.default_rng(3).standard_normal(p.sigma_size)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(p.psi).cuda()
+    go = torch.zeros(p.ops.size, dtype=torch.float64, device="cuda")
+    gy = torch.zeros(p.psi_size, dtype=torch.float64, device="cuda")
+    for r in range(2):
+        h = b2g.EffectiveHamiltonian(ctx, rank_pairs(seq, 2, r), p.ops, p.psi_size, p.sigma_size)
+        torch.cuda.synchronize()
+        h.adjoint(xd, yd, go, gy)
+        ctx.synchronize()
+        h.close()
+    ref_o, ref_y = oracle.adjoint(seq, p.ops, x, p.psi)
+    assert rel(go.cpu().numpy(), ref_o) <= RTOL
+    assert rel(gy.cpu().numpy(), ref_y) <= RTOL
+    ctx.close()
