@@ -23,6 +23,11 @@
  *                        (src/core/iterative_matrix_functions.hpp:864-1173, 93-108)
  *                        as called by EffectiveHamiltonian::eigs
  *                        (src/dmrg/effective_hamiltonian.hpp:481-568)
+ *   (further entries below: diag, multi-root products and Davidson, density-
+ *    matrix truncation, environment blocking, quantum-number bookkeeping and
+ *    connection infos, term partition; and, without a reference counterpart,
+ *    the adjoint of H_eff*psi, the tile autotuner and the allocation-free
+ *    product -- each with the interface it replaces or the reason it exists)
  *
  * Conventions: row-major matrices (as GMatrix, src/core/matrix.hpp:94-106);
  * offsets and sizes count doubles; every function returns 0 on success and a
