@@ -77,6 +77,11 @@ class ShardedEffectiveHamiltonian:
             c += part
         else:
             part = torch.zeros_like(c)
+            if part.is_cuda:
+                # the zero-fill (and whatever torch last wrote into b) runs on
+                # torch's current stream; the library launches on its own
+                # context stream, so finish torch's work first
+                torch.cuda.current_stream(part.device).synchronize()
             self.local(b, part, scale, form)
             if part.is_cuda:
                 # the rank's kernels run on the context stream: finish them
@@ -101,6 +106,10 @@ class ShardedEffectiveHamiltonian:
                 parts.append(None)
             else:
                 parts.append(np.zeros_like(g) if host else torch.zeros_like(g))
+        if not host:
+            # zero-fills and torch's writes to x, y run on torch's current
+            # stream, the adjoint kernels on the library's context stream
+            torch.cuda.current_stream(x.device).synchronize()
         self.local.adjoint(x, y, parts[0], parts[1], scale)
         if not host and hasattr(self.local, "ctx"):
             self.local.ctx.synchronize()

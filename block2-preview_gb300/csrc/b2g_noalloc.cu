@@ -11,7 +11,9 @@
 // file-scope device array, kNoAllocScratchBytes (32 MiB) large, that every
 // GPU which loads this library holds until the process exits.  Pairs are
 // processed in chunks that fit the array (descriptors copied in, GEMM0 into
-// the array, GEMM1 accumulated into sigma with FP64 atomics).
+// the array, GEMM1 accumulated into sigma with FP64 atomics, so the order of
+// the additions into one sigma element varies between runs and the FP64
+// result can differ in its last bits from call to call).
 //
 // Rules for callers:
 //   * the first call on a device looks up the device address of the array
@@ -21,7 +23,10 @@
 //     it; calls whose work overlaps on the GPU (different streams, or
 //     different host threads on one device) race on it -- serialize them;
 //   * a single pair whose work matrix does not fit the array is rejected with
-//     B2G_ERR_ARG before anything is launched.
+//     B2G_ERR_ARG before anything is launched;
+//   * each chunk's descriptors go from a host staging array to the device by
+//     an ordinary cudaMemcpyAsync from pageable memory, so a call can hold
+//     the host until that copy has been staged.
 #include <mutex>
 
 #include "b2g_internal.h"
@@ -124,13 +129,20 @@ extern "C" int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops
             return fail(B2G_ERR_UNSUPPORTED, "b2g_heff_apply_noalloc: GEMM1 does not consume GEMM0");
         if (m1 == 0 || n1 == 0 || k1 == 0 || k0 == 0)
             continue;
+        // a row must fit its leading dimension (op(X) stored rows x cols)
+        if (seq->lda0[i] < k0 || seq->ldb0[i] < (seq->tb0[i] ? k0 : n0) ||
+            seq->lda1[i] < (seq->ta1[i] ? m1 : k1) || seq->ldc1[i] < n1)
+            return fail(B2G_ERR_ARG, "b2g_heff_apply_noalloc: pair " + std::to_string(i) +
+                                         " has a leading dimension below its row length");
         auto ext = [](bool t, int64_t r, int64_t c, int64_t ld) {
             return (uint64_t)(t ? (c - 1) * ld + r : (r - 1) * ld + c);
         };
-        if (seq->a0[i] + ext(false, m0, k0, seq->lda0[i]) > psi_size ||
-            seq->b0[i] + ext(seq->tb0[i], k0, n0, seq->ldb0[i]) > ops_size ||
-            seq->a1[i] + ext(seq->ta1[i], m1, k1, seq->lda1[i]) > ops_size ||
-            seq->c1[i] + ext(false, m1, n1, seq->ldc1[i]) > sigma_size)
+        // offset + extent <= size, written so that no sum can wrap around
+        auto fits = [](uint64_t off, uint64_t e, uint64_t size) { return e <= size && off <= size - e; };
+        if (!fits(seq->a0[i], ext(false, m0, k0, seq->lda0[i]), psi_size) ||
+            !fits(seq->b0[i], ext(seq->tb0[i], k0, n0, seq->ldb0[i]), ops_size) ||
+            !fits(seq->a1[i], ext(seq->ta1[i], m1, k1, seq->lda1[i]), ops_size) ||
+            !fits(seq->c1[i], ext(false, m1, n1, seq->ldc1[i]), sigma_size))
             return fail(B2G_ERR_ARG, "b2g_heff_apply_noalloc: pair " + std::to_string(i) +
                                          " reads or writes out of range");
         if ((uint64_t)(m0 * n0) > kWorkDoubles)

@@ -213,6 +213,11 @@ int b2g_block_contract_device(b2g_context *ctx, const b2g_block_seq *seq, const 
  * that array is rejected (B2G_ERR_ARG).  The first call on a device looks
  * the array's address up and should precede any stream capture on that
  * device; calls share the array, so calls that overlap on the GPU race.
+ * sigma is accumulated with FP64 atomics, so unlike the other FP64 entry
+ * points the result is not bit-reproducible from call to call (it differs
+ * in the last bits).  The pair descriptors reach the device through an
+ * ordinary copy from pageable host memory, so a call can hold the host
+ * until that copy is staged.
  * stream: a cudaStream_t (NULL = legacy default stream).  Asynchronous.
  */
 int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops, uint64_t ops_size,

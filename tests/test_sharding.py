@@ -198,3 +198,57 @@ def test_gpu_rank_adjoint_shares_sum_to_full_adjoint(problems, name):
     assert rel(go.cpu().numpy(), ref_o) <= RTOL
     assert rel(gy.cpu().numpy(), ref_y) <= RTOL
     ctx.close()
+
+
+def _cuda_single_rank(rank, port, name, out_dir):
+    """One rank of a single-rank NCCL group driving ShardedEffectiveHamiltonian
+    on CUDA tensors with no synchronisation of its own: torch writes the
+    inputs on its current stream and the class must order the library's
+    context stream after them."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "block2-preview_gb300"))
+    sys.path.insert(0, ROOT)
+    import torch
+    import torch.distributed as dist
+    from b2g.problem import load_problem
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), NCCL_NVLS_ENABLE="0")
+    torch.cuda.set_device(0)
+    dist.init_process_group("nccl", rank=0, world_size=1)
+    try:
+        p = load_problem(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+        ctx = b2g.Context(0)
+        h = ShardedEffectiveHamiltonian(ctx, p.seq(), p.ops, p.psi_size, p.sigma_size)
+        psi = torch.from_numpy(p.psi).cuda() * 1.0          # written by a torch kernel
+        c = torch.full((p.sigma_size,), 0.25, dtype=torch.float64, device="cuda")
+        h(psi, c, scale=0.5)
+        x = torch.from_numpy(np.random.default_rng(2).standard_normal(p.sigma_size)).cuda() * 1.0
+        go = torch.zeros(p.ops.size, dtype=torch.float64, device="cuda")
+        gy = torch.ones(p.psi_size, dtype=torch.float64, device="cuda")
+        h.adjoint(x, psi, go, gy, scale=2.0)
+        np.save(os.path.join(out_dir, "sigma.npy"), c.cpu().numpy())
+        np.save(os.path.join(out_dir, "gops.npy"), go.cpu().numpy())
+        np.save(os.path.join(out_dir, "gpsi.npy"), gy.cpu().numpy())
+        h.close()
+        ctx.close()
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hub8_su2", "syn8_sz"])
+def test_gpu_sharded_class_orders_streams(problems, name, tmp_path):
+    """ShardedEffectiveHamiltonian.__call__ and .adjoint on CUDA tensors, with
+    no manual synchronisation in the caller, equal the reference's sigma and
+    the oracle's adjoint."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    mp = pytest.importorskip("torch.multiprocessing")
+    p = problems[name]
+    mp.start_processes(_cuda_single_rank, args=(_free_port(), name, str(tmp_path)), nprocs=1,
+                       start_method="spawn", join=True)
+    assert rel(np.load(tmp_path / "sigma.npy"), 0.25 + 0.5 * p.sigma) <= RTOL
+    x = np.random.default_rng(2).standard_normal(p.sigma_size)
+    go, gy = oracle.adjoint(p.seq(), p.ops, x, p.psi)
+    assert rel(np.load(tmp_path / "gops.npy"), 2.0 * go) <= RTOL
+    assert rel(np.load(tmp_path / "gpsi.npy"), 1.0 + 2.0 * gy) <= RTOL
