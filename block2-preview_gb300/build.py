@@ -76,5 +76,62 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     return LIB
 
 
+SHIM = os.path.join(HERE, "shim")
+STAGED_BLOCK2 = os.path.join(SHIM, "_block2", "src")
+SWEEP = os.path.join(LIBDIR, "dmrg_sweep")
+
+
+def block2_source() -> str | None:
+    """block2's headers for the drop-in: $BLOCK2_SRC (staged into
+    shim/_block2/src so the tree can travel with this working copy), else an
+    earlier staged copy, else None."""
+    src = os.environ.get("BLOCK2_SRC")
+    if src and os.path.isfile(os.path.join(src, "block2_core.hpp")):
+        sys.path.insert(0, SHIM)
+        import stage_block2
+
+        if not os.path.isfile(os.path.join(STAGED_BLOCK2, "block2_core.hpp")):
+            stage_block2.stage(src)
+        return src
+    if os.path.isfile(os.path.join(STAGED_BLOCK2, "block2_core.hpp")):
+        return STAGED_BLOCK2
+    return None
+
+
+def _newer(target: str, deps) -> bool:
+    return not os.path.exists(target) or any(os.path.getmtime(d) > os.path.getmtime(target) for d in deps)
+
+
+def build_sweep_programs(verbose: bool = False, force: bool = False) -> dict:
+    """Builds the DMRG sweep program twice, in parallel: lib/dmrg_sweep (block2
+    with the GB300 drop-in, linked to libb2g.so) and oracle/_ref/dmrg_sweep_ref
+    (block2's own CPU path, the reference arm).  Needs block2's headers
+    (block2_source()); returns what was built or why not."""
+    src = block2_source()
+    if src is None:
+        return {"skipped": "no block2 headers (set BLOCK2_SRC or stage them with shim/stage_block2.py)"}
+    deps = [os.path.join(SHIM, f) for f in ("dmrg_sweep.cpp", "b2g_block2.hpp", "build.sh", "blas_defs.sh")]
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
+    jobs = []
+    if force or _newer(SWEEP, deps + [LIB, os.path.join(ROOT, "include", "b2g.h")]):
+        jobs.append(["bash", os.path.join(SHIM, "build.sh"), src, "gpu", SWEEP])
+    if force or _newer(ref_bin, deps):
+        jobs.append(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), src])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{' '.join(cmd)} failed:\n{r.stdout}\n{r.stderr}")
+        return cmd[-1]
+
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        done = list(ex.map(run, jobs))
+    return {"built": done, "sweep": SWEEP, "reference": ref_bin}
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--sweep" in sys.argv:
+        print(build_sweep_programs(verbose="-v" in sys.argv, force="--force" in sys.argv))

@@ -1,0 +1,326 @@
+// b2g_block2.hpp -- the block2 side of the GB300 drop-in (header-only C++).
+//
+// Included after block2's own headers ("block2_core.hpp", "block2_dmrg.hpp")
+// and linked against libb2g.so.  It adds two subclasses that plug into
+// block2's virtual hooks, so block2's MovingEnvironment, EffectiveHamiltonian
+// and DMRG::solve / sweep run unchanged above the GPU path:
+//
+//   GpuTensorFunctions<S>  a TensorFunctions<S, double> installed as mpo->tf
+//                          (block2 copies it into every EffectiveHamiltonian,
+//                          src/dmrg/effective_hamiltonian.hpp:136).  Its
+//                          operator()(b, c, scale) -- the product Davidson
+//                          calls after EffectiveHamiltonian::precompute has
+//                          recorded the GEMM pairs (src/core/tensor_functions.hpp:59-62,
+//                          src/dmrg/effective_hamiltonian.hpp:514-532) --
+//                          replays the recorded pairs on the GPU instead of
+//                          BatchGEMMSeq::operator() (src/core/batch_gemm.hpp:1570-1690).
+//   GpuDMRG<S>             a DMRG<S, double, double> whose virtual
+//                          two_dot_eigs_and_perturb (src/dmrg/sweep_algorithm.hpp:1183-1268)
+//                          runs the whole Davidson solve on the device
+//                          (b2g_davidson) in the selected arithmetic form, with
+//                          diag(H_eff) computed on the device from the pairs.
+//
+// Errors: a non-zero status of the C ABI becomes std::runtime_error carrying
+// b2g_last_error(), block2's own error convention.  Options this GPU path does
+// not implement (metric, state-specific or projected solves, parallel rules,
+// non-Normal Davidson types, non-Tasked GEMM sequences) raise instead of
+// running on the host.
+#pragma once
+
+#include "b2g.h"
+
+#include <algorithm>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace b2g_block2 {
+
+inline void check(int rc, const char *what) {
+    if (rc != B2G_OK)
+        throw std::runtime_error(std::string(what) + ": " + b2g_last_error());
+}
+
+// One device context shared by every copy of the tensor functions.
+struct Runtime {
+    b2g_context *ctx = nullptr;
+    int form = B2G_FP64;        // arithmetic of the Davidson expansion products
+    // counters over the run (read by the driver program)
+    long long n_heff = 0, n_apply_fp64 = 0, n_apply_reduced = 0;
+    double t_plan = 0, t_upload = 0;
+    explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
+        check(b2g_context_create(device, &ctx), "b2g_context_create");
+    }
+    ~Runtime() {
+        if (ctx != nullptr)
+            b2g_context_destroy(ctx);
+    }
+    Runtime(const Runtime &) = delete;
+    Runtime &operator=(const Runtime &) = delete;
+};
+
+// The GEMM pairs block2 recorded for one H_eff*psi, translated into the C
+// ABI's pair format: psi / sigma pointers (recorded against null base
+// pointers by EffectiveHamiltonian::precompute) become offsets, and the
+// operator pointers become offsets into one packed blob holding every
+// operator element the pairs read.  The blob is the union of the operands'
+// extents, merged where they overlap or touch.
+struct RecordedPairs {
+    std::vector<int32_t> tb0, m0, n0, k0, lda0, ldb0, ta1, m1, n1, k1, lda1, ldc1;
+    std::vector<double> alpha0, alpha1;
+    std::vector<uint64_t> a0, b0, a1, c1;
+    std::vector<double> blob;
+    double mnk = 0;   // block2's multiply-add count of one product
+
+    b2g_pair_seq seq() const {
+        b2g_pair_seq s;
+        s.n_pairs = (int64_t)tb0.size();
+        s.tb0 = tb0.data(), s.m0 = m0.data(), s.n0 = n0.data(), s.k0 = k0.data();
+        s.lda0 = lda0.data(), s.ldb0 = ldb0.data();
+        s.ta1 = ta1.data(), s.m1 = m1.data(), s.n1 = n1.data(), s.k1 = k1.data();
+        s.lda1 = lda1.data(), s.ldc1 = ldc1.data();
+        s.alpha0 = alpha0.data(), s.alpha1 = alpha1.data();
+        s.a0 = a0.data(), s.b0 = b0.data(), s.a1 = a1.data(), s.c1 = c1.data();
+        return s;
+    }
+
+    // doubles spanned by op(X) of shape rows x cols stored with leading dim ld
+    static uint64_t extent(bool trans, int rows, int cols, int ld) {
+        if (rows <= 0 || cols <= 0)
+            return 0;
+        return trans ? (uint64_t)(cols - 1) * ld + rows : (uint64_t)(rows - 1) * ld + cols;
+    }
+
+    template <typename SEQ> void translate(const SEQ &sq, uint64_t nket, uint64_t nbra) {
+        const auto &g0 = *sq.batch[0], &g1 = *sq.batch[1];
+        if (!g0.acidxs.empty() || g0.c.size() != g1.c.size() || g0.gp.size() != g0.c.size() ||
+            g1.gp.size() != g1.c.size())
+            throw std::runtime_error("b2g: the recorded GEMM sequence is not a plain pair list "
+                                     "(SeqTypes::Tasked rotate records expected)");
+        const size_t np = g0.c.size();
+        const double *zero = (const double *)0;
+        tb0.resize(np), m0.resize(np), n0.resize(np), k0.resize(np), lda0.resize(np), ldb0.resize(np);
+        ta1.resize(np), m1.resize(np), n1.resize(np), k1.resize(np), lda1.resize(np), ldc1.resize(np);
+        alpha0.resize(np), alpha1.resize(np), a0.resize(np), b0.resize(np), a1.resize(np), c1.resize(np);
+        struct Span {
+            const double *p;
+            uint64_t n;
+        };
+        std::vector<Span> spans;
+        spans.reserve(2 * np);
+        mnk = 0;
+        for (size_t i = 0; i < np; i++) {
+            if (g0.ta[i] != block2::CblasNoTrans || g1.tb[i] != block2::CblasNoTrans || g0.ldc[i] != g0.n[i] ||
+                g1.ldb[i] != g1.n[i] || g0.c[i] != g1.b[i] || g0.beta[i] != 0.0)
+                throw std::runtime_error("b2g: unexpected work-matrix layout in a recorded pair");
+            tb0[i] = g0.tb[i] != block2::CblasNoTrans, m0[i] = g0.m[i], n0[i] = g0.n[i], k0[i] = g0.k[i];
+            lda0[i] = g0.lda[i], ldb0[i] = g0.ldb[i], alpha0[i] = g0.alpha[i];
+            ta1[i] = g1.ta[i] != block2::CblasNoTrans, m1[i] = g1.m[i], n1[i] = g1.n[i], k1[i] = g1.k[i];
+            lda1[i] = g1.lda[i], ldc1[i] = g1.ldc[i], alpha1[i] = g1.alpha[i];
+            a0[i] = (uint64_t)(g0.a[i] - zero);
+            c1[i] = (uint64_t)(g1.c[i] - zero);
+            if (a0[i] > nket || extent(false, m0[i], k0[i], lda0[i]) > nket - a0[i] ||
+                c1[i] > nbra || extent(false, m1[i], n1[i], ldc1[i]) > nbra - c1[i])
+                throw std::runtime_error("b2g: a recorded psi/sigma operand lies outside the wavefunction");
+            spans.push_back(Span{g0.b[i], extent(tb0[i], k0[i], n0[i], ldb0[i])});
+            spans.push_back(Span{g1.a[i], extent(ta1[i], m1[i], k1[i], lda1[i])});
+            mnk += (double)m0[i] * n0[i] * k0[i] + (double)m1[i] * n1[i] * k1[i];
+        }
+        // merge operand extents into disjoint regions, in address order
+        std::vector<Span> reg(spans);
+        std::sort(reg.begin(), reg.end(), [](const Span &x, const Span &y) { return x.p < y.p; });
+        std::vector<Span> merged;
+        for (auto &s : reg) {
+            if (!merged.empty() && s.p <= merged.back().p + merged.back().n) {
+                const double *end = std::max(merged.back().p + merged.back().n, s.p + s.n);
+                merged.back().n = (uint64_t)(end - merged.back().p);
+            } else
+                merged.push_back(s);
+        }
+        std::vector<uint64_t> off(merged.size());
+        uint64_t total = 0;
+        for (size_t r = 0; r < merged.size(); r++)
+            off[r] = total, total += merged[r].n;
+        auto locate = [&](const double *p) -> uint64_t {
+            auto it = std::upper_bound(merged.begin(), merged.end(), p,
+                                       [](const double *x, const Span &s) { return x < s.p; });
+            const size_t r = (size_t)(it - merged.begin()) - 1;
+            return off[r] + (uint64_t)(p - merged[r].p);
+        };
+        for (size_t i = 0; i < np; i++)
+            b0[i] = locate(g0.b[i]), a1[i] = locate(g1.a[i]);
+        blob.resize(total);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long r = 0; r < (long)merged.size(); r++)
+            std::copy(merged[r].p, merged[r].p + merged[r].n, blob.data() + off[r]);
+    }
+};
+
+// The device plan of one recorded H_eff (built lazily from the sequence the
+// owning tensor functions recorded; destroyed with them or when a different
+// sequence is recorded).
+struct DevicePlan {
+    std::shared_ptr<Runtime> rt;
+    b2g_heff *h = nullptr;
+    uint64_t nket = 0, nbra = 0;
+    double mnk = 0;
+    std::vector<const void *> signature;
+    explicit DevicePlan(const std::shared_ptr<Runtime> &rt) : rt(rt) {}
+    ~DevicePlan() { release(); }
+    void release() {
+        if (h != nullptr)
+            b2g_heff_destroy(h);
+        h = nullptr;
+        signature.clear();
+    }
+    template <typename SEQ> static std::vector<const void *> sign(const SEQ &sq) {
+        const auto &g0 = *sq.batch[0], &g1 = *sq.batch[1];
+        std::vector<const void *> s{&sq, (const void *)(uintptr_t)g0.c.size()};
+        if (!g0.c.empty())
+            s.insert(s.end(), {g0.a.front(), g0.b.front(), g1.a.front(), g1.c.front(), g0.a.back(),
+                               g0.b.back(), g1.a.back(), g1.c.back()});
+        return s;
+    }
+    template <typename SEQ> b2g_heff *get(const SEQ &sq, uint64_t ket_size, uint64_t bra_size) {
+        std::vector<const void *> s = sign(sq);
+        if (h != nullptr && s == signature && ket_size == nket && bra_size == nbra)
+            return h;
+        release();
+        block2::Timer t;
+        t.get_time();
+        RecordedPairs rp;
+        rp.translate(sq, ket_size, bra_size);
+        rt->t_plan += t.get_time();
+        b2g_pair_seq ps = rp.seq();
+        check(b2g_heff_create(rt->ctx, &ps, rp.blob.data(), (uint64_t)rp.blob.size(), 0, ket_size,
+                              bra_size, &h),
+              "b2g_heff_create");
+        rt->t_upload += t.get_time();
+        rt->n_heff++;
+        nket = ket_size, nbra = bra_size, mnk = rp.mnk, signature = s;
+        return h;
+    }
+};
+
+template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, double> {
+    typedef block2::TensorFunctions<S, double> TF;
+    std::shared_ptr<Runtime> rt;
+    std::shared_ptr<DevicePlan> plan;
+    GpuTensorFunctions(const std::shared_ptr<block2::OperatorFunctions<S, double>> &opf,
+                       const std::shared_ptr<Runtime> &rt)
+        : TF(opf), rt(rt), plan(std::make_shared<DevicePlan>(rt)) {
+        if (!(opf->seq->mode & block2::SeqTypes::Tasked))
+            throw std::runtime_error("GpuTensorFunctions: needs threading->seq_type = SeqTypes::Tasked "
+                                     "(the GEMM pairs are recorded by EffectiveHamiltonian::precompute)");
+    }
+    // every copy (one per EffectiveHamiltonian) owns its own device plan
+    std::shared_ptr<TF> copy() const override {
+        return std::make_shared<GpuTensorFunctions<S>>(this->opf->copy(), rt);
+    }
+    b2g_heff *device_plan(uint64_t ket_size, uint64_t bra_size) {
+        return plan->get(*this->opf->seq, ket_size, bra_size);
+    }
+    // c += scale * H_eff b (host buffers), after precompute recorded the pairs
+    void operator()(const block2::GMatrix<double> &b, const block2::GMatrix<double> &c,
+                    double scale = 1.0) override {
+        auto &sq = *this->opf->seq;
+        if (sq.batch[0]->c.empty() && sq.batch[1]->c.empty())
+            return;
+        b2g_heff *h = device_plan((uint64_t)b.size(), (uint64_t)c.size());
+        check(b2g_heff_apply_host(h, b.data, c.data, scale, B2G_FP64), "b2g_heff_apply_host");
+        rt->n_apply_fp64++;
+        sq.cumulative_nflop += (size_t)plan->mnk;
+    }
+};
+
+template <typename S> struct GpuDMRG : block2::DMRG<S, double, double> {
+    typedef block2::DMRG<S, double, double> D;
+    std::shared_ptr<Runtime> rt;
+    GpuDMRG(const std::shared_ptr<block2::MovingEnvironment<S, double, double>> &me,
+            const std::vector<block2::ubond_t> &bond_dims, const std::vector<double> &noises,
+            const std::shared_ptr<Runtime> &rt)
+        : D(me, bond_dims, noises), rt(rt) {}
+    void unsupported_check() const {
+        const char *why = nullptr;
+        if (this->state_specific || !this->projection_weights.empty() || !this->ext_mes.empty())
+            why = "state-specific / projected solves";
+        else if (this->metric_me != nullptr)
+            why = "a metric (generalized) eigenproblem";
+        else if (this->context_ket != nullptr)
+            why = "a context MPS";
+        else if (this->me->para_rule != nullptr)
+            why = "a parallel rule";
+        else if (this->me->bra != this->me->ket)
+            why = "a bra MPS different from the ket";
+        else if (this->davidson_type != block2::DavidsonTypes::Normal)
+            why = "a Davidson type other than Normal";
+        else if (this->davidson_rel_conv_thrd != 0)
+            why = "a relative Davidson threshold";
+        else if (this->eff_kernel != nullptr)
+            why = "an EffectiveKernel hook";
+        if (why != nullptr)
+            throw std::runtime_error(std::string("GpuDMRG: ") + why + " is not implemented on the GPU path");
+    }
+    // DMRG::two_dot_eigs_and_perturb (src/dmrg/sweep_algorithm.hpp:1183-1268)
+    // with the eigensolve on the device.  Timers, callbacks and bookkeeping
+    // follow the reference so the sweep prints and results keep their meaning.
+    typedef typename D::FPLS FPLS;  // the energy type of the sweep (long double)
+    std::tuple<FPLS, int, size_t, double>
+    two_dot_eigs_and_perturb(const bool forward, const int i, const double davidson_conv_thrd,
+                             const double noise,
+                             std::shared_ptr<block2::SparseMatrixGroup<S, double>> &pket) override {
+        unsupported_check();
+        this->_t.get_time();
+        this->torth += this->_t.get_time();
+        // compute_diag = false: the diagonal comes from the device (b2g_heff_diag)
+        std::shared_ptr<block2::EffectiveHamiltonian<S, double>> h_eff = this->me->eff_ham(
+            block2::FuseTypes::FuseLR, forward, false, this->me->bra->tensors[i], this->me->ket->tensors[i]);
+        auto gtf = std::dynamic_pointer_cast<GpuTensorFunctions<S>>(h_eff->tf);
+        if (gtf == nullptr)
+            throw std::runtime_error("GpuDMRG: mpo->tf must be a GpuTensorFunctions");
+        this->sweep_max_eff_ham_size = std::max(this->sweep_max_eff_ham_size, h_eff->op->get_total_memory());
+        this->sweep_max_eff_wfn_size = std::max(this->sweep_max_eff_wfn_size, (size_t)h_eff->ket->total_memory);
+        this->current_eff_ham = h_eff;
+        block2::callback_()->compute("DMRG::sweep::iter.eff_ham", this->iprint);
+        this->current_eff_ham = nullptr;
+        this->teff += this->_t.get_time();
+        block2::Timer t;
+        t.get_time();
+        const uint64_t nket = h_eff->ket->total_memory, nbra = h_eff->bra->total_memory;
+        h_eff->precompute();
+        b2g_heff *h = gtf->device_plan(nket, nbra);
+        std::vector<double> diag(nket);
+        check(b2g_heff_diag_host(h, diag.data()), "b2g_heff_diag_host");
+        b2g_davidson_result res;
+        check(b2g_davidson(h, diag.data(), h_eff->ket->data, davidson_conv_thrd, this->davidson_max_iter,
+                           this->davidson_def_min_size, this->davidson_def_max_size, rt->form, &res),
+              "b2g_davidson");
+        rt->n_apply_fp64 += res.n_apply_fp64;
+        rt->n_apply_reduced += res.n_apply_mixed;
+        const size_t nflop = (size_t)(gtf->plan->mnk * (double)(res.n_apply_fp64 + res.n_apply_mixed));
+        h_eff->post_precompute();
+        gtf->plan->release();
+        std::tuple<FPLS, int, size_t, double> pdi =
+            std::make_tuple((FPLS)res.energy, (int)res.n_iter, nflop, t.get_time());
+        this->teig += this->_t.get_time();
+        this->current_eff_ham = h_eff;
+        block2::callback_()->compute("DMRG::sweep::iter.eff_ham.end", this->iprint);
+        this->current_eff_ham = nullptr;
+        if ((this->noise_type & block2::NoiseTypes::Perturbative) && noise != 0)
+            pket = h_eff->perturbative_noise(forward, i, i + 1, block2::FuseTypes::FuseLR,
+                                             this->me->ket->info, this->noise_type, this->me->para_rule);
+        this->tprt += this->_t.get_time();
+        h_eff->deallocate();
+        return pdi;
+    }
+};
+
+// Installs the GPU tensor functions into an MPO (what a block2 user does
+// once per MPO before building the MovingEnvironment).
+template <typename S>
+void install(const std::shared_ptr<block2::MPO<S, double>> &mpo, const std::shared_ptr<Runtime> &rt) {
+    mpo->tf = std::make_shared<GpuTensorFunctions<S>>(mpo->tf->opf, rt);
+}
+
+} // namespace b2g_block2

@@ -39,7 +39,7 @@ struct Opts {
     vector<double> noises = {0.0};
     vector<double> dav_thrds = {1e-10};
     double tol = 0.0;
-    string out = "/tmp/b2g_dump";
+    string out = "b2g_dump";  // --out: dump directory (relative to the working directory)
     int dump_sweep = 0;       // -1: all sweeps
     int dump_site = -1;       // -1: middle site (n/2-1); -2: all sites
     bool with_data = true;    // false: structure only (no operator blob)

@@ -212,7 +212,9 @@ def main():
                              "SU(2), M=1000, sweep 2 middle site (spectrum and discarded weight)")
         return
     if not os.path.exists(HARNESS):
-        subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+        # block2 sources: $BLOCK2_SRC, else the staged copy (shim/stage_block2.py)
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"),
+                        os.environ.get("BLOCK2_SRC", ""), "harness"], check=True)
     for name, (args, desc) in CASES.items():
         if a.only and name != a.only:
             continue
