@@ -25,6 +25,7 @@ B2G_ERR_STATE = 6
 FP64 = 0
 TF32X3 = 1
 FP32 = 2
+PROBE_FP64_MMA = 16  # b2g_probe_peak only: the FP64 tensor-core instruction (DMMA)
 
 _i32p = C.POINTER(C.c_int32)
 _u64p = C.POINTER(C.c_uint64)
@@ -141,6 +142,7 @@ SIGNATURES = {
     "b2g_heff_set_params": (C.c_int, [C.c_void_p, C.POINTER(PairSeqC), C.c_void_p]),
     "b2g_heff_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "b2g_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,
                                C.c_int, C.c_int, C.POINTER(DavidsonResultC)]),
     "b2g_davidson_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,

@@ -57,3 +57,32 @@ def load_problem(path: str) -> HeffProblem:
     return HeffProblem(pairs=pairs, ops=z["ops"], psi_size=int(meta["psi_size"]),
                        sigma_size=int(meta["sigma_size"]), psi=get("psi"), sigma=get("sigma"),
                        diag=get("diag"), meta=meta, extra=extra)
+
+
+_DUMP_DT = {"i4": np.int32, "u8": np.uint64, "f8": np.float64}
+
+
+def load_dump(path: str) -> HeffProblem:
+    """An H_eff written by the drop-in's dump (b2g_block2::HeffDump, raw
+    arrays + manifest.txt): the translated pairs, the operator blob, the
+    Davidson initial guess (psi), diag(H_eff) and the converged eigenvector."""
+    import os
+
+    arrays, scalars = {}, {}
+    with open(os.path.join(path, "manifest.txt")) as f:
+        for ln in f:
+            t = ln.split()
+            if not t:
+                continue
+            if t[0].startswith("#"):
+                scalars[t[0][1:]] = float(t[1])
+            else:
+                arrays[t[0]] = np.fromfile(os.path.join(path, t[0] + ".bin"), dtype=_DUMP_DT[t[1]],
+                                           count=int(t[2]))
+    pairs = {k: arrays[k] for k in PAIR_FIELDS}
+    extra = {}
+    if "psi_converged" in arrays:
+        extra["psi_converged"] = arrays["psi_converged"]
+    return HeffProblem(pairs=pairs, ops=arrays["ops"], psi_size=int(scalars["psi_size"]),
+                       sigma_size=int(scalars["sigma_size"]), psi=arrays.get("psi"),
+                       diag=arrays.get("diag"), meta=dict(scalars), extra=extra)

@@ -63,9 +63,13 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
               dav=(1e-10,), arms=("gpu:fp64",), warm_sweeps: int = 0, warm_M=None,
               warm_noises=None, warm_dav=None, warm_device: str = "cpu", threads: int | None = None,
               seed: int = 1234, start_site: int = 0, end_site: int = -1, workdir: str | None = None,
-              timeout: float | None = None, env: dict | None = None) -> dict:
+              timeout: float | None = None, env: dict | None = None, dump_heff: str | None = None,
+              dump_arm: int = 0, dump_sweep: int = -1, dump_site: int = -1) -> dict:
     """Runs one dmrg_sweep invocation and returns its JSON report with
-    ``sites`` (parse_sites of its output), ``stdout`` and ``returncode``."""
+    ``sites`` (parse_sites of its output), ``stdout`` and ``cmd``.  With
+    dump_heff, GPU arm ``dump_arm`` writes the H_eff of ``dump_site`` (default:
+    the middle site) in its sweep ``dump_sweep`` to that directory
+    (b2g.problem.load_dump reads it)."""
     if not os.path.exists(binary):
         raise FileNotFoundError(f"{binary} is not built (build() needs block2's headers)")
     lst = lambda v: ",".join(str(x) for x in v)  # noqa: E731
@@ -79,6 +83,9 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
            "--arms", ",".join(arms), "--threads", str(threads), "--seed", str(seed),
            "--iprint", "2", "--json", js, "--scratch", os.path.join(wd, "scratch"),
            "--start-site", str(start_site), "--end-site", str(end_site)]
+    if dump_heff:
+        cmd += ["--dump-heff", os.path.abspath(dump_heff), "--dump-arm", str(dump_arm),
+                "--dump-sweep", str(dump_sweep), "--dump-site", str(dump_site)]
     if warm_sweeps:
         cmd += ["--warm-sweeps", str(warm_sweeps), "--warm-M", lst(warm_M or M),
                 "--warm-noises", lst(warm_noises or noises), "--warm-dav", lst(warm_dav or dav),

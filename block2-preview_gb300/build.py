@@ -114,17 +114,18 @@ def build_sweep_programs(verbose: bool = False, force: bool = False) -> dict:
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
     jobs = []
     if force or _newer(SWEEP, deps + [LIB, os.path.join(ROOT, "include", "b2g.h")]):
-        jobs.append(["bash", os.path.join(SHIM, "build.sh"), src, "gpu", SWEEP])
+        jobs.append((["bash", os.path.join(SHIM, "build.sh"), src, "gpu", SWEEP], SWEEP))
     if force or _newer(ref_bin, deps):
-        jobs.append(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), src])
+        jobs.append((["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), src], ref_bin))
 
-    def run(cmd):
+    def run(job):
+        cmd, out = job
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"{' '.join(cmd)} failed:\n{r.stdout}\n{r.stderr}")
-        return cmd[-1]
+        return out
 
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         done = list(ex.map(run, jobs))

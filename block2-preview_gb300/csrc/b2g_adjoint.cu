@@ -317,6 +317,7 @@ cudaError_t launch_stage(const AdjStage &st, const AdjSrc &src, double *dst, dou
     if (st.n_groups == 0)
         return cudaSuccess;
     const int64_t grid = std::min<int64_t>(st.n_groups, (int64_t)1 << 20);
+    note_launch();
     adj_items<<<(unsigned)grid, 256, 0, s>>>(st.items, st.grp, st.n_groups, src, dst, scale);
     return cudaGetLastError();
 }

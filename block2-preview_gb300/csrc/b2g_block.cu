@@ -218,6 +218,7 @@ static int block_contract(b2g_context *ctx, const b2g_block_seq *seq, const doub
         step(cudaMemcpyAsync(d_ia, ia_s.data(), sizeof(BlkIadd) * ia_s.size(), cudaMemcpyHostToDevice, s));
         step(cudaMemcpyAsync(d_iag, ia_grp.data(), sizeof(int64_t) * ia_grp.size(), cudaMemcpyHostToDevice, s));
         if (e == cudaSuccess) {
+            note_launch();
             iadd_kernel<<<(unsigned)(ia_grp.size() - 1), 256, 0, s>>>(d_ia, d_iag, d_env, d_site, d_tmp);
             step(cudaGetLastError());
         }
@@ -226,6 +227,7 @@ static int block_contract(b2g_context *ctx, const b2g_block_seq *seq, const doub
         step(cudaMemcpyAsync(d_kr, kr_s.data(), sizeof(BlkKron) * kr_s.size(), cudaMemcpyHostToDevice, s));
         step(cudaMemcpyAsync(d_krg, kr_grp.data(), sizeof(int64_t) * kr_grp.size(), cudaMemcpyHostToDevice, s));
         if (e == cudaSuccess) {
+            note_launch();
             kron_kernel<<<(unsigned)(kr_grp.size() - 1), 256, 0, s>>>(d_kr, d_krg, d_env, d_site, d_tmp, d_out);
             step(cudaGetLastError());
         }

@@ -2,6 +2,7 @@
 // creation/upload, H_eff*psi in the FP64, FP32 and TF32x3 (tensor-core)
 // forms for one or several roots, diag(H_eff), timing and the FP64 probe.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -18,6 +19,22 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int code, const std::string &msg) {
     set_error(msg);
     return code;
+}
+
+static std::atomic<uint64_t> g_launches{0};
+static thread_local int g_capturing = 0;
+static thread_local uint64_t g_captured = 0;
+
+void note_launch(uint64_t n) {
+    if (g_capturing)
+        g_captured += n;
+    else
+        g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+void capture_begin() { g_capturing = 1, g_captured = 0; }
+uint64_t capture_end() {
+    g_capturing = 0;
+    return g_captured;
 }
 
 template <typename T> static int upload(const std::vector<T> &v, T **dst, cudaStream_t s) {
@@ -362,6 +379,10 @@ int b2g_probe_peak(b2g_context *ctx, int form, double *tflops) {
         B2G_CUDA_TRY(probe_fp64_peak(ctx->stream, ctx->n_sm, tflops));
         return B2G_OK;
     }
+    if (form == B2G_PROBE_FP64_MMA) {
+        B2G_CUDA_TRY(probe_fp64_mma_peak(ctx->stream, ctx->n_sm, tflops));
+        return B2G_OK;
+    }
     return fail(B2G_ERR_UNSUPPORTED, "b2g_probe_peak: form not available");
 }
 
@@ -369,6 +390,13 @@ int b2g_heff_stats_get(const b2g_heff *h, b2g_heff_stats *out) {
     if (h == nullptr || out == nullptr)
         return fail(B2G_ERR_ARG, "b2g_heff_stats_get: null argument");
     *out = h->stats;
+    return B2G_OK;
+}
+
+int b2g_launch_count(uint64_t *out) {
+    if (out == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_launch_count: null argument");
+    *out = g_launches.load(std::memory_order_relaxed);
     return B2G_OK;
 }
 
@@ -498,6 +526,7 @@ static int apply_graphed(b2g_heff *h, const double *psi, double *sigma, int nroo
     g->last = ++h->graph_tick;
     if (g->state == 1) {
         B2G_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+        note_launch(g->n_kernels);
         return B2G_OK;
     }
     if (g->state < 0)
@@ -507,7 +536,9 @@ static int apply_graphed(b2g_heff *h, const double *psi, double *sigma, int nroo
         g->state = -1;
         return apply_launches(h, psi, sigma, nroots, scale, form);
     }
+    capture_begin();
     const int rc = apply_launches(h, psi, sigma, nroots, scale, form);
+    g->n_kernels = capture_end();
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(s, &graph);
     if (rc != B2G_OK) {
@@ -528,6 +559,7 @@ static int apply_graphed(b2g_heff *h, const double *psi, double *sigma, int nroo
     }
     g->state = 1;
     B2G_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+    note_launch(g->n_kernels);
     return B2G_OK;
 }
 

@@ -456,6 +456,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     // about four elements per thread: short per-thread FP64 chains and few partials
     const int dot_blocks = (int)std::min<uint64_t>(kRedBlocks, std::max<uint64_t>(1, (n + 1023) / 1024));
     auto dot_many = [&](const double *Xv, int nv, const double *y, double *out) {
+        note_launch();
         multidot<<<dot_blocks, kRedThreads, 0, st>>>(Xv, n, nv, y, n, partial, dot_counter, out);
     };
     std::vector<double> lam(kMaxSub), qq(kMaxSub);
@@ -474,6 +475,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     auto append = [&](double *q) -> int {
         for (int pass = 0; pass < 2 && m > 0; pass++) {
             dot_many(B, m, q, coef);
+            note_launch();
             combine<<<g, 256, 0, st>>>(q, 1.0, B, n, m, coef, -1.0, n);
         }
         dot_many(q, 1, q, sc + 1);
@@ -483,6 +485,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             return -1;
         if (!(nrm2 > 1e-28))
             return 0;
+        note_launch();
         normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)m * n, q, sc + 1, n);
         m++;
         return 1;
@@ -500,6 +503,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
         (pform == B2G_FP64 ? n_fp64 : n_mixed) += nn;
         for (int i = msig; i < m; i++) {
             dot_many(S, i + 1, B + (uint64_t)i * n, dots);
+            note_launch();
             set_sub_row<<<1, kMaxSub, 0, st>>>(A, kMaxSub, i, dots);
         }
         msig = m;
@@ -509,17 +513,25 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
     auto ritz = [&]() -> bool {
         if (vw > 0 && vw < m) {
             std::swap(V, Vprev);
+            note_launch();
             sub_warm_right<<<m, 64, 0, st>>>(A, m, vw, Vprev, T);
+            note_launch();
             sub_warm_left<<<m, 64, 0, st>>>(T, m, vw, Vprev, A2);
+            note_launch();
             jacobi_eig<<<1, 256, 0, st>>>(A2, kMaxSub, m, w, T);
+            note_launch();
             sub_warm_vec<<<m, 64, 0, st>>>(Vprev, m, vw, T, V);
         } else {
+            note_launch();
             jacobi_eig<<<1, 256, 0, st>>>(A, kMaxSub, m, w, V);
         }
         vw = m;
+        note_launch();
         rotate_basis<<<g, 256, 0, st>>>(X, B, n, m, k, V, kMaxSub, n);
+        note_launch();
         rotate_basis<<<g, 256, 0, st>>>(SX, S, n, m, k, V, kMaxSub, n);
         for (int i = 0; i < k; i++) {
+            note_launch();
             residual_olsen<<<g, 256, 0, st>>>(Q + (uint64_t)i * n, t, SX + (uint64_t)i * n,
                                               X + (uint64_t)i * n, D, w + i, n, 0);
             dot_many(Q + (uint64_t)i * n, 1, Q + (uint64_t)i * n, qqd + i);
@@ -586,12 +598,15 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             n_unconv += qq[i] >= (reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i])
                                                           : conv_thrd);
         if (m + n_unconv > def_max) {
+            note_launch();
             rotate_basis<<<g, 256, 0, st>>>(R, B, n, m, def_min, V, kMaxSub, n);
             if (!cuda_ok(cudaMemcpyAsync(B, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st), "B"))
                 goto done;
+            note_launch();
             rotate_basis<<<g, 256, 0, st>>>(R, S, n, m, def_min, V, kMaxSub, n);
             if (!cuda_ok(cudaMemcpyAsync(S, R, sizeof(double) * n * def_min, cudaMemcpyDeviceToDevice, st), "S"))
                 goto done;
+            note_launch();
             set_sub_diag<<<1, 256, 0, st>>>(A, kMaxSub, def_min, w);
             m = msig = def_min;
             vw = 0;
@@ -607,15 +622,19 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             if (qq[i] < thr || mp >= def_max)
                 continue;
             double *q = Q + (uint64_t)i * n, *x = X + (uint64_t)i * n;
+            note_launch();
             residual_olsen<<<g, 256, 0, st>>>(q, t, SX + (uint64_t)i * n, x, D, w + i, n, 1);
             dot_many(q, 1, x, sc + 2);
             dot_many(t, 1, x, sc + 3);
+            note_launch();
             olsen_update<<<g, 256, 0, st>>>(q, t, sc + 2, n);
             for (int pass = 0; pass < 2 && mp > 0; pass++) {
                 dot_many(B, mp, q, coef);
+                note_launch();
                 combine<<<g, 256, 0, st>>>(q, 1.0, B, n, mp, coef, -1.0, n);
             }
             dot_many(q, 1, q, dots + (mp - m));
+            note_launch();
             normalize_into<<<g, 256, 0, st>>>(B + (uint64_t)mp * n, q, dots + (mp - m), n);
             mp++;
         }

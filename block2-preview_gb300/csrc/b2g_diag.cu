@@ -72,6 +72,7 @@ cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cu
         return cudaSuccess;
     if (p.n_regions > 65535)
         return cudaErrorInvalidConfiguration;
+    note_launch();
     diag_kernel<<<dim3((unsigned)((maxcells + 255) / 256), (unsigned)p.n_regions), 256, 0, s>>>(
         p.regions, p.region_cb, p.contribs, p.works, ops, diag);
     return cudaGetLastError();

@@ -736,6 +736,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
         std::vector<double> de(2 * wtot);
         if (nb && maxdim > 0) {
             const int64_t cells = (int64_t)maxdim * maxdim;
+            note_launch();
             rho_kernel<<<dim3((unsigned)((cells + 255) / 256), nb), 256, 0, s>>>(
                 d_psi, d_lptr, d_list, d_prow, d_pcol, d_poff, d_dim, d_roff, d_rho, tr ? 1 : 0);
             DM_TRY(cudaGetLastError());
@@ -748,6 +749,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
             DM_TRY(cudaStreamWaitEvent(s2, ev_rho, 0));
             const size_t smem = sizeof(double) * 5 * (size_t)maxdim;
             DM_TRY(cudaFuncSetAttribute(eig_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            note_launch();
             eig_block<<<nb, kEigThreads, smem, s2>>>(d_rho, d_z, d_dim, d_roff, d_de, d_woff,
                                                       nbig ? kDmClusterMin : kDmMaxDim + 1);
             DM_TRY(cudaGetLastError());
@@ -756,6 +758,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
                 const size_t smem_c = sizeof(double) * 5 * (size_t)maxbig;
                 DM_TRY(cudaFuncSetAttribute(eig_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem_c));
+                note_launch();
                 eig_cluster<<<kDmCluster * nbig, kEigThreads, smem_c, s>>>(d_rho, d_z, d_dim, d_roff, d_de,
                                                                           d_woff, d_big, d_scr, d_scroff);
                 DM_TRY(cudaGetLastError());
@@ -833,11 +836,13 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
                 const size_t smem_r = sizeof(double) * 34 * (size_t)maxdim;
                 DM_TRY(cudaFuncSetAttribute(apply_rotations_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem_r));
+                note_launch();
                 apply_rotations_smem<<<dim3((unsigned)((maxdim + 31) / 32), nb), 32, smem_r, s>>>(
                     d_z, d_dim, d_roff, d_itf, (const int32_t *)(recs + r1), (const int32_t *)(recs + r2),
                     (const int64_t *)(recs + r0), (const double *)(recs + r3), (const double *)(recs + r4));
                 DM_TRY(cudaGetLastError());
             } else if (nb && maxdim > 0) {
+                note_launch();
                 apply_rotations<<<dim3((unsigned)((maxdim + 63) / 64), nb), 64, 0, s>>>(
                     d_z, d_dim, d_roff, d_itf, (const int32_t *)(recs + r1), (const int32_t *)(recs + r2),
                     (const int64_t *)(recs + r0), (const double *)(recs + r3), (const double *)(recs + r4));
@@ -904,6 +909,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
             DM_TRY(cudaMemcpyAsync(d_q, q.data(), sizeof(int32_t) * 3 * nk, cudaMemcpyHostToDevice, s));
             DM_TRY(cudaMemcpyAsync(d_kept, kept, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, s));
             DM_TRY(cudaMemcpyAsync(d_rotoff, rot_off.data(), sizeof(uint64_t) * nb, cudaMemcpyHostToDevice, s));
+            note_launch();
             gather_rotation<<<nk, 256, 0, s>>>(d_rot, d_z, d_q, d_q + nk, d_q + 2 * nk, d_dim, d_kept, d_roff,
                                                d_rotoff, nk, tr ? 1 : 0);
             DM_TRY(cudaGetLastError());
@@ -937,6 +943,7 @@ extern "C" int b2g_dm_truncate(b2g_context *ctx, const b2g_dm_layout *lay, const
         if (!tasks.empty()) {
             DM_TRY(cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(SplitTask) * tasks.size(), cudaMemcpyHostToDevice, s));
             const double *xb = tr ? d_rot : d_psi, *yb = tr ? d_psi : d_rot;
+            note_launch();
             split_gemm<<<dim3((unsigned)((max_el + 255) / 256), (unsigned)tasks.size()), 256, 0, s>>>(
                 d_out, xb, yb, d_tasks);
             DM_TRY(cudaGetLastError());

@@ -263,6 +263,7 @@ cudaError_t launch_g1_build_a(const DevicePlan &p, const float *ops32, unsigned 
                               cudaStream_t s) {
     if (p.n_g1aimg == 0)
         return cudaSuccess;
+    note_launch();
     g1_build_a<<<(unsigned)p.n_g1aimg, 256, 0, s>>>(p.g1aimg, ops32, aimg);
     return cudaGetLastError();
 }
@@ -280,11 +281,13 @@ cudaError_t launch_g1(const DevicePlan &p, const unsigned char *aimg, const unsi
             return e;
         attr_set = true;
     }
+    note_launch();
     g1_kernel<<<dim3((unsigned)p.n_g1task, rs.nroots), kG1Threads, kG1SmemBytes, s>>>(
         p.g1task, p.g1tile, p.g1stage, aimg, wimg, part, err, rs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
+    note_launch();
     g1_reduce<<<dim3((unsigned)p.n_g1red, rs.nroots), 256, 0, s>>>(p.g1red, p.g1cover, p.g1tile,
                                                                   p.regions, part, sigma, scale, rs);
     return cudaGetLastError();

@@ -14,6 +14,14 @@ namespace b2g {
 void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 
+// Kernel-launch accounting (b2g_launch_count): every launch site calls
+// note_launch(); launches made while a stream capture is being recorded on
+// this thread count towards the graph being built instead, and each replay of
+// a captured graph adds the kernels it holds.
+void note_launch(uint64_t n = 1);
+void capture_begin();
+uint64_t capture_end();   // kernels recorded since capture_begin()
+
 #define B2G_CUDA_TRY(expr)                                                                  \
     do {                                                                                    \
         cudaError_t _e = (expr);                                                            \
@@ -251,6 +259,7 @@ cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work,
 cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t s);
 // compute-ceiling probe: TFLOP/s of a register-resident FP64 FMA loop
 cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops);
+cudaError_t probe_fp64_mma_peak(cudaStream_t s, int n_sm, double *tflops);
 
 } // namespace b2g
 
@@ -270,6 +279,7 @@ struct ApplyGraph {
     int nroots = 0, form = 0;
     double scale = 0.0;
     cudaGraphExec_t exec = nullptr;
+    uint64_t n_kernels = 0;  // kernels the captured graph launches
     int state = 0;        // 0 seen once, 1 captured, -1 not capturable (runs eagerly)
     uint64_t last = 0;    // LRU tick
 };

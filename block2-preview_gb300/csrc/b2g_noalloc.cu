@@ -186,8 +186,10 @@ extern "C" int b2g_heff_apply_noalloc(const b2g_pair_seq *seq, const double *ops
         // pageable source: the call returns once the data is staged, so the
         // host array may be refilled for the next chunk
         B2G_CUDA_TRY(cudaMemcpyAsync(d_desc, g_host_desc, sizeof(NaPair) * n, cudaMemcpyHostToDevice, s));
+        note_launch();
         na_gemm0<<<n, 128, 0, s>>>(d_desc, ops, psi, d_work);
         B2G_CUDA_TRY(cudaGetLastError());
+        note_launch();
         na_gemm1<<<n, 128, 0, s>>>(d_desc, ops, d_work, sigma, scale);
         B2G_CUDA_TRY(cudaGetLastError());
     }

@@ -260,6 +260,28 @@ __global__ void __launch_bounds__(256) fp64_fma_loop(double *out, int iters, dou
         out[0] = s;
 }
 
+// FP64 tensor-core (DMMA) throughput: eight independent accumulator chains of
+// mma.sync m8n8k4 f64 per warp (512 FLOP per warp instruction), registers only.
+__global__ void __launch_bounds__(256) fp64_mma_loop(double *out, int iters) {
+    const double a = 1.0 + threadIdx.x * 1e-9, b = 0.999999;
+    double c[8][2];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        c[j][0] = j * 1e-3, c[j][1] = -j * 1e-3;
+    for (int i = 0; i < iters; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(c[j][0]), "+d"(c[j][1])
+                         : "d"(a), "d"(b));
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        s += c[j][0] + c[j][1];
+    if (s == 12345.678)  // never true: keeps the loop live
+        out[0] = s;
+}
+
 __global__ void to_float(const double *__restrict__ x, float *__restrict__ y, uint64_t n) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
@@ -276,8 +298,10 @@ cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops) {
     cudaEvent_t a, b;
     cudaEventCreate(&a), cudaEventCreate(&b);
     const int blocks = n_sm * 8, iters = 4096;
+    note_launch();
     fp64_fma_loop<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);  // warm-up
     cudaEventRecord(a, s);
+    note_launch();
     fp64_fma_loop<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);
     cudaEventRecord(b, s);
     e = cudaEventSynchronize(b);
@@ -291,10 +315,37 @@ cudaError_t probe_fp64_peak(cudaStream_t s, int n_sm, double *tflops) {
     return e;
 }
 
+cudaError_t probe_fp64_mma_peak(cudaStream_t s, int n_sm, double *tflops) {
+    double *out = nullptr;
+    cudaError_t e = cudaMalloc(&out, sizeof(double));
+    if (e != cudaSuccess)
+        return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a), cudaEventCreate(&b);
+    const int blocks = n_sm * 8, iters = 1024;
+    note_launch();
+    fp64_mma_loop<<<blocks, 256, 0, s>>>(out, iters);  // warm-up
+    cudaEventRecord(a, s);
+    note_launch();
+    fp64_mma_loop<<<blocks, 256, 0, s>>>(out, iters);
+    cudaEventRecord(b, s);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    // per warp instruction 8 x 8 x 4 multiply-adds; 8 per iteration; 8 warps per block
+    *tflops = 2.0 * 256.0 * 8.0 * iters * (double)blocks * 8 / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(a), cudaEventDestroy(b);
+    cudaFree(out);
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    return e;
+}
+
 cudaError_t launch_to_float(const double *x, float *y, uint64_t n, cudaStream_t s) {
     if (n == 0)
         return cudaSuccess;
     const uint64_t b = (n + 255) / 256;
+    note_launch();
     to_float<<<(unsigned)(b < 152 * 16 ? b : 152 * 16), 256, 0, s>>>(x, y, n);
     return cudaGetLastError();
 }
@@ -305,6 +356,7 @@ cudaError_t launch_simt_phase1(const DevicePlan &p, const T *ops, const T *psi, 
     if (p.n_t1 == 0)
         return cudaSuccess;
     const int64_t blocks = (p.n_t1 + 3) / 4;
+    note_launch();
     simt_phase1<T><<<dim3((unsigned)blocks, rs.nroots), 128, 0, s>>>(p.works, p.t1, p.n_t1, ops, psi,
                                                                      work, rs);
     return cudaGetLastError();
@@ -315,11 +367,13 @@ cudaError_t launch_simt_phase2(const DevicePlan &p, const T *ops, const T *work,
                                T *part, double scale, const RootStrides &rs, cudaStream_t s) {
     if (p.n_t2 == 0)
         return cudaSuccess;
+    note_launch();
     simt_phase2<T><<<dim3((unsigned)p.n_t2, rs.nroots), 128, 0, s>>>(
         p.t2, p.lists, p.contribs, p.regions, p.works, ops, work, sigma, part, scale, rs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.n_t2multi == 0)
         return e;
+    note_launch();
     simt_reduce<T><<<dim3((unsigned)p.n_t2multi, rs.nroots), 128, 0, s>>>(p.t2multi, p.regions, part,
                                                                           sigma, scale, rs);
     return cudaGetLastError();

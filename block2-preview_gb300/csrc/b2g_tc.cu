@@ -289,6 +289,7 @@ static cudaError_t launch_g0_class(const G0Tile *tiles, int64_t n, const DeviceP
             return e;
         attr_set = true;
     }
+    note_launch();
     g0_kernel<kRingBytes, kTmemCols, kMinBlocks><<<dim3((unsigned)n, rs.nroots), kThreads, smem, s>>>(
         tiles, p.g0col, aimg, psi_packed, wimg, err, rs);
     return cudaGetLastError();
@@ -299,6 +300,7 @@ cudaError_t launch_g0(const DevicePlan &p, const unsigned char *aimg, const doub
                       cudaStream_t s) {
     if (p.n_g0tile == 0)
         return cudaSuccess;
+    note_launch();
     g0_pack_psi<<<dim3((unsigned)p.n_g0psi, rs.nroots), 256, 0, s>>>(p.g0psi, psi, psi_packed, rs,
                                                                     p.g0_psi_floats);
     cudaError_t e = cudaGetLastError();

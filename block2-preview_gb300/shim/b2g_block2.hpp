@@ -30,6 +30,7 @@
 #include "b2g.h"
 
 #include <algorithm>
+#include <fstream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -49,6 +50,7 @@ struct Runtime {
     // counters over the run (read by the driver program)
     long long n_heff = 0, n_apply_fp64 = 0, n_apply_reduced = 0;
     double t_plan = 0, t_upload = 0;
+    double t_davidson = 0;      // wall time inside b2g_davidson (device-resident solves)
     explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
         check(b2g_context_create(device, &ctx), "b2g_context_create");
     }
@@ -182,14 +184,17 @@ struct DevicePlan {
                                g0.b.back(), g1.a.back(), g1.c.back()});
         return s;
     }
-    template <typename SEQ> b2g_heff *get(const SEQ &sq, uint64_t ket_size, uint64_t bra_size) {
+    // keep: when given, receives the translated pairs and blob (for dumps)
+    template <typename SEQ>
+    b2g_heff *get(const SEQ &sq, uint64_t ket_size, uint64_t bra_size, RecordedPairs *keep = nullptr) {
         std::vector<const void *> s = sign(sq);
-        if (h != nullptr && s == signature && ket_size == nket && bra_size == nbra)
+        if (h != nullptr && s == signature && ket_size == nket && bra_size == nbra && keep == nullptr)
             return h;
         release();
         block2::Timer t;
         t.get_time();
-        RecordedPairs rp;
+        RecordedPairs local;
+        RecordedPairs &rp = keep != nullptr ? *keep : local;
         rp.translate(sq, ket_size, bra_size);
         rt->t_plan += t.get_time();
         b2g_pair_seq ps = rp.seq();
@@ -218,8 +223,8 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
     std::shared_ptr<TF> copy() const override {
         return std::make_shared<GpuTensorFunctions<S>>(this->opf->copy(), rt);
     }
-    b2g_heff *device_plan(uint64_t ket_size, uint64_t bra_size) {
-        return plan->get(*this->opf->seq, ket_size, bra_size);
+    b2g_heff *device_plan(uint64_t ket_size, uint64_t bra_size, RecordedPairs *keep = nullptr) {
+        return plan->get(*this->opf->seq, ket_size, bra_size, keep);
     }
     // c += scale * H_eff b (host buffers), after precompute recorded the pairs
     void operator()(const block2::GMatrix<double> &b, const block2::GMatrix<double> &c,
@@ -234,9 +239,36 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
     }
 };
 
+// Writes one H_eff as raw little-endian arrays plus a manifest ("name dtype
+// count" lines and "#key value" scalars): the translated pairs, the operator
+// blob, the Davidson initial guess psi, diag(H_eff), and after the solve the
+// eigenvector and energy -- a real-operator problem for measurements.
+struct HeffDump {
+    std::string dir;
+    std::ofstream man;
+    explicit HeffDump(const std::string &d) : dir(d), man(d + "/manifest.txt") { man.precision(17); }
+    template <typename T> void arr(const char *name, const std::vector<T> &v, const char *dt) {
+        std::ofstream f(dir + "/" + name + ".bin", std::ios::binary);
+        f.write((const char *)v.data(), (std::streamsize)(sizeof(T) * v.size()));
+        man << name << " " << dt << " " << v.size() << "\n";
+    }
+    void scalar(const char *name, double v) { man << "#" << name << " " << v << "\n"; }
+    void pairs(const RecordedPairs &rp) {
+        arr("tb0", rp.tb0, "i4"), arr("m0", rp.m0, "i4"), arr("n0", rp.n0, "i4"), arr("k0", rp.k0, "i4");
+        arr("lda0", rp.lda0, "i4"), arr("ldb0", rp.ldb0, "i4"), arr("ta1", rp.ta1, "i4");
+        arr("m1", rp.m1, "i4"), arr("n1", rp.n1, "i4"), arr("k1", rp.k1, "i4"), arr("lda1", rp.lda1, "i4");
+        arr("ldc1", rp.ldc1, "i4"), arr("alpha0", rp.alpha0, "f8"), arr("alpha1", rp.alpha1, "f8");
+        arr("a0", rp.a0, "u8"), arr("b0", rp.b0, "u8"), arr("a1", rp.a1, "u8"), arr("c1", rp.c1, "u8");
+        arr("ops", rp.blob, "f8");
+    }
+};
+
 template <typename S> struct GpuDMRG : block2::DMRG<S, double, double> {
     typedef block2::DMRG<S, double, double> D;
     std::shared_ptr<Runtime> rt;
+    // optional: dump the H_eff of site dump_site in sweep dump_sweep to dump_dir
+    std::string dump_dir;
+    int dump_sweep = -1, dump_site = -1;
     GpuDMRG(const std::shared_ptr<block2::MovingEnvironment<S, double, double>> &me,
             const std::vector<block2::ubond_t> &bond_dims, const std::vector<double> &noises,
             const std::shared_ptr<Runtime> &rt)
@@ -289,13 +321,36 @@ template <typename S> struct GpuDMRG : block2::DMRG<S, double, double> {
         t.get_time();
         const uint64_t nket = h_eff->ket->total_memory, nbra = h_eff->bra->total_memory;
         h_eff->precompute();
-        b2g_heff *h = gtf->device_plan(nket, nbra);
+        const bool dump = !dump_dir.empty() && this->isweep == dump_sweep && i == dump_site;
+        std::unique_ptr<RecordedPairs> kept(dump ? new RecordedPairs() : nullptr);
+        b2g_heff *h = gtf->device_plan(nket, nbra, kept.get());
         std::vector<double> diag(nket);
         check(b2g_heff_diag_host(h, diag.data()), "b2g_heff_diag_host");
+        std::unique_ptr<HeffDump> dw;
+        if (dump) {
+            dw.reset(new HeffDump(dump_dir));
+            dw->pairs(*kept);
+            kept.reset();
+            dw->arr("psi", std::vector<double>(h_eff->ket->data, h_eff->ket->data + nket), "f8");
+            dw->arr("diag", diag, "f8");
+            dw->scalar("psi_size", (double)nket), dw->scalar("sigma_size", (double)nbra);
+            dw->scalar("isweep", this->isweep), dw->scalar("site", i), dw->scalar("forward", forward);
+            dw->scalar("conv_thrd", davidson_conv_thrd), dw->scalar("n_sites", this->me->n_sites);
+            dw->scalar("const_e", (double)this->me->mpo->const_e);
+            dw->scalar("def_min", this->davidson_def_min_size), dw->scalar("def_max", this->davidson_def_max_size);
+        }
+        block2::Timer td;
+        td.get_time();
         b2g_davidson_result res;
         check(b2g_davidson(h, diag.data(), h_eff->ket->data, davidson_conv_thrd, this->davidson_max_iter,
                            this->davidson_def_min_size, this->davidson_def_max_size, rt->form, &res),
               "b2g_davidson");
+        rt->t_davidson += td.get_time();
+        if (dw != nullptr) {
+            dw->arr("psi_converged", std::vector<double>(h_eff->ket->data, h_eff->ket->data + nket), "f8");
+            dw->scalar("davidson_energy", res.energy), dw->scalar("davidson_iterations", res.n_iter);
+            dw->man.flush();
+        }
         rt->n_apply_fp64 += res.n_apply_fp64;
         rt->n_apply_reduced += res.n_apply_mixed;
         const size_t nflop = (size_t)(gtf->plan->mnk * (double)(res.n_apply_fp64 + res.n_apply_mixed));

@@ -16,7 +16,8 @@
 //            its own MovingEnvironment; so every arm starts from the same state
 //            with the same schedule, and arms can be compared sweep by sweep.
 // An arm is "cpu" (block2's own CPU path) or "gpu:FORM" (FORM = fp64, tf32x3,
-// fp32): b2g_block2::GpuTensorFunctions installed as mpo->tf and
+// fp32), optionally with "/K" to run K sweeps instead of --sweeps; a GPU arm has
+// b2g_block2::GpuTensorFunctions installed as mpo->tf and
 // b2g_block2::GpuDMRG as the sweep driver, so every Davidson solve runs on the
 // device.  Built with -DB2G_REFERENCE_ONLY the program has no GPU code at all
 // and accepts only cpu arms.
@@ -55,6 +56,9 @@ struct Opts {
     double tol = 0.0;
     string json, scratch = "";
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
+    // GPU arms: dump the H_eff of one site of one sweep of arm dump_arm
+    string dump_dir;
+    int dump_arm = 0, dump_sweep = -1, dump_site = -1;
 };
 
 static void mkdirs(const string &p) {
@@ -68,6 +72,9 @@ static void mkdirs(const string &p) {
 
 struct SweepPhase {
     double wall, teff, teig, tprt, tblk, tmve, tdm, tsplt, trot, tctr, tmid, tint, tdctr, tdiag, tinfo;
+    // GPU arms: time inside the device Davidson solves, the pair translation
+    // and the plan build + operator upload during the sweep
+    double gdav = 0, gtranslate = 0, gplan = 0;
 };
 
 // Times each sweep and reads the reference's own per-phase timers when it
@@ -77,17 +84,30 @@ template <typename S> struct PhaseRecorder : CallbackKernel {
     DMRG<S, double, double> *d = nullptr;
     mutable vector<SweepPhase> phases;
     mutable Timer t;
+#ifndef B2G_REFERENCE_ONLY
+    b2g_block2::Runtime *rt = nullptr;
+    mutable double g0[3] = {0, 0, 0};
+#endif
     void compute(const string &name, int iprint) const override {
         if (d == nullptr)
             return;
-        if (name == "DMRG::sweep.start")
+        if (name == "DMRG::sweep.start") {
+#ifndef B2G_REFERENCE_ONLY
+            if (rt != nullptr)
+                g0[0] = rt->t_davidson, g0[1] = rt->t_plan, g0[2] = rt->t_upload;
+#endif
             t.get_time();
+        }
         if (name != "DMRG::sweep.end")
             return;
         auto &me = *d->me;
-        phases.push_back(SweepPhase{t.get_time(), d->teff, d->teig, d->tprt, d->tblk, d->tmve, d->tdm,
-                                    d->tsplt, me.trot, me.tctr, me.tmid, me.tint, me.tdctr, me.tdiag,
-                                    me.tinfo});
+        SweepPhase p{t.get_time(), d->teff, d->teig, d->tprt, d->tblk, d->tmve, d->tdm,
+                     d->tsplt, me.trot, me.tctr, me.tmid, me.tint, me.tdctr, me.tdiag, me.tinfo};
+#ifndef B2G_REFERENCE_ONLY
+        if (rt != nullptr)
+            p.gdav = rt->t_davidson - g0[0], p.gtranslate = rt->t_plan - g0[1], p.gplan = rt->t_upload - g0[2];
+#endif
+        phases.push_back(p);
     }
 };
 
@@ -130,7 +150,7 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
             pb.rt = make_shared<b2g_block2::Runtime>(0, f);
         pb.rt->form = f;
         pb.rt->n_heff = pb.rt->n_apply_fp64 = pb.rt->n_apply_reduced = 0;
-        pb.rt->t_plan = pb.rt->t_upload = 0;
+        pb.rt->t_plan = pb.rt->t_upload = pb.rt->t_davidson = 0;
         b2g_block2::install<S>(pb.mpo, pb.rt);
     }
 #else
@@ -146,9 +166,15 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
     me->cached_contraction = true;
     shared_ptr<DMRG<S, FL, FL>> dmrg;
 #ifndef B2G_REFERENCE_ONLY
-    if (gpu)
-        dmrg = make_shared<b2g_block2::GpuDMRG<S>>(me, bdims, sc.noises, pb.rt);
-    else
+    if (gpu) {
+        auto gd = make_shared<b2g_block2::GpuDMRG<S>>(me, bdims, sc.noises, pb.rt);
+        if (!o.dump_dir.empty() && tag == "ARM" + to_string(o.dump_arm)) {
+            mkdirs(o.dump_dir);
+            gd->dump_dir = o.dump_dir, gd->dump_sweep = o.dump_sweep;
+            gd->dump_site = o.dump_site >= 0 ? o.dump_site : pb.n / 2 - 1;
+        }
+        dmrg = gd;
+    } else
 #endif
         dmrg = make_shared<DMRG<S, FL, FL>>(me, bdims, sc.noises);
     dmrg->davidson_conv_thrds = sc.dav_thrds;
@@ -159,6 +185,10 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
         dmrg->sweep_end_site = o.end_site;
     auto rec = make_shared<PhaseRecorder<S>>();
     rec->d = dmrg.get();
+#ifndef B2G_REFERENCE_ONLY
+    if (gpu)
+        rec->rt = pb.rt.get();
+#endif
     callback_() = rec;
     cout << "== stage " << tag << ": " << device << ", " << sc.nsweeps << " sweeps" << endl;
     Timer t;
@@ -189,7 +219,8 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
            << ", \"tblk\": " << p.tblk << ", \"tmve\": " << p.tmve << ", \"tdm\": " << p.tdm
            << ", \"tsplt\": " << p.tsplt << ", \"trot\": " << p.trot << ", \"tctr\": " << p.tctr
            << ", \"tmid\": " << p.tmid << ", \"tint\": " << p.tint << ", \"tdctr\": " << p.tdctr
-           << ", \"tdiag\": " << p.tdiag << ", \"tinfo\": " << p.tinfo << "}";
+           << ", \"tdiag\": " << p.tdiag << ", \"tinfo\": " << p.tinfo << ", \"gpu_davidson\": " << p.gdav
+           << ", \"gpu_translate\": " << p.gtranslate << ", \"gpu_plan_upload\": " << p.gplan << "}";
     }
     js << "]";
     // block structure of the final MPS: per site tensor, each block's packed
@@ -281,7 +312,12 @@ template <typename S> int run(const Opts &o) {
     for (size_t a = 0; a < o.arms.size(); a++) {
         auto amps = copies ? mps->deep_copy("ARM" + to_string(a)) : mps;
         js << (a ? ", " : "");
-        solve_stage<S>(pb, amps, o.arms[a], o.sched, o, true, "ARM" + to_string(a), js);
+        // "DEVICE[:FORM][/SWEEPS]": an arm may run fewer sweeps than --sweeps
+        string arm = o.arms[a];
+        Schedule sc = o.sched;
+        if (arm.find('/') != string::npos)
+            sc.nsweeps = atoi(arm.substr(arm.find('/') + 1).c_str()), arm = arm.substr(0, arm.find('/'));
+        solve_stage<S>(pb, amps, arm, sc, o, true, "ARM" + to_string(a), js);
     }
     js << "]}\n";
     if (!o.json.empty()) {
@@ -341,6 +377,10 @@ int main(int argc, char **argv) {
         else if (k == "--warm-noises") o.warm.noises = parse_list(v);
         else if (k == "--warm-dav") o.warm.dav_thrds = parse_list(v);
         else if (k == "--warm-device") o.warm_device = v;
+        else if (k == "--dump-heff") o.dump_dir = v;
+        else if (k == "--dump-arm") o.dump_arm = atoi(v.c_str());
+        else if (k == "--dump-sweep") o.dump_sweep = atoi(v.c_str());
+        else if (k == "--dump-site") o.dump_site = atoi(v.c_str());
         else {
             cerr << "unknown option " << k << endl;
             return 2;

@@ -99,6 +99,10 @@ typedef struct {
 /* version and error reporting */
 int b2g_version(void);
 const char *b2g_last_error(void);
+/* Kernels this library has launched in this process so far (a replayed CUDA
+ * graph counts the kernels it holds).  No reference counterpart: launch
+ * accounting for measurements. */
+int b2g_launch_count(uint64_t *out);
 
 /* one context per device (the device is made current by every call) */
 int b2g_context_create(int device, b2g_context **out);
@@ -293,7 +297,10 @@ int b2g_heff_set_params(b2g_heff *h, const b2g_pair_seq *seq, const int32_t *par
 
 /* Measured compute ceiling of one arithmetic form on this device (a
  * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as
- * the roofline denominator where no measured peak exists (FP64). */
+ * the roofline denominator where no measured peak exists (FP64).
+ * form = B2G_FP64: FP64 FMA on the CUDA cores (DFMA); B2G_PROBE_FP64_MMA: the
+ * FP64 tensor-core instruction (mma.sync m8n8k4 f64, DMMA). */
+#define B2G_PROBE_FP64_MMA 16
 int b2g_probe_peak(b2g_context *ctx, int form, double *tflops);
 
 /*
