@@ -143,6 +143,7 @@ SIGNATURES = {
     "b2g_heff_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "b2g_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "b2g_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
+    "b2g_host_buffer": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "b2g_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int,
                                C.c_int, C.c_int, C.POINTER(DavidsonResultC)]),
     "b2g_davidson_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,

@@ -205,7 +205,34 @@ int b2g_context_destroy(b2g_context *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->host_buf != nullptr)
+        cudaFreeHost(ctx->host_buf);
     delete ctx;
+    return B2G_OK;
+}
+
+int b2g_host_buffer(b2g_context *ctx, uint64_t bytes, void **out) {
+    if (ctx == nullptr || out == nullptr)
+        return fail(B2G_ERR_ARG, "b2g_host_buffer: null argument");
+    *out = nullptr;
+    B2G_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (bytes > ctx->host_buf_bytes) {
+        // copies out of the old buffer may still be in flight
+        B2G_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        if (ctx->host_buf != nullptr)
+            cudaFreeHost(ctx->host_buf);
+        ctx->host_buf = nullptr, ctx->host_buf_bytes = 0;
+        // grow by a quarter beyond the request, so a slowly growing sweep does
+        // not reallocate at every site
+        const uint64_t want = bytes + bytes / 4;
+        if (cudaHostAlloc(&ctx->host_buf, want, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->host_buf = nullptr;
+            return fail(B2G_ERR_NOMEM, "cudaHostAlloc failed for the pinned staging buffer");
+        }
+        ctx->host_buf_bytes = want;
+    }
+    *out = ctx->host_buf;
     return B2G_OK;
 }
 
@@ -222,7 +249,8 @@ int b2g_context_synchronize(b2g_context *ctx) {
 int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops,
                     uint64_t ops_size, int ops_on_device, uint64_t psi_size, uint64_t sigma_size,
                     b2g_heff **out) {
-    if (ctx == nullptr || seq == nullptr || out == nullptr || (ops == nullptr && ops_size != 0))
+    const bool deferred = ops_on_device == B2G_OPS_DEFERRED;
+    if (ctx == nullptr || seq == nullptr || out == nullptr || (ops == nullptr && ops_size != 0 && !deferred))
         return fail(B2G_ERR_ARG, "b2g_heff_create: null argument");
     *out = nullptr;
     B2G_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -248,9 +276,9 @@ int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops
             h->ops = nullptr;
             return bail(fail(B2G_ERR_NOMEM, "cudaMalloc failed for the operator blob"));
         }
-        if (cudaMemcpyAsync(h->ops, ops, sizeof(double) * ops_size,
-                            ops_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                            s) != cudaSuccess)
+        if (!deferred && cudaMemcpyAsync(h->ops, ops, sizeof(double) * ops_size,
+                                         ops_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                         s) != cudaSuccess)
             return bail(fail(B2G_ERR_CUDA, "operator blob upload failed"));
     }
     h->simt_part_size = (uint64_t)4 * 256 * hp.t2_part_tiles;

@@ -540,12 +540,30 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
                cuda_ok(cudaMemcpyAsync(qq.data(), qqd, sizeof(double) * k, cudaMemcpyDeviceToHost, st), "qq") &&
                cuda_ok(cudaStreamSynchronize(st), "sync");
     };
-    auto all_below = [&](bool loose) {
-        for (int i = 0; i < k; i++) {
-            const double thr = loose ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i]) : conv_thrd;
-            if (!(qq[i] < thr))
+    // Threshold on the residual the reduced-precision products estimate, per
+    // root: before any FP64 product, the noise floor of a reduced product of
+    // an eigenvalue of size lam (1e-12 lam^2); after an FP64 certification that
+    // left exact residuals qq_exact, four orders of magnitude below the largest
+    // of them (each reduced cycle has to earn its next FP64 product), never
+    // below conv_thrd.  The FP64 form uses conv_thrd throughout.
+    double qq_exact = 0.0;
+    auto red_thr = [&](bool reduced, int i) {
+        if (!reduced)
+            return conv_thrd;
+        if (!have_exact)
+            return std::max(conv_thrd, 1e-12 * lam[i] * lam[i]);
+        return std::max(conv_thrd, 1e-4 * qq_exact);
+    };
+    auto all_below = [&](bool reduced) {
+        for (int i = 0; i < k; i++)
+            if (!(qq[i] < red_thr(reduced, i)))
                 return false;
-        }
+        return true;
+    };
+    auto all_below_exact = [&]() {
+        for (int i = 0; i < k; i++)
+            if (!(qq[i] < conv_thrd))
+                return false;
         return true;
     };
     // ---- initial basis: the k guesses, orthonormalised
@@ -569,7 +587,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
         if (!expand(form) || !ritz())
             goto done;
         const bool reduced = form != B2G_FP64;
-        if (all_below(reduced && !have_exact) || (reduced && since_refine >= 40)) {
+        if (all_below(reduced) || (reduced && since_refine >= 40)) {
             if (!reduced) {
                 converged = true;
                 break;
@@ -583,20 +601,20 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
             if (!cuda_ok(cudaMemsetAsync(A, 0, sizeof(double) * kMaxSub * kMaxSub, st), "A") ||
                 !expand(B2G_FP64) || !ritz())
                 goto done;
-            if (all_below(false)) {
+            if (all_below_exact()) {
                 converged = true;
                 break;
             }
             if (++n_refine > 30)
                 break;
             have_exact = true;
+            qq_exact = *std::max_element(qq.begin(), qq.begin() + k);
             since_refine = 0;
         }
         // ---- restart when the new corrections would not fit
         int n_unconv = 0;
         for (int i = 0; i < k; i++)
-            n_unconv += qq[i] >= (reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i])
-                                                          : conv_thrd);
+            n_unconv += qq[i] >= red_thr(reduced, i);
         if (m + n_unconv > def_max) {
             note_launch();
             rotate_basis<<<g, 256, 0, st>>>(R, B, n, m, def_min, V, kMaxSub, n);
@@ -618,8 +636,7 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
         // vector, and one read of the norms afterwards drops those
         int added = 0, mp = m;
         for (int i = 0; i < k; i++) {
-            const double thr = reduced && !have_exact ? std::max(conv_thrd, 1e-12 * lam[i] * lam[i]) : conv_thrd;
-            if (qq[i] < thr || mp >= def_max)
+            if (qq[i] < red_thr(reduced, i) || mp >= def_max)
                 continue;
             double *q = Q + (uint64_t)i * n, *x = X + (uint64_t)i * n;
             note_launch();

@@ -267,6 +267,8 @@ struct b2g_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     int n_sm = 0;
+    void *host_buf = nullptr;     // pinned staging buffer (b2g_host_buffer)
+    uint64_t host_buf_bytes = 0;
 };
 
 namespace b2g {

@@ -34,6 +34,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace b2g_block2 {
@@ -51,6 +52,7 @@ struct Runtime {
     long long n_heff = 0, n_apply_fp64 = 0, n_apply_reduced = 0;
     double t_plan = 0, t_upload = 0;
     double t_davidson = 0;      // wall time inside b2g_davidson (device-resident solves)
+    double h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic of the drop-in
     explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
         check(b2g_context_create(device, &ctx), "b2g_context_create");
     }
@@ -72,8 +74,32 @@ struct RecordedPairs {
     std::vector<int32_t> tb0, m0, n0, k0, lda0, ldb0, ta1, m1, n1, k1, lda1, ldc1;
     std::vector<double> alpha0, alpha1;
     std::vector<uint64_t> a0, b0, a1, c1;
-    std::vector<double> blob;
+    std::vector<double> blob;   // filled only by pack() (dumps); the device path uses pack_into
     double mnk = 0;   // block2's multiply-add count of one product
+    // the merged operand regions of block2's memory and their blob offsets
+    struct Span {
+        const double *p;
+        uint64_t n;
+    };
+    std::vector<Span> regions;
+    std::vector<uint64_t> region_off;
+    uint64_t blob_size = 0;
+
+    // copies every region into dst (blob_size doubles), all host threads
+    void pack_into(double *dst) const {
+#pragma omp parallel for schedule(dynamic, 16)
+        for (long r = 0; r < (long)regions.size(); r++) {
+            const double *src = regions[r].p;
+            const uint64_t n = regions[r].n;
+            double *d = dst + region_off[r];
+            // split large regions so every thread streams a share
+            std::copy(src, src + n, d);
+        }
+    }
+    void pack() {
+        blob.resize(blob_size);
+        pack_into(blob.data());
+    }
 
     b2g_pair_seq seq() const {
         b2g_pair_seq s;
@@ -105,10 +131,6 @@ struct RecordedPairs {
         tb0.resize(np), m0.resize(np), n0.resize(np), k0.resize(np), lda0.resize(np), ldb0.resize(np);
         ta1.resize(np), m1.resize(np), n1.resize(np), k1.resize(np), lda1.resize(np), ldc1.resize(np);
         alpha0.resize(np), alpha1.resize(np), a0.resize(np), b0.resize(np), a1.resize(np), c1.resize(np);
-        struct Span {
-            const double *p;
-            uint64_t n;
-        };
         std::vector<Span> spans;
         spans.reserve(2 * np);
         mnk = 0;
@@ -140,10 +162,21 @@ struct RecordedPairs {
             } else
                 merged.push_back(s);
         }
+        // large regions are cut into pieces of at most 4 Mi doubles so the
+        // parallel pack spreads them over the host threads
+        const uint64_t piece = (uint64_t)1 << 22;
         std::vector<uint64_t> off(merged.size());
         uint64_t total = 0;
-        for (size_t r = 0; r < merged.size(); r++)
-            off[r] = total, total += merged[r].n;
+        regions.clear(), region_off.clear();
+        for (size_t r = 0; r < merged.size(); r++) {
+            off[r] = total;
+            for (uint64_t q = 0; q < merged[r].n; q += piece) {
+                regions.push_back(Span{merged[r].p + q, std::min(piece, merged[r].n - q)});
+                region_off.push_back(total + q);
+            }
+            total += merged[r].n;
+        }
+        blob_size = total;
         auto locate = [&](const double *p) -> uint64_t {
             auto it = std::upper_bound(merged.begin(), merged.end(), p,
                                        [](const double *x, const Span &s) { return x < s.p; });
@@ -152,10 +185,6 @@ struct RecordedPairs {
         };
         for (size_t i = 0; i < np; i++)
             b0[i] = locate(g0.b[i]), a1[i] = locate(g1.a[i]);
-        blob.resize(total);
-#pragma omp parallel for schedule(dynamic, 64)
-        for (long r = 0; r < (long)merged.size(); r++)
-            std::copy(merged[r].p, merged[r].p + merged[r].n, blob.data() + off[r]);
     }
 };
 
@@ -196,12 +225,38 @@ struct DevicePlan {
         RecordedPairs local;
         RecordedPairs &rp = keep != nullptr ? *keep : local;
         rp.translate(sq, ket_size, bra_size);
-        rt->t_plan += t.get_time();
+        // the device plan is built on a second thread while this one packs
+        // the operator blob into the context's pinned staging buffer; the
+        // blob is uploaded when both are done
         b2g_pair_seq ps = rp.seq();
-        check(b2g_heff_create(rt->ctx, &ps, rp.blob.data(), (uint64_t)rp.blob.size(), 0, ket_size,
-                              bra_size, &h),
-              "b2g_heff_create");
+        int rc_create = B2G_OK;
+        std::string err_create;
+        std::thread builder([&] {
+            rc_create = b2g_heff_create(rt->ctx, &ps, nullptr, rp.blob_size, B2G_OPS_DEFERRED, ket_size,
+                                        bra_size, &h);
+            if (rc_create != B2G_OK)
+                err_create = b2g_last_error();
+        });
+        void *stage = nullptr;
+        const int rc_buf = b2g_host_buffer(rt->ctx, 8 * std::max<uint64_t>(rp.blob_size, 1), &stage);
+        const std::string err_buf = rc_buf != B2G_OK ? b2g_last_error() : "";
+        if (rc_buf == B2G_OK)
+            rp.pack_into((double *)stage);
+        rt->t_plan += t.get_time();
+        builder.join();
+        if (rc_create != B2G_OK) {
+            h = nullptr;
+            throw std::runtime_error("b2g_heff_create: " + err_create);
+        }
+        if (rc_buf != B2G_OK) {
+            release();
+            throw std::runtime_error("b2g_host_buffer: " + err_buf);
+        }
+        check(b2g_heff_set_ops(h, (const double *)stage, 0), "b2g_heff_set_ops");
+        if (keep != nullptr)
+            keep->blob.assign((const double *)stage, (const double *)stage + rp.blob_size);
         rt->t_upload += t.get_time();
+        rt->h2d_bytes += 8.0 * (double)rp.blob_size;
         rt->n_heff++;
         nket = ket_size, nbra = bra_size, mnk = rp.mnk, signature = s;
         return h;
@@ -235,6 +290,7 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
         b2g_heff *h = device_plan((uint64_t)b.size(), (uint64_t)c.size());
         check(b2g_heff_apply_host(h, b.data, c.data, scale, B2G_FP64), "b2g_heff_apply_host");
         rt->n_apply_fp64++;
+        rt->h2d_bytes += 8.0 * (double)b.size(), rt->d2h_bytes += 8.0 * (double)c.size();
         sq.cumulative_nflop += (size_t)plan->mnk;
     }
 };
@@ -346,6 +402,8 @@ template <typename S> struct GpuDMRG : block2::DMRG<S, double, double> {
                            this->davidson_def_min_size, this->davidson_def_max_size, rt->form, &res),
               "b2g_davidson");
         rt->t_davidson += td.get_time();
+        // diag down, diag + psi up, psi down
+        rt->d2h_bytes += 16.0 * (double)nket, rt->h2d_bytes += 16.0 * (double)nket;
         if (dw != nullptr) {
             dw->arr("psi_converged", std::vector<double>(h_eff->ket->data, h_eff->ket->data + nket), "f8");
             dw->scalar("davidson_energy", res.energy), dw->scalar("davidson_iterations", res.n_iter);

@@ -56,7 +56,8 @@ struct Opts {
     double tol = 0.0;
     string json, scratch = "";
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
-    // GPU arms: dump the H_eff of one site of one sweep of arm dump_arm
+    // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
+    // (-1: of the warm-up)
     string dump_dir;
     int dump_arm = 0, dump_sweep = -1, dump_site = -1;
 };
@@ -74,7 +75,8 @@ struct SweepPhase {
     double wall, teff, teig, tprt, tblk, tmve, tdm, tsplt, trot, tctr, tmid, tint, tdctr, tdiag, tinfo;
     // GPU arms: time inside the device Davidson solves, the pair translation
     // and the plan build + operator upload during the sweep
-    double gdav = 0, gtranslate = 0, gplan = 0;
+    double gdav = 0, gtranslate = 0, gplan = 0, h2d = 0, d2h = 0;
+    double nflop = 0;  // block2's multiply-add counter of the sweep (sweep_cumulative_nflop)
 };
 
 // Times each sweep and reads the reference's own per-phase timers when it
@@ -86,7 +88,7 @@ template <typename S> struct PhaseRecorder : CallbackKernel {
     mutable Timer t;
 #ifndef B2G_REFERENCE_ONLY
     b2g_block2::Runtime *rt = nullptr;
-    mutable double g0[3] = {0, 0, 0};
+    mutable double g0[5] = {0, 0, 0, 0, 0};
 #endif
     void compute(const string &name, int iprint) const override {
         if (d == nullptr)
@@ -94,7 +96,8 @@ template <typename S> struct PhaseRecorder : CallbackKernel {
         if (name == "DMRG::sweep.start") {
 #ifndef B2G_REFERENCE_ONLY
             if (rt != nullptr)
-                g0[0] = rt->t_davidson, g0[1] = rt->t_plan, g0[2] = rt->t_upload;
+                g0[0] = rt->t_davidson, g0[1] = rt->t_plan, g0[2] = rt->t_upload, g0[3] = rt->h2d_bytes,
+                g0[4] = rt->d2h_bytes;
 #endif
             t.get_time();
         }
@@ -105,8 +108,10 @@ template <typename S> struct PhaseRecorder : CallbackKernel {
                      d->tsplt, me.trot, me.tctr, me.tmid, me.tint, me.tdctr, me.tdiag, me.tinfo};
 #ifndef B2G_REFERENCE_ONLY
         if (rt != nullptr)
-            p.gdav = rt->t_davidson - g0[0], p.gtranslate = rt->t_plan - g0[1], p.gplan = rt->t_upload - g0[2];
+            p.gdav = rt->t_davidson - g0[0], p.gtranslate = rt->t_plan - g0[1], p.gplan = rt->t_upload - g0[2],
+            p.h2d = rt->h2d_bytes - g0[3], p.d2h = rt->d2h_bytes - g0[4];
 #endif
+        p.nflop = (double)d->sweep_cumulative_nflop;
         phases.push_back(p);
     }
 };
@@ -168,7 +173,7 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
 #ifndef B2G_REFERENCE_ONLY
     if (gpu) {
         auto gd = make_shared<b2g_block2::GpuDMRG<S>>(me, bdims, sc.noises, pb.rt);
-        if (!o.dump_dir.empty() && tag == "ARM" + to_string(o.dump_arm)) {
+        if (!o.dump_dir.empty() && tag == (o.dump_arm < 0 ? string("WARM") : "ARM" + to_string(o.dump_arm))) {
             mkdirs(o.dump_dir);
             gd->dump_dir = o.dump_dir, gd->dump_sweep = o.dump_sweep;
             gd->dump_site = o.dump_site >= 0 ? o.dump_site : pb.n / 2 - 1;
@@ -191,6 +196,11 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
 #endif
     callback_() = rec;
     cout << "== stage " << tag << ": " << device << ", " << sc.nsweeps << " sweeps" << endl;
+    uint64_t launches0 = 0;
+#ifndef B2G_REFERENCE_ONLY
+    if (gpu)
+        b2g_launch_count(&launches0);
+#endif
     Timer t;
     t.get_time();
     const double e = (double)dmrg->solve(sc.nsweeps, forward, o.tol);
@@ -220,7 +230,8 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
            << ", \"tsplt\": " << p.tsplt << ", \"trot\": " << p.trot << ", \"tctr\": " << p.tctr
            << ", \"tmid\": " << p.tmid << ", \"tint\": " << p.tint << ", \"tdctr\": " << p.tdctr
            << ", \"tdiag\": " << p.tdiag << ", \"tinfo\": " << p.tinfo << ", \"gpu_davidson\": " << p.gdav
-           << ", \"gpu_translate\": " << p.gtranslate << ", \"gpu_plan_upload\": " << p.gplan << "}";
+           << ", \"gpu_translate\": " << p.gtranslate << ", \"gpu_plan_upload\": " << p.gplan
+           << ", \"mnk\": " << p.nflop << ", \"h2d_bytes\": " << p.h2d << ", \"d2h_bytes\": " << p.d2h << "}";
     }
     js << "]";
     // block structure of the final MPS: per site tensor, each block's packed
@@ -250,7 +261,11 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
     if (gpu)
         js << ", \"gpu\": {\"heff_plans\": " << pb.rt->n_heff << ", \"apply_fp64\": " << pb.rt->n_apply_fp64
            << ", \"apply_reduced\": " << pb.rt->n_apply_reduced << ", \"t_translate\": " << pb.rt->t_plan
-           << ", \"t_plan_upload\": " << pb.rt->t_upload << "}";
+           << ", \"t_plan_upload\": " << pb.rt->t_upload << ", \"kernel_launches\": " << [&] {
+                  uint64_t n1 = 0;
+                  b2g_launch_count(&n1);
+                  return n1 - launches0;
+              }() << "}";
 #endif
     js << "}";
     pb.mpo->tf = pb.cpu_tf;

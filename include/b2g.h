@@ -109,13 +109,25 @@ int b2g_context_create(int device, b2g_context **out);
 int b2g_context_destroy(b2g_context *ctx);
 /* the CUDA stream the context launches on (cudaStream_t), for callers that sync/overlap */
 void *b2g_context_stream(b2g_context *ctx);
+/* A pinned (page-locked) host buffer of at least `bytes` owned by the context,
+ * for staging operator blobs: host->device copies from it run at the link's
+ * full rate and without driver staging.  The pointer stays valid until a
+ * later call asks for more bytes (the buffer is then replaced, after the
+ * context stream has drained) or the context is destroyed.  No reference
+ * counterpart (block2's operators live in its own pageable allocators). */
+int b2g_host_buffer(b2g_context *ctx, uint64_t bytes, void **out);
 int b2g_context_synchronize(b2g_context *ctx);
 
 /*
  * Build the device plan of one H_eff from its recorded pair sequence and
  * upload the operator blob (ops_size doubles; host memory when
- * ops_on_device == 0, else a device pointer that is copied).
+ * ops_on_device == 0, else a device pointer that is copied).  With
+ * ops_on_device == B2G_OPS_DEFERRED the blob is allocated but not filled
+ * (ops may be NULL): the caller installs the values with b2g_heff_set_ops
+ * before the first product, e.g. while this call builds the plan on another
+ * thread.
  */
+#define B2G_OPS_DEFERRED 2
 int b2g_heff_create(b2g_context *ctx, const b2g_pair_seq *seq, const double *ops,
                     uint64_t ops_size, int ops_on_device, uint64_t psi_size,
                     uint64_t sigma_size, b2g_heff **out);
