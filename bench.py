@@ -55,18 +55,19 @@ REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
 
 # name -> Hamiltonian, bond dimension and warm-up schedule (noise, Davidson threshold)
 WORKLOADS = {
+# Warm-up sweeps run without noise (block2's density-matrix noise at M = 1000
+# randomises the kept states for several sweeps); the first warm-up sweep has
+# the timed sweeps' Davidson threshold, which makes it the same sweep the
+# reference arm times (the first sweep from the seeded random MPS).
+WORKLOADS = {
     "syn24": {"desc": "synthetic ab initio n=24 N=24 S=0 SU(2), M=1000 (integral recipe, numpy default_rng(0))",
-              "n": 24, "M": 1000, "sym": "su2",
-              "warm_noises": (1e-5, 1e-5, 1e-6, 1e-6), "warm_dav": (1e-6, 1e-6, 1e-7, 1e-7)},
+              "n": 24, "M": 1000, "sym": "su2", "warm_noises": (0.0,)},
     "syn16": {"desc": "synthetic ab initio n=16 N=16 S=0 SU(2), M=500 (integral recipe, numpy default_rng(0))",
-              "n": 16, "M": 500, "sym": "su2",
-              "warm_noises": (1e-5, 1e-5, 1e-6, 1e-6), "warm_dav": (1e-6, 1e-6, 1e-7, 1e-7)},
+              "n": 16, "M": 500, "sym": "su2", "warm_noises": (0.0,)},
     "syn32": {"desc": "synthetic ab initio n=32 N=32 S=0 SU(2), M=2000 (integral recipe, numpy default_rng(0))",
-              "n": 32, "M": 2000, "sym": "su2",
-              "warm_noises": (1e-5, 1e-5, 1e-6, 1e-6), "warm_dav": (1e-6, 1e-6, 1e-7, 1e-7)},
+              "n": 32, "M": 2000, "sym": "su2", "warm_noises": (0.0,)},
     "hub16": {"desc": "1D Hubbard L=16 t=1 U=4 OBC half filling S=0 SU(2), M=250",
-              "hubbard": True, "n": 16, "M": 250, "sym": "su2",
-              "warm_noises": (1e-6, 1e-7), "warm_dav": (1e-10, 1e-10)},
+              "hubbard": True, "n": 16, "M": 250, "sym": "su2", "warm_noises": (1e-6, 1e-7)},
 }
 
 
@@ -282,6 +283,32 @@ def cpu_port_rate(prob, budget_s: float = 25.0):
     return flop / statistics.median(times), len(times), nth, blas
 
 
+def heff_only(dump_dir: str, form_name: str, products: int, dev_index: int) -> dict:
+    """A few products of one form on a dumped H_eff (nothing else runs: for
+    profiler captures of the product kernels)."""
+    import torch
+
+    import b2g
+    from b2g.problem import load_dump
+    prob = load_dump(dump_dir)
+    ctx = b2g.Context(dev_index)
+    dev = torch.device("cuda", dev_index)
+    h = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
+    form = {"fp64": b2g.FP64, "tf32x3": b2g.TF32X3, "fp32": b2g.FP32}[form_name]
+    psi = torch.from_numpy(prob.extra.get("psi_converged", prob.psi)).to(dev)
+    sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(products):
+        h.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, form)
+    h.status()
+    out = {"section": "heff_only", "form": form_name, "products": products, "n_pairs": h.stats["n_pairs"],
+           "mnk": h.stats["mnk"], "ops_bytes": h.stats["ops_bytes"], "wall_s": time.perf_counter() - t0}
+    h.close()
+    ctx.close()
+    return out
+
+
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, rank, local_rank, world, dist):
     import torch
@@ -293,7 +320,7 @@ def run_ours(args, rank, local_rank, world, dist):
     ham = hamiltonian(spec, wd)
     warm = max(2, args.warmup + args.warmup % 2)  # even: the arms start forward from site 0
     wn = tuple(spec["warm_noises"][min(i, len(spec["warm_noises"]) - 1)] for i in range(warm))
-    wdv = tuple(spec["warm_dav"][min(i, len(spec["warm_dav"]) - 1)] for i in range(warm))
+    wdv = (args.dav,) * warm
     kf = min(args.steps, args.fp64_sweeps)
     arms = [f"gpu:tf32x3/{args.steps}"] + ([f"gpu:fp64/{kf}"] if kf > 0 else [])
     if args.cpu_arm:
@@ -342,7 +369,11 @@ def run_ours(args, rank, local_rank, world, dist):
                                "gpu_plan_upload")},
         "sweeps": {"mixed": {"energies": mixed["sweep_energies"], "discarded_weights": mixed["discarded_weights"],
                              "seconds": mixed["sweep_time"], "gpu": mixed.get("gpu")},
-                   "warmup_seconds": r["warm"]["sweep_time"]},
+                   "warmup_seconds": r["warm"]["sweep_time"], "warmup_energies": r["warm"]["sweep_energies"]},
+        "first_sweep_s": r["warm"]["sweep_time"][0],
+        "first_sweep_note": ("the first warm-up sweep (mixed form, from the seeded random MPS, noise 0, the "
+                             "timed sweeps' Davidson threshold) is the sweep `--impl reference` times on the "
+                             "host cores"),
         "gpu_launches": int(mixed["gpu"]["kernel_launches"]),
         "clocks": ck, "wall_s": wall,
     }
@@ -358,6 +389,14 @@ def run_ours(args, rank, local_rank, world, dist):
         cpu = r["arms"][-1]
         res["sweeps"]["cpu"] = {"energies": cpu["sweep_energies"], "seconds": cpu["sweep_time"],
                                 "phases": cpu["phases"]}
+        res["same_state_cpu"] = {
+            "cpu_s_per_sweep": cpu["sweep_time"][0], "mixed_s_per_sweep": mixed["sweep_time"][0],
+            "cpu_over_mixed": cpu["sweep_time"][0] / mixed["sweep_time"][0],
+            "abs_dE_mixed_vs_cpu": abs(cpu["sweep_energies"][0] - mixed["sweep_energies"][0]),
+            "what": "block2's CPU path, one sweep from the same warmed MPS as the timed sweeps"}
+        if fp64 is not None:
+            res["same_state_cpu"]["abs_dE_fp64_gpu_vs_cpu"] = abs(cpu["sweep_energies"][0]
+                                                                  - fp64["sweep_energies"][0])
     # the middle-site H_eff of the last warm-up sweep, on its own
     if rank == 0 and not args.no_heff:
         hs, prob = heff_section(dump, local_rank)
@@ -378,6 +417,9 @@ def run_ours(args, rank, local_rank, world, dist):
                            f"({host_part:.1f} s, block2's own code in both)"),
                 "cpu_heff_tflops": rate / 1e12}
     import shutil
+    if args.keep_dump:
+        shutil.rmtree(args.keep_dump, ignore_errors=True)
+        shutil.copytree(dump, args.keep_dump)
     shutil.rmtree(wd, ignore_errors=True)
     return res
 
@@ -432,6 +474,13 @@ def main():
     ap.add_argument("--no-heff", action="store_true", help="skip the dumped-site H_eff measurements")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
+    ap.add_argument("--keep-dump", default=None,
+                    help="copy the dumped middle-site H_eff to this directory (for --heff-only runs)")
+    ap.add_argument("--heff-only", default=None, metavar="DUMP",
+                    help="only time H_eff*psi products of a dumped H_eff (profiler runs)")
+    ap.add_argument("--form", default="tf32x3", choices=["fp64", "tf32x3", "fp32"],
+                    help="--heff-only: the form to run")
+    ap.add_argument("--products", type=int, default=3, help="--heff-only: products to run")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -439,6 +488,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.heff_only:
+        print(json.dumps(heff_only(args.heff_only, args.form, args.products, local_rank)), flush=True)
         return
     dist = None
     if world > 1:

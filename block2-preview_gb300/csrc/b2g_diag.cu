@@ -12,8 +12,10 @@
 // x = c1 + i ldc1 + j and y = a0 + k lda0 + l, so the diagonal entry x
 // collects, over the pairs whose sigma block holds x, the term with y = x
 // (k = (x - a0) / lda0, l = (x - a0) % lda0, when that lands inside the psi
-// sub-block).  One thread owns one sigma cell of a region and loops over the
-// region's contributions in a fixed order (no atomics, reproducible).
+// sub-block).  One thread owns one sigma cell of a region and loops, in a
+// fixed order (no atomics, reproducible), over the region's contributions
+// whose psi and sigma sub-blocks overlap -- the plan builder lists those per
+// region; every other contribution of the region cannot reach the diagonal.
 #include <algorithm>
 
 #include "b2g_internal.h"
@@ -23,7 +25,8 @@ namespace b2g {
 namespace {
 
 __global__ void __launch_bounds__(256) diag_kernel(const Region *__restrict__ regions,
-                                                   const int64_t *__restrict__ region_cb,
+                                                   const int64_t *__restrict__ diag_cb,
+                                                   const int32_t *__restrict__ diag_list,
                                                    const Contrib *__restrict__ contribs,
                                                    const WorkDesc *__restrict__ works,
                                                    const double *__restrict__ ops,
@@ -40,8 +43,8 @@ __global__ void __launch_bounds__(256) diag_kernel(const Region *__restrict__ re
         return;
     double s = 0.0;
     bool covered = false;
-    for (int64_t q = region_cb[g]; q < region_cb[g + 1]; q++) {
-        const Contrib ct = contribs[q];
+    for (int64_t e = diag_cb[g]; e < diag_cb[g + 1]; e++) {
+        const Contrib ct = contribs[diag_list[e]];
         const int i = r - ct.row0, j = c - ct.col0;
         if (i < 0 || i >= ct.m1 || j < 0 || j >= ct.n1)
             continue;
@@ -74,7 +77,7 @@ cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cu
         return cudaErrorInvalidConfiguration;
     note_launch();
     diag_kernel<<<dim3((unsigned)((maxcells + 255) / 256), (unsigned)p.n_regions), 256, 0, s>>>(
-        p.regions, p.region_cb, p.contribs, p.works, ops, diag);
+        p.regions, p.diag_cb, p.diag_list, p.contribs, p.works, ops, diag);
     return cudaGetLastError();
 }
 

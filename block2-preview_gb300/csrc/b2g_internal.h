@@ -174,6 +174,11 @@ struct HostPlan {
     std::vector<Contrib> contribs;
     std::vector<Region> regions;
     std::vector<int64_t> region_cb;  // contributions of region g: [region_cb[g], region_cb[g + 1])
+    // contributions whose psi sub-block overlaps their sigma sub-block (the
+    // only ones that can reach diag(H_eff)), per region: diag_list[diag_cb[g]
+    // .. diag_cb[g + 1]), in contribution order
+    std::vector<int64_t> diag_cb;
+    std::vector<int32_t> diag_list;
     std::vector<Task1> t1;
     std::vector<Task2> t2;
     std::vector<Tile2> t2multi;
@@ -202,6 +207,8 @@ struct DevicePlan {
     Contrib *contribs = nullptr;
     Region *regions = nullptr;
     int64_t *region_cb = nullptr;
+    int64_t *diag_cb = nullptr;
+    int32_t *diag_list = nullptr;
     int64_t max_region_cells = 0;
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;

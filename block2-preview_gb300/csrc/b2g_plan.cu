@@ -307,6 +307,23 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         }
     }
     plan.region_cb.push_back((int64_t)plan.contribs.size());
+    // ---- diagonal lists: a contribution reaches diag(H_eff) only where its
+    // psi sub-block and its sigma sub-block share offsets (conservative span
+    // test; the diag kernel applies the exact index test)
+    plan.diag_cb.assign(1, 0);
+    for (size_t g = 0; g < plan.regions.size(); g++) {
+        const Region &rg = plan.regions[g];
+        for (int64_t q = plan.region_cb[g]; q < plan.region_cb[g + 1]; q++) {
+            const Contrib &ct = plan.contribs[q];
+            const WorkDesc &w = plan.works[ct.u];
+            const uint64_t x0 = rg.base + (uint64_t)ct.row0 * rg.ld + (uint64_t)ct.col0;
+            const uint64_t x1 = x0 + (uint64_t)(ct.m1 - 1) * rg.ld + (uint64_t)ct.n1;
+            const uint64_t y0 = w.a0, y1 = w.a0 + extent(false, w.m0, w.k0, w.lda0);
+            if (x0 < y1 && y0 < x1)
+                plan.diag_list.push_back((int32_t)q);
+        }
+        plan.diag_cb.push_back((int64_t)plan.diag_list.size());
+    }
     // ---- image-fed GEMM1: A images (one per distinct operator block and
     // coefficient), W image offsets, stage byte offsets, split-K chunks
     {
