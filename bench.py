@@ -53,8 +53,7 @@ METRIC = ("sweep time & H_eff·ψ TFLOP/s: mixed/batched vs FP64 on 1 GB300 at "
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
 
-# name -> Hamiltonian, bond dimension and warm-up schedule (noise, Davidson threshold)
-WORKLOADS = {
+# name -> Hamiltonian, bond dimension and warm-up noise.
 # Warm-up sweeps run without noise (block2's density-matrix noise at M = 1000
 # randomises the kept states for several sweeps); the first warm-up sweep has
 # the timed sweeps' Davidson threshold, which makes it the same sweep the
@@ -323,6 +322,12 @@ def run_ours(args, rank, local_rank, world, dist):
     wdv = (args.dav,) * warm
     kf = min(args.steps, args.fp64_sweeps)
     arms = [f"gpu:tf32x3/{args.steps}"] + ([f"gpu:fp64/{kf}"] if kf > 0 else [])
+    if args.partial_end:
+        # the FP64 comparison on one partial forward sweep (sites 0 .. E-2) of
+        # both forms from the same MPS (a full FP64 sweep is too long here)
+        kf = 1
+        arms = [f"gpu:tf32x3/{args.steps}", f"gpu:fp64/1@{args.partial_end}",
+                f"gpu:tf32x3/1@{args.partial_end}"]
     if args.cpu_arm:
         arms.append("cpu/1")
     dump = os.path.join(wd, "heff_dump")
@@ -377,7 +382,20 @@ def run_ours(args, rank, local_rank, world, dist):
         "gpu_launches": int(mixed["gpu"]["kernel_launches"]),
         "clocks": ck, "wall_s": wall,
     }
-    if fp64 is not None:
+    if fp64 is not None and args.partial_end:
+        part = r["arms"][2]
+        res["sweeps"]["fp64_partial"] = {"energies": fp64["sweep_energies"], "seconds": fp64["sweep_time"],
+                                         "gpu": fp64.get("gpu"), "end_site": args.partial_end}
+        res["sweeps"]["mixed_partial"] = {"energies": part["sweep_energies"], "seconds": part["sweep_time"],
+                                          "gpu": part.get("gpu"), "end_site": args.partial_end}
+        res["forms"] = {"what": f"one partial forward sweep (sites 0..{args.partial_end - 2}) of each form "
+                                "from the same MPS",
+                        "mixed_s": part["sweep_time"][0], "fp64_s": fp64["sweep_time"][0],
+                        "fp64_over_mixed": fp64["sweep_time"][0] / part["sweep_time"][0],
+                        "abs_dE": abs(part["sweep_energies"][0] - fp64["sweep_energies"][0]), "dE_bound": 1e-8,
+                        "fp64_davidson_s": fp64["phases"][0]["gpu_davidson"],
+                        "mixed_davidson_s": part["phases"][0]["gpu_davidson"]}
+    elif fp64 is not None:
         dE = [abs(a - b) for a, b in zip(mixed["sweep_energies"][:kf], fp64["sweep_energies"])]
         t64 = mean(fp64["sweep_time"])
         res["sweeps"]["fp64"] = {"energies": fp64["sweep_energies"], "discarded_weights": fp64["discarded_weights"],
@@ -469,6 +487,8 @@ def main():
     ap.add_argument("--fp64-sweeps", type=int, default=1, help="sweeps of the plain FP64 form for the ratio")
     ap.add_argument("--dav", type=float, default=1e-12, help="Davidson threshold of the timed sweeps")
     ap.add_argument("--threads", type=int, default=0, help="host threads of block2 (default: all)")
+    ap.add_argument("--partial-end", type=int, default=0,
+                    help="compare the forms on one partial forward sweep ending at this site")
     ap.add_argument("--cpu-arm", action="store_true",
                     help="also run one sweep of block2's CPU path from the same warmed MPS")
     ap.add_argument("--no-heff", action="store_true", help="skip the dumped-site H_eff measurements")

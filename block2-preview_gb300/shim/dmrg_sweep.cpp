@@ -16,7 +16,8 @@
 //            its own MovingEnvironment; so every arm starts from the same state
 //            with the same schedule, and arms can be compared sweep by sweep.
 // An arm is "cpu" (block2's own CPU path) or "gpu:FORM" (FORM = fp64, tf32x3,
-// fp32), optionally with "/K" to run K sweeps instead of --sweeps; a GPU arm has
+// fp32), optionally with "/K" to run K sweeps instead of --sweeps and "@E" to
+// stop a single forward sweep at site E (a partial sweep); a GPU arm has
 // b2g_block2::GpuTensorFunctions installed as mpo->tf and
 // b2g_block2::GpuDMRG as the sweep driver, so every Davidson solve runs on the
 // device.  Built with -DB2G_REFERENCE_ONLY the program has no GPU code at all
@@ -327,12 +328,19 @@ template <typename S> int run(const Opts &o) {
     for (size_t a = 0; a < o.arms.size(); a++) {
         auto amps = copies ? mps->deep_copy("ARM" + to_string(a)) : mps;
         js << (a ? ", " : "");
-        // "DEVICE[:FORM][/SWEEPS]": an arm may run fewer sweeps than --sweeps
+        // "DEVICE[:FORM][/SWEEPS][@END]": an arm may run fewer sweeps than
+        // --sweeps, and may stop its forward sweeps at site END (a partial
+        // sweep over sites 0 .. END-2, block2's sweep_end_site)
         string arm = o.arms[a];
         Schedule sc = o.sched;
+        Opts oa = o;
+        if (arm.find('@') != string::npos)
+            oa.end_site = atoi(arm.substr(arm.find('@') + 1).c_str()), arm = arm.substr(0, arm.find('@'));
         if (arm.find('/') != string::npos)
             sc.nsweeps = atoi(arm.substr(arm.find('/') + 1).c_str()), arm = arm.substr(0, arm.find('/'));
-        solve_stage<S>(pb, amps, arm, sc, o, true, "ARM" + to_string(a), js);
+        if (oa.end_site > 0 && sc.nsweeps != 1)
+            throw runtime_error("a partial-sweep arm (@END) runs one forward sweep");
+        solve_stage<S>(pb, amps, arm, sc, oa, true, "ARM" + to_string(a), js);
     }
     js << "]}\n";
     if (!o.json.empty()) {
