@@ -298,11 +298,21 @@ def heff_only(dump_dir: str, form_name: str, products: int, dev_index: int) -> d
     sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(products):
-        h.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, form)
-    h.status()
-    out = {"section": "heff_only", "form": form_name, "products": products, "n_pairs": h.stats["n_pairs"],
-           "mnk": h.stats["mnk"], "ops_bytes": h.stats["ops_bytes"], "wall_s": time.perf_counter() - t0}
+    out = {"section": "heff_only", "form": form_name, "n_pairs": h.stats["n_pairs"], "mnk": h.stats["mnk"],
+           "ops_bytes": h.stats["ops_bytes"], "psi_size": prob.psi_size}
+    if products > 0:
+        for _ in range(products):
+            h.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, form)
+        h.status()
+        out["products"] = products
+    else:
+        # one Davidson solve from the dumped initial guess (its vector kernels
+        # run on psi-sized vectors: the memory-bound part of the solve)
+        x = np.array(prob.psi, copy=True)
+        e, nd, nf, td = h.eigs(prob.diag, x, conv_thrd=1e-12, form=form)
+        out.update(davidson_energy=e, iterations=nd, fp64_products=h.last_davidson.n_apply_fp64,
+                   reduced_products=h.last_davidson.n_apply_mixed)
+    out["wall_s"] = time.perf_counter() - t0
     h.close()
     ctx.close()
     return out
@@ -500,7 +510,8 @@ def main():
                     help="only time H_eff*psi products of a dumped H_eff (profiler runs)")
     ap.add_argument("--form", default="tf32x3", choices=["fp64", "tf32x3", "fp32"],
                     help="--heff-only: the form to run")
-    ap.add_argument("--products", type=int, default=3, help="--heff-only: products to run")
+    ap.add_argument("--products", type=int, default=3,
+                    help="--heff-only: products to run (0: one Davidson solve instead)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
