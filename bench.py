@@ -329,7 +329,7 @@ def run_ours(args, rank, local_rank, world, dist):
     ham = hamiltonian(spec, wd)
     warm = max(2, args.warmup + args.warmup % 2)  # even: the arms start forward from site 0
     wn = tuple(spec["warm_noises"][min(i, len(spec["warm_noises"]) - 1)] for i in range(warm))
-    wdv = (args.dav,) * warm
+    wdv = (args.warm_dav or args.dav,) * warm
     kf = min(args.steps, args.fp64_sweeps)
     arms = [f"gpu:tf32x3/{args.steps}"] + ([f"gpu:fp64/{kf}"] if kf > 0 else [])
     if args.partial_end:
@@ -497,6 +497,8 @@ def main():
     ap.add_argument("--fp64-sweeps", type=int, default=1, help="sweeps of the plain FP64 form for the ratio")
     ap.add_argument("--dav", type=float, default=1e-12, help="Davidson threshold of the timed sweeps")
     ap.add_argument("--threads", type=int, default=0, help="host threads of block2 (default: all)")
+    ap.add_argument("--warm-dav", type=float, default=0.0,
+                    help="Davidson threshold of the warm-up sweeps (default: --dav)")
     ap.add_argument("--partial-end", type=int, default=0,
                     help="compare the forms on one partial forward sweep ending at this site")
     ap.add_argument("--cpu-arm", action="store_true",
