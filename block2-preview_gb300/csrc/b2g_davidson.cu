@@ -541,17 +541,20 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
                cuda_ok(cudaStreamSynchronize(st), "sync");
     };
     // Threshold on the residual the reduced-precision products estimate, per
-    // root: before any FP64 product, the noise floor of a reduced product of
-    // an eigenvalue of size lam (1e-12 lam^2); after an FP64 certification that
-    // left exact residuals qq_exact, four orders of magnitude below the largest
-    // of them (each reduced cycle has to earn its next FP64 product), never
-    // below conv_thrd.  The FP64 form uses conv_thrd throughout.
+    // root.  Before any FP64 product: 1e-10 lam^2, safely above the noise floor
+    // of a reduced product of an eigenvalue of size lam (a TF32x3 product is
+    // good to a few 1e-6 relative), so the reduced Davidson has settled on the
+    // lowest states before the first FP64 product collapses the basis onto its
+    // Ritz vectors.  After an FP64 certification that left exact residuals
+    // qq_exact: four orders of magnitude below the largest of them (each
+    // reduced cycle has to earn its next FP64 product).  Never below conv_thrd;
+    // the FP64 form uses conv_thrd throughout.
     double qq_exact = 0.0;
     auto red_thr = [&](bool reduced, int i) {
         if (!reduced)
             return conv_thrd;
         if (!have_exact)
-            return std::max(conv_thrd, 1e-12 * lam[i] * lam[i]);
+            return std::max(conv_thrd, 1e-10 * lam[i] * lam[i]);
         return std::max(conv_thrd, 1e-4 * qq_exact);
     };
     auto all_below = [&](bool reduced) {
@@ -587,7 +590,10 @@ static int davidson_impl(b2g_heff *h, const double *diag, double *psi, int k, do
         if (!expand(form) || !ritz())
             goto done;
         const bool reduced = form != B2G_FP64;
-        if (all_below(reduced) || (reduced && since_refine >= 40)) {
+        // reduced cycles are also cut off after a fixed number of iterations
+        // (longer before the first FP64 product, while the lowest states are
+        // still being found)
+        if (all_below(reduced) || (reduced && since_refine >= (have_exact ? 40 : 200))) {
             if (!reduced) {
                 converged = true;
                 break;

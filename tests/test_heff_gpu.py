@@ -151,3 +151,29 @@ def test_size_mismatch_raises(problems, heffs):
     h = heffs[name]
     with pytest.raises(ValueError):
         h(np.zeros(h.psi_size + 1), np.zeros(h.sigma_size))
+
+
+@pytest.mark.parametrize("name", fixture_ids())
+@pytest.mark.parametrize("seed", [1, 2])
+def test_davidson_from_random_guess_finds_lowest_state(problems, heffs, name, seed):
+    """From a random initial guess (the situation of the first sweep from a
+    random MPS) both forms converge to the lowest eigenvalue of the symmetric
+    H_eff -- the reduced-precision form must not lock onto an excited state
+    when its FP64 certifications restart the basis.  Tight threshold 1e-12."""
+    p, h = problems[name], heffs[name]
+    if p.psi_size != p.sigma_size:
+        pytest.skip("bra and ket spaces differ")
+    psi0 = np.random.default_rng(seed).standard_normal(p.psi_size)
+    out = {}
+    for form in (b2g.FP64, b2g.TF32X3):
+        x = psi0.copy()
+        e, *_ = h.eigs(p.diag, x, conv_thrd=1e-12, form=form)
+        out[form] = e
+    # the lowest eigenvalue, from a dense FP64 solve of the small H_eff
+    ref = min(out.values())
+    if p.psi_size <= 4000:
+        hm = np.stack([oracle.replay(p.seq(), p.ops, col, p.sigma_size)
+                       for col in np.eye(p.psi_size)], axis=1)
+        ref = float(np.linalg.eigvalsh(0.5 * (hm + hm.T))[0])
+    assert abs(out[b2g.FP64] - ref) <= 1e-8, (out, ref)
+    assert abs(out[b2g.TF32X3] - ref) <= 1e-8, (out, ref)
