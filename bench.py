@@ -160,7 +160,7 @@ def mean(v):
     return float(sum(v) / len(v)) if v else None
 
 
-def heff_section(dump_dir: str, dev_index: int, reps: int = 5) -> dict:
+def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = False) -> dict:
     """H_eff*psi on the real middle-site operators the drop-in dumped: each
     form timed with CUDA events on the library's stream (operator blob resident
     in HBM, far above L2), relative error against FP64, per-phase times of the
@@ -257,9 +257,64 @@ def heff_section(dump_dir: str, dev_index: int, reps: int = 5) -> dict:
     dav["abs_energy_diff"] = abs(dav["tf32x3"]["energy"] - dav["fp64"]["energy"])
     dav["speedup"] = dav["fp64"]["seconds"] / dav["tf32x3"]["seconds"]
     out["davidson"] = dav
+    if adjoint:
+        out["adjoint"] = adjoint_section(h, prob, ctx, dev, stream)
     h.close()
     ctx.close()
     return out, prob
+
+
+def adjoint_section(h, prob, ctx, dev, stream, n_dirs: int = 20) -> dict:
+    """The differentiation form on the dumped site: one adjoint of
+    f = <psi| H_eff(ops) |psi> (operator gradient, FP64) timed with CUDA events,
+    and the gradient checked against central differences of f in n_dirs
+    random directions of operator space (f is quadratic in the blob, so the
+    central difference is exact up to rounding)."""
+    import torch
+    psi = torch.from_numpy(prob.extra.get("psi_converged", prob.psi)).to(dev)
+    psi = psi / torch.linalg.norm(psi)
+    ops = torch.from_numpy(prob.ops).to(dev)
+    g = torch.zeros_like(ops)
+    torch.cuda.synchronize()
+    h.adjoint(psi, psi, g, None)
+    ctx.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for e0, e1 in ev:
+        with torch.cuda.stream(stream):
+            g.zero_()
+        e0.record(stream)
+        h.adjoint(psi, psi, g, None)
+        e1.record(stream)
+    ctx.synchronize()
+    ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
+    sig = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+
+    def f(blob):
+        torch.cuda.current_stream(dev).synchronize()  # blob was made on torch's stream
+        h.set_ops(blob)
+        with torch.cuda.stream(stream):
+            sig.zero_()
+        h.apply_ptr(psi.data_ptr(), sig.data_ptr(), 1.0, 0)
+        ctx.synchronize()
+        return float(torch.dot(psi, sig))
+
+    gen = torch.Generator(device=dev).manual_seed(7)
+    scale = float(torch.linalg.norm(ops)) / max(1.0, float(ops.numel()) ** 0.5)
+    errs = []
+    for _ in range(n_dirs):
+        d = torch.randn(ops.shape, dtype=torch.float64, device=dev, generator=gen) * scale
+        t = 1e-5
+        fd = (f(ops + t * d) - f(ops - t * d)) / (2 * t)
+        gd = float(torch.dot(g, d))
+        errs.append(abs(gd - fd) / max(abs(fd), 1e-300))
+    torch.cuda.current_stream(dev).synchronize()
+    h.set_ops(ops)
+    ctx.synchronize()
+    nflop = h.adjoint_nflop
+    return {"what": "gradient of <psi|H_eff(ops)|psi> w.r.t. the operator blob (FP64 adjoint kernel)",
+            "ms": ms, "flop": nflop, "tflops": nflop / ms / 1e9,
+            "fd_directions": n_dirs, "fd_step": 1e-5, "max_rel_err_vs_central_differences": max(errs),
+            "bound": 1e-6}
 
 
 def cpu_port_rate(prob, budget_s: float = 25.0):
@@ -427,7 +482,7 @@ def run_ours(args, rank, local_rank, world, dist):
                                                                   - fp64["sweep_energies"][0])
     # the middle-site H_eff of the last warm-up sweep, on its own
     if rank == 0 and not args.no_heff:
-        hs, prob = heff_section(dump, local_rank)
+        hs, prob = heff_section(dump, local_rank, adjoint=args.adjoint or args.workload == "syn16")
         res["heff"] = hs
         res["roofline"] = hs["roofline"]
         if world == 1 and not args.no_cpu_baseline:
@@ -504,6 +559,9 @@ def main():
     ap.add_argument("--cpu-arm", action="store_true",
                     help="also run one sweep of block2's CPU path from the same warmed MPS")
     ap.add_argument("--no-heff", action="store_true", help="skip the dumped-site H_eff measurements")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time the adjoint on the dumped site and check it against central differences "
+                         "(always on for syn16, the differentiation form's configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
     ap.add_argument("--keep-dump", default=None,
