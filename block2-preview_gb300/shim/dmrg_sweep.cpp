@@ -51,7 +51,7 @@ struct Opts {
     string sym = "su2";
     int nthreads = 4, iprint = 2;
     unsigned seed = 1234;  // block2 seeds from the clock when given 0
-    Schedule sched, warm;
+    Schedule sched, warm = Schedule{{250}, {0.0}, {1e-10}, 0};  // no warm-up unless asked
     string warm_device = "cpu";
     vector<string> arms = {"cpu"};
     double tol = 0.0;
