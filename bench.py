@@ -406,7 +406,11 @@ def run_ours(args, rank, local_rank, world, dist):
     r = run_sweep(binary=SWEEP_BIN, sym=spec["sym"], M=(spec["M"],), sweeps=args.steps, noises=(0.0,),
                   dav=(args.dav,), arms=tuple(arms), warm_sweeps=warm, warm_noises=wn, warm_dav=wdv, warm_M=wm,
                   warm_device="gpu:tf32x3", threads=args.threads or host_threads(),
-                  workdir=os.path.join(wd, "run"), dump_heff=dump, dump_arm=-1, dump_sweep=warm - 1,
+                  workdir=os.path.join(wd, "run"), dump_heff=dump,
+                  # the dumped site: the middle of the last warm-up sweep, or with
+                  # --partial-end the last full-M site of the mixed partial sweep
+                  dump_arm=2 if args.partial_end else -1, dump_sweep=0 if args.partial_end else warm - 1,
+                  dump_site=args.partial_end - 2 if args.partial_end else -1,
                   env=rank_device_env(local_rank) if world > 1 else None, **ham)
     wall = time.perf_counter() - t0
     ck = clocks.stop()
