@@ -394,7 +394,8 @@ def run_ours(args, rank, local_rank, world, dist):
         # both forms from the same MPS (a full FP64 sweep is too long here)
         kf = 1
         arms = [f"gpu:tf32x3/{args.steps}", f"gpu:fp64/1@{args.partial_end}",
-                f"gpu:tf32x3/1@{args.partial_end}"]
+                f"gpu:tf32x3/1@{args.partial_end}",
+                f"gpu:tf32x3/1@{args.partial_end}"]   # a fourth, untimed arm writes the dump
     if args.cpu_arm:
         arms.append("cpu/1")
     dump = os.path.join(wd, "heff_dump")
@@ -408,8 +409,8 @@ def run_ours(args, rank, local_rank, world, dist):
                   warm_device="gpu:tf32x3", threads=args.threads or host_threads(),
                   workdir=os.path.join(wd, "run"), dump_heff=dump,
                   # the dumped site: the middle of the last warm-up sweep, or with
-                  # --partial-end the last full-M site of the mixed partial sweep
-                  dump_arm=2 if args.partial_end else -1, dump_sweep=0 if args.partial_end else warm - 1,
+                  # --partial-end the last site of an extra mixed partial sweep
+                  dump_arm=3 if args.partial_end else -1, dump_sweep=0 if args.partial_end else warm - 1,
                   dump_site=args.partial_end - 2 if args.partial_end else -1,
                   env=rank_device_env(local_rank) if world > 1 else None, **ham)
     wall = time.perf_counter() - t0
