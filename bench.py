@@ -396,6 +396,11 @@ def run_ours(args, rank, local_rank, world, dist):
         arms = [f"gpu:tf32x3/{args.steps}", f"gpu:fp64/1@{args.partial_end}",
                 f"gpu:tf32x3/1@{args.partial_end}",
                 f"gpu:tf32x3/1@{args.partial_end}"]   # a fourth, untimed arm writes the dump
+    n_main = len(arms)
+    if args.tol_study:
+        # both forms again from the same MPS at a tighter Davidson tolerance:
+        # how far each form's sweep energies move with the tolerance alone
+        arms += [f"gpu:tf32x3/{max(kf, 1)}%{args.tol_study:g}", f"gpu:fp64/{max(kf, 1)}%{args.tol_study:g}"]
     if args.cpu_arm:
         arms.append("cpu/1")
     dump = os.path.join(wd, "heff_dump")
@@ -475,6 +480,26 @@ def run_ours(args, rank, local_rank, world, dist):
         res["forms"] = {"mixed_s_per_sweep": mean(mixed["sweep_time"][:kf]), "fp64_s_per_sweep": t64,
                         "fp64_over_mixed": t64 / mean(mixed["sweep_time"][:kf]),
                         "abs_dE_per_sweep": dE, "max_abs_dE": max(dE), "dE_bound": 1e-8}
+    if args.tol_study:
+        tm, tf = r["arms"][n_main], r["arms"][n_main + 1]
+        nk = len(tf["sweep_energies"])
+
+        def diff(a, b):
+            return [abs(x - y) for x, y in zip(a["sweep_energies"][:nk], b["sweep_energies"][:nk])]
+        res["tolerance_study"] = {
+            "dav": args.dav, "tight_dav": args.tol_study,
+            "what": ("both forms from the same MPS at the bench tolerance and at a tighter one: the "
+                     "mixed-vs-FP64 energy difference at each tolerance, and how far each form's own "
+                     "sweep energies move when only the Davidson tolerance changes"),
+            "abs_dE_mixed_vs_fp64_tight": diff(tm, tf),
+            "fp64_tolerance_shift": diff(fp64, tf) if fp64 is not None and not args.partial_end else None,
+            "mixed_tolerance_shift": diff(mixed, tm),
+            "tight_energies": {"mixed": tm["sweep_energies"], "fp64": tf["sweep_energies"]},
+            "tight_seconds": {"mixed": tm["sweep_time"], "fp64": tf["sweep_time"]},
+            "tight_gpu": {"mixed": tm.get("gpu"), "fp64": tf.get("gpu")}}
+        if fp64 is not None and not args.partial_end:
+            res["tolerance_study"]["abs_dE_mixed_vs_fp64"] = diff(mixed, fp64)
+            res["tolerance_study"]["tight_fp64_over_mixed"] = mean(tf["sweep_time"]) / mean(tm["sweep_time"])
     if args.cpu_arm:
         cpu = r["arms"][-1]
         res["sweeps"]["cpu"] = {"energies": cpu["sweep_energies"], "seconds": cpu["sweep_time"],
@@ -566,6 +591,8 @@ def main():
                     help="compare the forms on one partial forward sweep ending at this site")
     ap.add_argument("--cpu-arm", action="store_true",
                     help="also run one sweep of block2's CPU path from the same warmed MPS")
+    ap.add_argument("--tol-study", type=float, default=0.0, metavar="TOL",
+                    help="also run both forms from the same MPS with Davidson threshold TOL")
     ap.add_argument("--no-heff", action="store_true", help="skip the dumped-site H_eff measurements")
     ap.add_argument("--adjoint", action="store_true",
                     help="time the adjoint on the dumped site and check it against central differences "

@@ -427,6 +427,91 @@ template <typename S> struct GpuDMRG : block2::DMRG<S, double, double> {
         h_eff->deallocate();
         return pdi;
     }
+    // DMRG::multi_two_dot_eigs_and_perturb (src/dmrg/sweep_algorithm.hpp:2361-2495),
+    // the state-averaged (MultiMPS) step: all roots share one H_eff, which is
+    // recorded once and solved by the device block Davidson (b2g_davidson_multi:
+    // the Olsen corrections of every unconverged root go through one batched
+    // product per iteration).  Roots with several target quanta per root (a
+    // wavefunction group of more than one block structure) are not supported.
+    std::tuple<std::vector<FPLS>, int, size_t, double>
+    multi_two_dot_eigs_and_perturb(const bool forward, const int i, const double davidson_conv_thrd,
+                                   const double noise,
+                                   std::shared_ptr<block2::SparseMatrixGroup<S, double>> &pket,
+                                   std::vector<std::vector<std::pair<S, double>>> &mps_quanta) override {
+        unsupported_check();
+        if (this->cpx_me != nullptr)
+            throw std::runtime_error("GpuDMRG: a complex correction environment is not implemented on the GPU path");
+        auto mket = std::dynamic_pointer_cast<block2::MultiMPS<S, double>>(this->me->ket);
+        this->_t.get_time();
+        this->torth += this->_t.get_time();
+        std::shared_ptr<block2::EffectiveHamiltonian<S, double, block2::MultiMPS<S, double>>> h_eff =
+            this->me->multi_eff_ham(block2::FuseTypes::FuseLR, forward, false);
+        auto gtf = std::dynamic_pointer_cast<GpuTensorFunctions<S>>(h_eff->tf);
+        if (gtf == nullptr)
+            throw std::runtime_error("GpuDMRG: mpo->tf must be a GpuTensorFunctions");
+        const int nroot = (int)h_eff->ket.size();
+        for (int r = 0; r < nroot; r++)
+            if (h_eff->ket[r]->n != 1 || h_eff->bra[r]->n != 1)
+                throw std::runtime_error("GpuDMRG: state-averaged roots with several target quanta per root are "
+                                         "not implemented on the GPU path");
+        this->sweep_max_eff_ham_size = std::max(this->sweep_max_eff_ham_size, h_eff->op->get_total_memory());
+        size_t wsz = 0;
+        for (int r = 0; r < nroot; r++)
+            wsz += h_eff->ket[r]->total_memory;
+        this->sweep_max_eff_wfn_size = std::max(this->sweep_max_eff_wfn_size, wsz);
+        this->current_multi_eff_ham = h_eff;
+        block2::callback_()->compute("DMRG::sweep::iter.eff_ham", this->iprint);
+        this->current_multi_eff_ham = nullptr;
+        this->teff += this->_t.get_time();
+        block2::Timer t;
+        t.get_time();
+        const uint64_t nket = h_eff->ket[0]->total_memory, nbra = h_eff->bra[0]->total_memory;
+        // as in the reference (effective_hamiltonian.hpp:1726-1728): no more
+        // roots than the dimension; the surplus roots keep their vectors
+        const int k = (int)std::min<uint64_t>((uint64_t)nroot, nket);
+        h_eff->precompute();
+        b2g_heff *h = gtf->device_plan(nket, nbra);
+        std::vector<double> diag(nket), psi((size_t)k * nket), energies(k);
+        check(b2g_heff_diag_host(h, diag.data()), "b2g_heff_diag_host");
+        for (int r = 0; r < k; r++)
+            std::copy(h_eff->ket[r]->data, h_eff->ket[r]->data + nket, psi.data() + (size_t)r * nket);
+        block2::Timer td;
+        td.get_time();
+        b2g_davidson_result res;
+        check(b2g_davidson_multi(h, diag.data(), psi.data(), k, davidson_conv_thrd, this->davidson_max_iter,
+                                 std::max(this->davidson_def_min_size, k),
+                                 std::max(this->davidson_def_max_size, k + k / 2 + 1), rt->form,
+                                 energies.data(), &res),
+              "b2g_davidson_multi");
+        rt->t_davidson += td.get_time();
+        rt->d2h_bytes += 8.0 * (double)nket * (k + 1), rt->h2d_bytes += 8.0 * (double)nket * (k + 1);
+        for (int r = 0; r < k; r++)
+            std::copy(psi.data() + (size_t)r * nket, psi.data() + (size_t)(r + 1) * nket, h_eff->ket[r]->data);
+        rt->n_apply_fp64 += res.n_apply_fp64;
+        rt->n_apply_reduced += res.n_apply_mixed;
+        const size_t nflop = (size_t)(gtf->plan->mnk * (double)(res.n_apply_fp64 + res.n_apply_mixed));
+        h_eff->post_precompute();
+        gtf->plan->release();
+        std::tuple<std::vector<FPLS>, int, size_t, double> pdi = std::make_tuple(
+            std::vector<FPLS>(energies.begin(), energies.end()), (int)res.n_iter, nflop, t.get_time());
+        for (int r = 0; r < mket->nroots; r++) {
+            mps_quanta[r] = h_eff->ket[r]->delta_quanta();
+            const double cut = this->quanta_cutoff;
+            mps_quanta[r].erase(std::remove_if(mps_quanta[r].begin(), mps_quanta[r].end(),
+                                               [cut](const std::pair<S, double> &p) { return p.second < cut; }),
+                                mps_quanta[r].end());
+        }
+        this->teig += this->_t.get_time();
+        this->current_multi_eff_ham = h_eff;
+        block2::callback_()->compute("DMRG::sweep::iter.eff_ham.end", this->iprint);
+        this->current_multi_eff_ham = nullptr;
+        if ((this->noise_type & block2::NoiseTypes::Perturbative) && noise != 0)
+            pket = h_eff->perturbative_noise(forward, i, i + 1, block2::FuseTypes::FuseLR, mket->info,
+                                             mket->weights, this->noise_type, this->me->para_rule);
+        this->tprt += this->_t.get_time();
+        h_eff->deallocate();
+        return pdi;
+    }
 };
 
 // Installs the GPU tensor functions into an MPO (what a block2 user does

@@ -16,8 +16,9 @@
 //            its own MovingEnvironment; so every arm starts from the same state
 //            with the same schedule, and arms can be compared sweep by sweep.
 // An arm is "cpu" (block2's own CPU path) or "gpu:FORM" (FORM = fp64, tf32x3,
-// fp32), optionally with "/K" to run K sweeps instead of --sweeps and "@E" to
-// stop a single forward sweep at site E (a partial sweep); a GPU arm has
+// fp32), optionally with "/K" to run K sweeps instead of --sweeps, "@E" to
+// stop a single forward sweep at site E (a partial sweep) and "%T" to solve
+// every Davidson problem of the arm to tolerance T instead of --dav; a GPU arm has
 // b2g_block2::GpuTensorFunctions installed as mpo->tf and
 // b2g_block2::GpuDMRG as the sweep driver, so every Davidson solve runs on the
 // device.  Built with -DB2G_REFERENCE_ONLY the program has no GPU code at all
@@ -49,7 +50,7 @@ struct Opts {
     int L = 16;
     double t = 1.0, U = 4.0;
     string sym = "su2";
-    int nthreads = 4, iprint = 2;
+    int nthreads = 4, iprint = 2, nroots = 1;  // nroots > 1: state-averaged MultiMPS
     unsigned seed = 1234;  // block2 seeds from the clock when given 0
     Schedule sched, warm = Schedule{{250}, {0.0}, {1e-10}, 0};  // no warm-up unless asked
     string warm_device = "cpu";
@@ -219,6 +220,13 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
         walls.push_back(p.wall);
     js << ", \"sweep_energies\": ";
     json_list(js, es);
+    js << ", \"sweep_energies_roots\": [";
+    for (size_t q = 0; q < dmrg->energies.size(); q++) {
+        vector<double> er(dmrg->energies[q].begin(), dmrg->energies[q].end());
+        js << (q ? ", " : "");
+        json_list(js, er);
+    }
+    js << "]";
     js << ", \"discarded_weights\": ";
     json_list(js, dws);
     js << ", \"sweep_time\": ";
@@ -302,9 +310,17 @@ template <typename S> int run(const Opts &o) {
                                                OpNamesSet({OpNames::R, OpNames::RD}));
     pb.cpu_tf = pb.mpo->tf;
     const Schedule &first = o.warm.nsweeps > 0 ? o.warm : o.sched;
-    auto mps_info = make_shared<MPSInfo<S>>(pb.n, vacuum, target, pb.hamil->basis);
+    shared_ptr<MPSInfo<S>> mps_info;
+    shared_ptr<MPS<S, FL>> mps;
+    if (o.nroots > 1) {
+        // state-averaged roots of one target (block2's MultiMPS, equal weights)
+        mps_info = make_shared<MultiMPSInfo<S>>(pb.n, vacuum, vector<S>{target}, pb.hamil->basis);
+        mps = make_shared<MultiMPS<S, FL>>(pb.n, 0, 2, o.nroots);
+    } else {
+        mps_info = make_shared<MPSInfo<S>>(pb.n, vacuum, target, pb.hamil->basis);
+        mps = make_shared<MPS<S, FL>>(pb.n, 0, 2);
+    }
     mps_info->set_bond_dimension((ubond_t)first.bond_dims[0]);
-    auto mps = make_shared<MPS<S, FL>>(pb.n, 0, 2);
     mps->initialize(mps_info);
     mps->random_canonicalize();
     mps->save_mutable();
@@ -328,12 +344,20 @@ template <typename S> int run(const Opts &o) {
     for (size_t a = 0; a < o.arms.size(); a++) {
         auto amps = copies ? mps->deep_copy("ARM" + to_string(a)) : mps;
         js << (a ? ", " : "");
-        // "DEVICE[:FORM][/SWEEPS][@END]": an arm may run fewer sweeps than
-        // --sweeps, and may stop its forward sweeps at site END (a partial
-        // sweep over sites 0 .. END-2, block2's sweep_end_site)
+        // "DEVICE[:FORM][/SWEEPS][@END][%TOL]": an arm may run fewer sweeps
+        // than --sweeps, may stop its forward sweeps at site END (a partial
+        // sweep over sites 0 .. END-2, block2's sweep_end_site) and may use
+        // its own Davidson tolerance
         string arm = o.arms[a];
         Schedule sc = o.sched;
         Opts oa = o;
+        if (arm.find('%') != string::npos) {
+            const double tol = atof(arm.substr(arm.find('%') + 1).c_str());
+            if (!(tol > 0))
+                throw runtime_error("arm " + arm + ": the Davidson tolerance after % must be positive");
+            sc.dav_thrds.assign(sc.dav_thrds.size(), tol);
+            arm = arm.substr(0, arm.find('%'));
+        }
         if (arm.find('@') != string::npos)
             oa.end_site = atoi(arm.substr(arm.find('@') + 1).c_str()), arm = arm.substr(0, arm.find('@'));
         if (arm.find('/') != string::npos)
@@ -383,6 +407,7 @@ int main(int argc, char **argv) {
         else if (k == "--U") o.U = atof(v.c_str());
         else if (k == "--sym") o.sym = v;
         else if (k == "--threads") o.nthreads = atoi(v.c_str());
+        else if (k == "--nroots") o.nroots = atoi(v.c_str());
         else if (k == "--seed") o.seed = (unsigned)atol(v.c_str());
         else if (k == "--tol") o.tol = atof(v.c_str());
         else if (k == "--json") o.json = v;

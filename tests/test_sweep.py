@@ -98,3 +98,32 @@ def test_gpu_sweep_matches_reference_cpu(tmp_path):
     assert gtf["gpu"]["apply_reduced"] > 0
     # and the converged energy block2 gives for this Hamiltonian
     assert abs(g64["sweep_energies"][-1] - _golden()["arms"][0]["sweep_energies"][-1]) < 1e-9
+
+
+# State-averaged roots (block2's MultiMPS; GpuDMRG's multi_two_dot_eigs_and_perturb
+# runs the block Davidson b2g_davidson_multi): Hubbard L=8 U=4, four roots, M=100.
+HUB8_SA = dict(ham="hubbard", L=8, U=4.0, t=1.0, sym="su2", M=(100,), sweeps=2, noises=(0.0,),
+               dav=(1e-12,), warm_sweeps=4, warm_noises=(1e-6, 1e-7, 0.0, 0.0), warm_dav=(1e-10,),
+               seed=1234, nroots=4)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="block2 reference build absent")
+def test_reference_state_averaged_sweep(tmp_path):
+    r = run_sweep(binary=REF_BIN, arms=("cpu",), threads=_threads(), workdir=str(tmp_path), **HUB8_SA)
+    e = r["arms"][0]["sweep_energies_roots"][-1]
+    assert len(e) == 4 and all(e[i] <= e[i + 1] + 1e-12 for i in range(3))
+
+
+@pytest.mark.gpu
+def test_gpu_state_averaged_sweep_matches_reference_cpu(tmp_path):
+    if not (os.path.exists(REF_BIN) and os.path.exists(SWEEP_BIN)):
+        pytest.skip("sweep programs not built (no block2 headers)")
+    r = run_sweep(binary=SWEEP_BIN, arms=("cpu", "gpu:fp64", "gpu:tf32x3"), threads=_threads(),
+                  workdir=str(tmp_path), **HUB8_SA)
+    cpu, g64, gtf = r["arms"]
+    ref = np.array(cpu["sweep_energies_roots"])
+    for arm, tol in ((g64, 1e-9), (gtf, 1e-8)):
+        got = np.array(arm["sweep_energies_roots"])
+        assert got.shape == ref.shape == (2, 4)
+        assert np.abs(got - ref).max() <= tol, (got, ref)
+        assert arm["gpu"]["heff_plans"] > 0
