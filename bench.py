@@ -65,7 +65,7 @@ WORKLOADS = {
     "syn16": {"desc": "synthetic ab initio n=16 N=16 S=0 SU(2), M=500 (integral recipe, numpy default_rng(0))",
               "n": 16, "M": 500, "sym": "su2", "warm_noises": (0.0,)},
     "syn32": {"desc": "synthetic ab initio n=32 N=32 S=0 SU(2), M=2000 (integral recipe, numpy default_rng(0))",
-              "n": 32, "M": 2000, "sym": "su2", "warm_noises": (0.0,)},
+              "n": 32, "M": 2000, "sym": "su2", "warm_noises": (0.0,), "stack_gb": 48.0},
     "hub16": {"desc": "1D Hubbard L=16 t=1 U=4 OBC half filling S=0 SU(2), M=250",
               "hubbard": True, "n": 16, "M": 250, "sym": "su2", "warm_noises": (1e-6, 1e-7)},
 }
@@ -176,7 +176,10 @@ def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = F
     prob = load_dump(dump_dir)
     ctx = b2g.Context(dev_index)
     dev = torch.device("cuda", dev_index)
+    t_plan = time.perf_counter()
     h = b2g.EffectiveHamiltonian(ctx, prob.seq(), prob.ops, prob.psi_size, prob.sigma_size)
+    ctx.synchronize()
+    t_plan = time.perf_counter() - t_plan
     st = h.stats
     a = prob.pairs
     flop = 2.0 * st["mnk"]
@@ -187,7 +190,24 @@ def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = F
     torch.cuda.synchronize()
     out = {"site": int(prob.meta["site"]), "sweep": int(prob.meta["isweep"]), "n_pairs": st["n_pairs"],
            "mnk": st["mnk"], "mnk_executed": st["mnk_executed"], "ops_bytes": st["ops_bytes"],
-           "psi_size": prob.psi_size, "forms": {}}
+           "psi_size": prob.psi_size, "plan_build_and_upload_s": t_plan, "forms": {}}
+    # diag(H_eff) from the pairs (the Davidson preconditioner, once per site):
+    # CUDA events on the library's stream, median of 5, against the dumped diagonal
+    dg = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()  # dg was made on torch's stream
+    h.diag(dg)
+    ctx.synchronize()
+    evd = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for e0, e1 in evd:
+        e0.record(stream)
+        h.diag(dg)
+        e1.record(stream)
+    ctx.synchronize()
+    out["diag_ms"] = statistics.median(e0.elapsed_time(e1) for e0, e1 in evd)
+    if prob.diag is not None:
+        ref_d = torch.from_numpy(np.asarray(prob.diag)).to(dev)
+        out["diag_max_rel_err_vs_dump"] = float((dg - ref_d).abs().max() / ref_d.abs().max())
+    del dg
     sig = {}
     for name, form in (("fp64", b2g.FP64), ("tf32x3", b2g.TF32X3), ("fp32", b2g.FP32)):
         s = torch.zeros(prob.sigma_size, dtype=torch.float64, device=dev)
@@ -417,7 +437,8 @@ def run_ours(args, rank, local_rank, world, dist):
                   # --partial-end the last site of an extra mixed partial sweep
                   dump_arm=3 if args.partial_end else -1, dump_sweep=0 if args.partial_end else warm - 1,
                   dump_site=args.partial_end - 2 if args.partial_end else -1,
-                  env=rank_device_env(local_rank) if world > 1 else None, **ham)
+                  env=rank_device_env(local_rank) if world > 1 else None,
+                  stack_gb=spec.get("stack_gb", 4.0), **ham)
     wall = time.perf_counter() - t0
     ck = clocks.stop()
     mixed = r["arms"][0]
@@ -552,7 +573,8 @@ def run_reference(args):
     t0 = time.perf_counter()
     r = run_sweep(binary=REF_BIN, sym=spec["sym"], M=(spec["M"],), sweeps=1, noises=(0.0,), dav=(args.dav,),
                   arms=("cpu",), warm_sweeps=2, warm_M=(spec["M"] // 4,), warm_noises=(0.0,), warm_dav=(1e-8,),
-                  warm_device="cpu", threads=nth, workdir=os.path.join(wd, "run"), **ham)
+                  warm_device="cpu", threads=nth, workdir=os.path.join(wd, "run"),
+                  stack_gb=spec.get("stack_gb", 4.0), **ham)
     wall = time.perf_counter() - t0
     arm = r["arms"][0]
     v = mean(arm["sweep_time"])

@@ -64,12 +64,14 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
               warm_noises=None, warm_dav=None, warm_device: str = "cpu", threads: int | None = None,
               seed: int = 1234, start_site: int = 0, end_site: int = -1, workdir: str | None = None,
               timeout: float | None = None, env: dict | None = None, dump_heff: str | None = None,
-              dump_arm: int = 0, dump_sweep: int = -1, dump_site: int = -1, nroots: int = 1) -> dict:
+              dump_arm: int = 0, dump_sweep: int = -1, dump_site: int = -1, nroots: int = 1,
+              stack_gb: float = 4.0) -> dict:
     """Runs one dmrg_sweep invocation and returns its JSON report with
     ``sites`` (parse_sites of its output), ``stdout`` and ``cmd``.  With
     dump_heff, GPU arm ``dump_arm`` writes the H_eff of ``dump_site`` (default:
     the middle site) in its sweep ``dump_sweep`` to that directory
-    (b2g.problem.load_dump reads it)."""
+    (b2g.problem.load_dump reads it).  stack_gb sizes block2's DataFrame stack
+    (4 GB is enough up to M = 1000; n = 32 M = 2000 needs more)."""
     if not os.path.exists(binary):
         raise FileNotFoundError(f"{binary} is not built (build() needs block2's headers)")
     lst = lambda v: ",".join(str(x) for x in v)  # noqa: E731
@@ -82,7 +84,8 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
            "--M", lst(M), "--sweeps", str(sweeps), "--noises", lst(noises), "--dav", lst(dav),
            "--arms", ",".join(arms), "--threads", str(threads), "--seed", str(seed),
            "--iprint", "2", "--json", js, "--scratch", os.path.join(wd, "scratch"),
-           "--start-site", str(start_site), "--end-site", str(end_site), "--nroots", str(nroots)]
+           "--start-site", str(start_site), "--end-site", str(end_site), "--nroots", str(nroots),
+           "--stack-gb", str(stack_gb)]
     if dump_heff:
         cmd += ["--dump-heff", os.path.abspath(dump_heff), "--dump-arm", str(dump_arm),
                 "--dump-sweep", str(dump_sweep), "--dump-site", str(dump_site)]

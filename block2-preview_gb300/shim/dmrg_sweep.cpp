@@ -57,6 +57,7 @@ struct Opts {
     vector<string> arms = {"cpu"};
     double tol = 0.0;
     string json, scratch = "";
+    double stack_gb = 4.0;  // block2's DataFrame stack (its second frame holds 30 % of it)
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
     // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
     // (-1: of the warm-up)
@@ -286,7 +287,7 @@ template <typename S> int run(const Opts &o) {
     Random::rand_seed(o.seed);
     const string scratch = o.scratch.empty() ? string("./nodex_b2g_sweep") : o.scratch;
     mkdirs(scratch);
-    frame_<FL>() = make_shared<DataFrame<FL>>((size_t)1 << 26, (size_t)1 << 32, scratch);
+    frame_<FL>() = make_shared<DataFrame<FL>>((size_t)1 << 26, (size_t)(o.stack_gb * (double)(1ull << 30)), scratch);
     frame_<FL>()->use_main_stack = false;
     frame_<FL>()->minimal_disk_usage = true;
     threading_() = make_shared<Threading>(ThreadingTypes::OperatorBatchedGEMM | ThreadingTypes::Global,
@@ -412,6 +413,7 @@ int main(int argc, char **argv) {
         else if (k == "--tol") o.tol = atof(v.c_str());
         else if (k == "--json") o.json = v;
         else if (k == "--scratch") o.scratch = v;
+        else if (k == "--stack-gb") o.stack_gb = atof(v.c_str());
         else if (k == "--iprint") o.iprint = atoi(v.c_str());
         else if (k == "--start-site") o.start_site = atoi(v.c_str());
         else if (k == "--end-site") o.end_site = atoi(v.c_str());
