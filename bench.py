@@ -150,6 +150,21 @@ def host_threads() -> int:
     return len(os.sched_getaffinity(0))
 
 
+def host_info() -> dict:
+    """The host cores block2's CPU path can use and the BLAS it is linked to
+    (scipy's bundled LP64 OpenBLAS, as the build recipe resolves it)."""
+    import glob
+    try:
+        import scipy
+        libs = sorted(glob.glob(os.path.join(os.path.dirname(scipy.__file__), os.pardir, "scipy.libs",
+                                             "libscipy_openblas*.so")))
+        blas = os.path.basename(libs[0]) if libs else "not found"
+    except ImportError:
+        blas = "not found"
+    return {"cpu_count": os.cpu_count(), "affinity_cpus": host_threads(), "blas": blas,
+            "blas_threads": 1, "openmp_threads": host_threads()}
+
+
 def rank_device_env(local_rank: int) -> dict:
     """The sweep program uses device 0 of what it sees: give each rank its own GPU."""
     vis = os.environ.get("CUDA_VISIBLE_DEVICES")
@@ -159,6 +174,20 @@ def rank_device_env(local_rank: int) -> dict:
 
 def mean(v):
     return float(sum(v) / len(v)) if v else None
+
+
+def per_site_forms(sites: dict, mixed_tag: str, fp64_tag: str) -> dict:
+    """Site by site, the first sweep of the two forms from the same MPS (block2's
+    per-site lines): Davidson seconds of each form, the energy difference, and
+    the first site where the energies part by more than 1e-9 Ha (from there on
+    the two sweeps carry different states)."""
+    a = [x for x in sites.get(mixed_tag, []) if x["sweep"] == 0]
+    b = [x for x in sites.get(fp64_tag, []) if x["sweep"] == 0]
+    rows = [{"site": x["site"], "mixed_tdav": x["tdav"], "fp64_tdav": y["tdav"], "ndav": [x["ndav"], y["ndav"]],
+             "dE": x["energy"] - y["energy"]} for x, y in zip(a, b)]
+    first = next((r["site"] for r in rows if abs(r["dE"]) > 1e-9), None)
+    return {"rows": rows, "first_site_dE_above_1e-9": first,
+            "mixed_tdav_sum": sum(r["mixed_tdav"] for r in rows), "fp64_tdav_sum": sum(r["fp64_tdav"] for r in rows)}
 
 
 def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = False) -> dict:
@@ -435,7 +464,9 @@ def run_ours(args, rank, local_rank, world, dist):
                   workdir=os.path.join(wd, "run"), dump_heff=dump,
                   # the dumped site: the middle of the last warm-up sweep, or with
                   # --partial-end the last site of an extra mixed partial sweep
-                  dump_arm=3 if args.partial_end else -1, dump_sweep=0 if args.partial_end else warm - 1,
+                  dump_arm=3 if args.partial_end else (0 if args.dump_arm_sweep >= 0 else -1),
+                  dump_sweep=(0 if args.partial_end else
+                              args.dump_arm_sweep if args.dump_arm_sweep >= 0 else warm - 1),
                   dump_site=args.partial_end - 2 if args.partial_end else -1,
                   env=rank_device_env(local_rank) if world > 1 else None,
                   stack_gb=spec.get("stack_gb", 4.0), **ham)
@@ -500,7 +531,8 @@ def run_ours(args, rank, local_rank, world, dist):
                                  "seconds": fp64["sweep_time"], "gpu": fp64.get("gpu")}
         res["forms"] = {"mixed_s_per_sweep": mean(mixed["sweep_time"][:kf]), "fp64_s_per_sweep": t64,
                         "fp64_over_mixed": t64 / mean(mixed["sweep_time"][:kf]),
-                        "abs_dE_per_sweep": dE, "max_abs_dE": max(dE), "dE_bound": 1e-8}
+                        "abs_dE_per_sweep": dE, "max_abs_dE": max(dE), "dE_bound": 1e-8,
+                        "first_sweep_sites": per_site_forms(r["sites"], "ARM0", "ARM1")}
     if args.tol_study:
         tm, tf = r["arms"][n_main], r["arms"][n_main + 1]
         nk = len(tf["sweep_energies"])
@@ -551,7 +583,7 @@ def run_ours(args, rank, local_rank, world, dist):
                            f"threads): {rate / 1e12:.3f} TFLOP/s; scaled to a sweep as the FP64 sweep's "
                            f"Davidson FLOP ({flop_sweep:.3e}) at that rate plus the FP64 sweep's host-side time "
                            f"({host_part:.1f} s, block2's own code in both)"),
-                "cpu_heff_tflops": rate / 1e12}
+                "cpu_heff_tflops": rate / 1e12, "host": host_info()}
     import shutil
     if args.keep_dump:
         shutil.rmtree(args.keep_dump, ignore_errors=True)
@@ -590,7 +622,8 @@ def run_reference(args):
         "dtype": "f64", "data": "synthetic: seeded integrals / Hubbard chain, seeded random initial MPS",
         "config": {"workload": f"{args.workload}: full two-site sweep of block2's DMRG::solve, {spec['desc']}",
                    "davidson_conv_thrd": args.dav, "host_threads": nth},
-        "cpu_baseline": {"value": v, "unit": "s/sweep", "cores": nth, "kind": "reference", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "s/sweep", "cores": nth, "kind": "reference", "sample": sample,
+                         "host": host_info()},
         "e2e": {"value": v, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "phases": {k: p[k] for k in ("teff", "teig", "tmve", "tdm", "tsplt")},
         "energy": arm["sweep_energies"], "wall_s": wall,
@@ -621,6 +654,9 @@ def main():
                          "(always on for syn16, the differentiation form's configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
+    ap.add_argument("--dump-arm-sweep", type=int, default=-1, metavar="S",
+                    help="measure the middle-site H_eff of the mixed arm's sweep S (default: of the last "
+                         "warm-up sweep); at n=32 M=2000 sweep 1 is the first with M=2000 on both sides")
     ap.add_argument("--keep-dump", default=None,
                     help="copy the dumped middle-site H_eff to this directory (for --heff-only runs)")
     ap.add_argument("--heff-only", default=None, metavar="DUMP",
