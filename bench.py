@@ -11,7 +11,8 @@ GpuDMRG installed: every Davidson solve on the device, block2's environment,
 truncation and bookkeeping on the host).  Default workload: the synthetic ab
 initio Hamiltonian n=24, N=24, S=0, SU(2), M=1000 (seeded integral recipe).
 
-Our arm: W warm-up sweeps (mixed form, with noise) from the seeded random MPS;
+Our arm: W warm-up sweeps (mixed form; two at M/4, the rest at M) from the
+seeded random MPS;
 then, from that same MPS (MPS::deep_copy per arm), K timed sweeps in the mixed
 form (split-TF32x3 tensor-core products + FP64 defect correction) and KF
 sweeps in the plain FP64 form.  `value` is the mean wall time of a mixed
@@ -20,8 +21,9 @@ uploaded as the sweep reaches it), so the sweep has no HBM-resident variant and
 `e2e` is the same measurement; `device_resident` gives the part spent in the
 device Davidson solves with the operators already in HBM.  The mixed/FP64
 sweep-time ratio and the per-sweep |dE| between the forms are reported beside
-it.  The middle-site H_eff of the last warm-up sweep is dumped by the drop-in
-and measured on its own (H_eff*psi TFLOP/s per form on the real operators,
+it.  The middle-site H_eff of a sweep with M on both sides (the last warm-up
+sweep, or the mixed arm's second sweep when the warm-up is only the two M/4
+sweeps) is dumped by the drop-in and measured on its own (H_eff*psi TFLOP/s per form on the real operators,
 relative error against FP64, the roofline of the dominant kernel).
 
 `--impl reference` runs block2's own CPU path (oracle/_ref/dmrg_sweep_ref,
@@ -453,6 +455,8 @@ def run_ours(args, rank, local_rank, world, dist):
     if args.cpu_arm:
         arms.append("cpu/1")
     dump = os.path.join(wd, "heff_dump")
+    dump_sweep_arm = (args.dump_arm_sweep if args.dump_arm_sweep >= 0 else
+                      -1 if warm >= 4 else min(1, args.steps - 1))
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler(local_rank)
@@ -462,11 +466,13 @@ def run_ours(args, rank, local_rank, world, dist):
                   dav=(args.dav,), arms=tuple(arms), warm_sweeps=warm, warm_noises=wn, warm_dav=wdv, warm_M=wm,
                   warm_device="gpu:tf32x3", threads=args.threads or host_threads(),
                   workdir=os.path.join(wd, "run"), dump_heff=dump,
-                  # the dumped site: the middle of the last warm-up sweep, or with
-                  # --partial-end the last site of an extra mixed partial sweep
-                  dump_arm=3 if args.partial_end else (0 if args.dump_arm_sweep >= 0 else -1),
-                  dump_sweep=(0 if args.partial_end else
-                              args.dump_arm_sweep if args.dump_arm_sweep >= 0 else warm - 1),
+                  # the dumped site: with --partial-end the last site of an extra
+                  # mixed partial sweep; else the middle site of a sweep with M on
+                  # both sides: the last warm-up sweep when the warm-up reaches M
+                  # twice (warm >= 4), else the mixed arm's second sweep (its first
+                  # grows the bonds from M/4)
+                  dump_arm=3 if args.partial_end else (-1 if dump_sweep_arm < 0 else 0),
+                  dump_sweep=0 if args.partial_end else (warm - 1 if dump_sweep_arm < 0 else dump_sweep_arm),
                   dump_site=args.partial_end - 2 if args.partial_end else -1,
                   env=rank_device_env(local_rank) if world > 1 else None,
                   stack_gb=spec.get("stack_gb", 4.0), **ham)
@@ -565,7 +571,7 @@ def run_ours(args, rank, local_rank, world, dist):
         if fp64 is not None:
             res["same_state_cpu"]["abs_dE_fp64_gpu_vs_cpu"] = abs(cpu["sweep_energies"][0]
                                                                   - fp64["sweep_energies"][0])
-    # the middle-site H_eff of the last warm-up sweep, on its own
+    # the dumped middle-site H_eff (M on both sides), on its own
     if rank == 0 and not args.no_heff:
         hs, prob = heff_section(dump, local_rank, adjoint=args.adjoint or args.workload == "syn16")
         res["heff"] = hs

@@ -55,7 +55,7 @@ static void free_plan(DevicePlan &p) {
     cudaFree(p.t2multi), cudaFree(p.g0tile), cudaFree(p.g0col);
     cudaFree(p.g1tile), cudaFree(p.g1stage), cudaFree(p.g1task), cudaFree(p.g1aimg);
     cudaFree(p.g1red), cudaFree(p.g1cover), cudaFree(p.region_cb);
-    cudaFree(p.diag_cb), cudaFree(p.diag_list);
+    cudaFree(p.diag_task), cudaFree(p.diag_tlist);
     p = DevicePlan();
 }
 
@@ -146,15 +146,13 @@ static int install_plan(b2g_heff *h, const HostPlan &hp) {
         (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
         (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
         (rc = upload(hp.g0psi, &p.g0psi, s)) || (rc = upload(hp.region_cb, &p.region_cb, s)) ||
-        (rc = upload(hp.diag_cb, &p.diag_cb, s)) || (rc = upload(hp.diag_list, &p.diag_list, s)))
+        (rc = upload(hp.diag_task, &p.diag_task, s)) || (rc = upload(hp.diag_tlist, &p.diag_tlist, s)))
         return rc;
     p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
     p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();
     p.n_g0psi = (int64_t)hp.g0psi.size(), p.g0_psi_floats = hp.g0_psi_floats;
     p.n_g0wide = hp.g0_wide;
-    p.max_region_cells = 0;
-    for (const Region &r : hp.regions)
-        p.max_region_cells = std::max<int64_t>(p.max_region_cells, (int64_t)r.rows * r.cols);
+    p.n_diag_task = (int64_t)hp.diag_task.size();
     p.g1_abytes = hp.g1_abytes, p.g1_wbytes = hp.g1_wbytes, p.g1_part = hp.g1_part;
     p.n_t2multi = (int64_t)hp.t2multi.size();
     p.n_works = (int64_t)hp.works.size(), p.n_contribs = (int64_t)hp.contribs.size();

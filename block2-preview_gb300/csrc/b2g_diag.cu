@@ -12,10 +12,12 @@
 // x = c1 + i ldc1 + j and y = a0 + k lda0 + l, so the diagonal entry x
 // collects, over the pairs whose sigma block holds x, the term with y = x
 // (k = (x - a0) / lda0, l = (x - a0) % lda0, when that lands inside the psi
-// sub-block).  One thread owns one sigma cell of a region and loops, in a
-// fixed order (no atomics, reproducible), over the region's contributions
-// whose psi and sigma sub-blocks overlap -- the plan builder lists those per
-// region; every other contribution of the region cannot reach the diagonal.
+// sub-block).  The plan builder cuts each sigma region into row bands of about
+// kDiagBandCells cells and lists, per band, the contributions whose psi and
+// sigma sub-blocks overlap on rows of that band -- every other contribution
+// cannot reach a diagonal cell there.  One CTA per band; one thread owns a
+// cell and loops over the band's list in contribution order (no atomics,
+// reproducible; bands are disjoint, so every cell has one owner).
 #include <algorithm>
 
 #include "b2g_internal.h"
@@ -24,60 +26,55 @@ namespace b2g {
 
 namespace {
 
-__global__ void __launch_bounds__(256) diag_kernel(const Region *__restrict__ regions,
-                                                   const int64_t *__restrict__ diag_cb,
-                                                   const int32_t *__restrict__ diag_list,
+__global__ void __launch_bounds__(256) diag_kernel(const DiagTask *__restrict__ tasks,
+                                                   const int32_t *__restrict__ tlist,
+                                                   const Region *__restrict__ regions,
                                                    const Contrib *__restrict__ contribs,
                                                    const WorkDesc *__restrict__ works,
                                                    const double *__restrict__ ops,
                                                    double *__restrict__ diag) {
-    const int g = blockIdx.y;
-    const Region rg = regions[g];
-    const int64_t ncell = (int64_t)rg.rows * rg.cols;
-    const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= ncell)
-        return;
-    const int r = (int)(cell / rg.cols), c = (int)(cell % rg.cols);
-    const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
-    if (x < rg.lo || x >= rg.hi)
-        return;
-    double s = 0.0;
-    bool covered = false;
-    for (int64_t e = diag_cb[g]; e < diag_cb[g + 1]; e++) {
-        const Contrib ct = contribs[diag_list[e]];
-        const int i = r - ct.row0, j = c - ct.col0;
-        if (i < 0 || i >= ct.m1 || j < 0 || j >= ct.n1)
+    const DiagTask t = tasks[blockIdx.x];
+    const Region rg = regions[t.g];
+    const int64_t ncell = (int64_t)(t.r1 - t.r0) * rg.cols;
+    for (int64_t cell = threadIdx.x; cell < ncell; cell += blockDim.x) {
+        const int r = t.r0 + (int)(cell / rg.cols), c = (int)(cell % rg.cols);
+        const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
+        if (x < rg.lo || x >= rg.hi)
             continue;
-        covered = true;
-        const WorkDesc w = works[ct.u];
-        if (x < w.a0)
-            continue;
-        const uint64_t dy = x - w.a0;
-        const uint64_t k = dy / (uint64_t)w.lda0, l = dy % (uint64_t)w.lda0;
-        if (k >= (uint64_t)w.m0 || l >= (uint64_t)w.k0)
-            continue;
-        const double lv = ops[ct.a1 + (ct.ta1 ? k * ct.lda1 + i : (uint64_t)i * ct.lda1 + k)];
-        const double rv = ops[w.b0 + (w.tb0 ? (uint64_t)j * w.ldb0 + l : l * w.ldb0 + j)];
-        s = fma(ct.alpha * lv, rv, s);
+        double s = 0.0;
+        bool covered = false;
+        for (int64_t e = t.lb; e < t.le; e++) {
+            const Contrib ct = contribs[tlist[e]];
+            const int i = r - ct.row0, j = c - ct.col0;
+            if (i < 0 || i >= ct.m1 || j < 0 || j >= ct.n1)
+                continue;
+            covered = true;
+            const WorkDesc w = works[ct.u];
+            if (x < w.a0)
+                continue;
+            const uint64_t dy = x - w.a0;
+            const uint64_t k = dy / (uint64_t)w.lda0, l = dy % (uint64_t)w.lda0;
+            if (k >= (uint64_t)w.m0 || l >= (uint64_t)w.k0)
+                continue;
+            const double lv = ops[ct.a1 + (ct.ta1 ? k * ct.lda1 + i : (uint64_t)i * ct.lda1 + k)];
+            const double rv = ops[w.b0 + (w.tb0 ? (uint64_t)j * w.ldb0 + l : l * w.ldb0 + j)];
+            s = fma(ct.alpha * lv, rv, s);
+        }
+        if (covered)
+            diag[x] += s;
     }
-    if (covered)
-        diag[x] += s;
 }
 
 } // namespace
 
 cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cudaStream_t s) {
-    if (p.n_regions == 0)
+    if (p.n_diag_task == 0)
         return cudaSuccess;
-    // grid.x covers the largest region; smaller regions leave threads idle
-    const int64_t maxcells = p.max_region_cells;
-    if (maxcells == 0)
-        return cudaSuccess;
-    if (p.n_regions > 65535)
+    if (p.n_diag_task > 0x7fffffff)
         return cudaErrorInvalidConfiguration;
     note_launch();
-    diag_kernel<<<dim3((unsigned)((maxcells + 255) / 256), (unsigned)p.n_regions), 256, 0, s>>>(
-        p.regions, p.diag_cb, p.diag_list, p.contribs, p.works, ops, diag);
+    diag_kernel<<<(unsigned)p.n_diag_task, 256, 0, s>>>(p.diag_task, p.diag_tlist, p.regions, p.contribs,
+                                                         p.works, ops, diag);
     return cudaGetLastError();
 }
 

@@ -66,6 +66,14 @@ struct Task2 {
     int64_t lb, le;     // contribution list range of this chunk
     int64_t part;       // partial-tile slot (in 4 x 256 tiles) of chunk 0, -1: single chunk
 };
+// diag(H_eff): one row band [r0, r1) of region g and the diagonal
+// contributions whose overlap rows meet it, diag_tlist[lb .. le), in
+// contribution order (bands are disjoint: one owner per diagonal cell)
+struct DiagTask {
+    int32_t g, r0, r1, pad;
+    int64_t lb, le;
+};
+constexpr int kDiagBandCells = 2048;   // cells per band (rows = max(1, this / region cols))
 struct Tile2 {          // a phase-2 tile split over several chunks (reduced after)
     int32_t g, rb, col0, n_chunks;
     int64_t part;
@@ -175,10 +183,9 @@ struct HostPlan {
     std::vector<Region> regions;
     std::vector<int64_t> region_cb;  // contributions of region g: [region_cb[g], region_cb[g + 1])
     // contributions whose psi sub-block overlaps their sigma sub-block (the
-    // only ones that can reach diag(H_eff)), per region: diag_list[diag_cb[g]
-    // .. diag_cb[g + 1]), in contribution order
-    std::vector<int64_t> diag_cb;
-    std::vector<int32_t> diag_list;
+    // only ones that can reach diag(H_eff)), listed per row band of each region
+    std::vector<DiagTask> diag_task;
+    std::vector<int32_t> diag_tlist;
     std::vector<Task1> t1;
     std::vector<Task2> t2;
     std::vector<Tile2> t2multi;
@@ -207,9 +214,9 @@ struct DevicePlan {
     Contrib *contribs = nullptr;
     Region *regions = nullptr;
     int64_t *region_cb = nullptr;
-    int64_t *diag_cb = nullptr;
-    int32_t *diag_list = nullptr;
-    int64_t max_region_cells = 0;
+    DiagTask *diag_task = nullptr;
+    int32_t *diag_tlist = nullptr;
+    int64_t n_diag_task = 0;
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;
     Tile2 *t2multi = nullptr;

@@ -307,22 +307,48 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         }
     }
     plan.region_cb.push_back((int64_t)plan.contribs.size());
-    // ---- diagonal lists: a contribution reaches diag(H_eff) only where its
-    // psi sub-block and its sigma sub-block share offsets (conservative span
-    // test; the diag kernel applies the exact index test)
-    plan.diag_cb.assign(1, 0);
-    for (size_t g = 0; g < plan.regions.size(); g++) {
-        const Region &rg = plan.regions[g];
-        for (int64_t q = plan.region_cb[g]; q < plan.region_cb[g + 1]; q++) {
-            const Contrib &ct = plan.contribs[q];
-            const WorkDesc &w = plan.works[ct.u];
-            const uint64_t x0 = rg.base + (uint64_t)ct.row0 * rg.ld + (uint64_t)ct.col0;
-            const uint64_t x1 = x0 + (uint64_t)(ct.m1 - 1) * rg.ld + (uint64_t)ct.n1;
-            const uint64_t y0 = w.a0, y1 = w.a0 + extent(false, w.m0, w.k0, w.lda0);
-            if (x0 < y1 && y0 < x1)
-                plan.diag_list.push_back((int32_t)q);
+    // ---- diagonal tasks: a contribution reaches diag(H_eff) only where its
+    // psi sub-block and its sigma sub-block share offsets, i.e. inside the rows
+    // of the region frame that the flat overlap [max(x0, y0), min(x1, y1)) spans
+    // (a conservative row range; the diag kernel applies the exact index test).
+    // Each region is cut into row bands of about kDiagBandCells cells; a band
+    // lists the contributions whose overlap rows meet it, in contribution order.
+    {
+        std::vector<std::vector<int32_t>> band;
+        for (size_t g = 0; g < plan.regions.size(); g++) {
+            const Region &rg = plan.regions[g];
+            if (rg.rows <= 0 || rg.cols <= 0)
+                continue;
+            const int32_t bh = std::max<int32_t>(1, kDiagBandCells / rg.cols);
+            const int32_t nb = (rg.rows + bh - 1) / bh;
+            band.assign((size_t)nb, std::vector<int32_t>());
+            for (int64_t q = plan.region_cb[g]; q < plan.region_cb[g + 1]; q++) {
+                const Contrib &ct = plan.contribs[q];
+                const WorkDesc &w = plan.works[ct.u];
+                const uint64_t x0 = rg.base + (uint64_t)ct.row0 * rg.ld + (uint64_t)ct.col0;
+                const uint64_t x1 = x0 + (uint64_t)(ct.m1 - 1) * rg.ld + (uint64_t)ct.n1;
+                const uint64_t y0 = w.a0, y1 = w.a0 + extent(false, w.m0, w.k0, w.lda0);
+                if (!(x0 < y1 && y0 < x1))
+                    continue;
+                const uint64_t lo = std::max(x0, y0), hi = std::min(x1, y1);
+                int64_t r_lo = (int64_t)((lo - rg.base) / (uint64_t)rg.ld);
+                int64_t r_hi = (int64_t)((hi - 1 - rg.base) / (uint64_t)rg.ld) + 1;
+                r_lo = std::max<int64_t>(r_lo, ct.row0);
+                r_hi = std::min<int64_t>(r_hi, (int64_t)ct.row0 + ct.m1);
+                for (int64_t b = r_lo / bh; b < nb && b * bh < r_hi; b++)
+                    band[(size_t)b].push_back((int32_t)q);
+            }
+            for (int32_t b = 0; b < nb; b++) {
+                if (band[(size_t)b].empty())
+                    continue;
+                DiagTask t;
+                t.g = (int32_t)g, t.r0 = b * bh, t.r1 = std::min(rg.rows, (b + 1) * bh), t.pad = 0;
+                t.lb = (int64_t)plan.diag_tlist.size();
+                plan.diag_tlist.insert(plan.diag_tlist.end(), band[(size_t)b].begin(), band[(size_t)b].end());
+                t.le = (int64_t)plan.diag_tlist.size();
+                plan.diag_task.push_back(t);
+            }
         }
-        plan.diag_cb.push_back((int64_t)plan.diag_list.size());
     }
     // ---- image-fed GEMM1: A images (one per distinct operator block and
     // coefficient), W image offsets, stage byte offsets, split-K chunks
