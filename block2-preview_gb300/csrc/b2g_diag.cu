@@ -12,12 +12,14 @@
 // x = c1 + i ldc1 + j and y = a0 + k lda0 + l, so the diagonal entry x
 // collects, over the pairs whose sigma block holds x, the term with y = x
 // (k = (x - a0) / lda0, l = (x - a0) % lda0, when that lands inside the psi
-// sub-block).  The plan builder cuts each sigma region into row bands of about
-// kDiagBandCells cells and lists, per band, the contributions whose psi and
-// sigma sub-blocks overlap on rows of that band -- every other contribution
-// cannot reach a diagonal cell there.  One CTA per band; one thread owns a
-// cell and loops over the band's list in contribution order (no atomics,
-// reproducible; bands are disjoint, so every cell has one owner).
+// sub-block).  The plan builder cuts each sigma region into tiles of
+// kDiagTileRows x kDiagTileCols cells and lists, per tile, the contributions
+// whose sigma rectangle meets the tile on rows where their psi and sigma
+// sub-blocks overlap -- no other contribution can reach a diagonal cell there.
+// One CTA per tile, one thread per tile column; a thread owns the column's
+// cells and loops over the tile's list in contribution order for each of
+// them (no atomics, reproducible; tiles are disjoint, so every cell has one
+// owner).  The list is staged through shared memory in chunks.
 #include <algorithm>
 
 #include "b2g_internal.h"
@@ -26,42 +28,73 @@ namespace b2g {
 
 namespace {
 
-__global__ void __launch_bounds__(256) diag_kernel(const DiagTask *__restrict__ tasks,
-                                                   const int32_t *__restrict__ tlist,
-                                                   const Region *__restrict__ regions,
-                                                   const Contrib *__restrict__ contribs,
-                                                   const WorkDesc *__restrict__ works,
-                                                   const double *__restrict__ ops,
-                                                   double *__restrict__ diag) {
+constexpr int kDiagChunk = 128;   // contributions staged in shared memory at a time
+
+__global__ void __launch_bounds__(kDiagTileCols) diag_kernel(const DiagTask *__restrict__ tasks,
+                                                             const int32_t *__restrict__ tlist,
+                                                             const Region *__restrict__ regions,
+                                                             const Contrib *__restrict__ contribs,
+                                                             const WorkDesc *__restrict__ works,
+                                                             const double *__restrict__ ops,
+                                                             double *__restrict__ diag) {
+    __shared__ Contrib sc[kDiagChunk];
+    __shared__ WorkDesc sw[kDiagChunk];
     const DiagTask t = tasks[blockIdx.x];
     const Region rg = regions[t.g];
-    const int64_t ncell = (int64_t)(t.r1 - t.r0) * rg.cols;
-    for (int64_t cell = threadIdx.x; cell < ncell; cell += blockDim.x) {
-        const int r = t.r0 + (int)(cell / rg.cols), c = (int)(cell % rg.cols);
+    const int c = t.c0 + (int)threadIdx.x;
+    const bool col_ok = c < t.c1;
+    double s[kDiagTileRows];
+    bool covered[kDiagTileRows];
+#pragma unroll
+    for (int q = 0; q < kDiagTileRows; q++)
+        s[q] = 0.0, covered[q] = false;
+    for (int64_t e0 = t.lb; e0 < t.le; e0 += kDiagChunk) {
+        const int n = (int)min((int64_t)kDiagChunk, t.le - e0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            sc[i] = contribs[tlist[e0 + i]];
+            sw[i] = works[sc[i].u];
+        }
+        __syncthreads();
+        if (!col_ok)
+            continue;
+        for (int e = 0; e < n; e++) {
+            const Contrib &ct = sc[e];
+            const int j = c - ct.col0;
+            if (j < 0 || j >= ct.n1)
+                continue;
+            const WorkDesc &w = sw[e];
+#pragma unroll
+            for (int q = 0; q < kDiagTileRows; q++) {
+                const int r = t.r0 + q;
+                const int i = r - ct.row0;
+                if (r >= t.r1 || i < 0 || i >= ct.m1)
+                    continue;
+                covered[q] = true;
+                const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
+                if (x < w.a0)
+                    continue;
+                const uint64_t dy = x - w.a0;
+                const uint64_t k = dy / (uint64_t)w.lda0, l = dy % (uint64_t)w.lda0;
+                if (k >= (uint64_t)w.m0 || l >= (uint64_t)w.k0)
+                    continue;
+                const double lv = ops[ct.a1 + (ct.ta1 ? k * ct.lda1 + i : (uint64_t)i * ct.lda1 + k)];
+                const double rv = ops[w.b0 + (w.tb0 ? (uint64_t)j * w.ldb0 + l : l * w.ldb0 + j)];
+                s[q] = fma(ct.alpha * lv, rv, s[q]);
+            }
+        }
+    }
+    if (!col_ok)
+        return;
+#pragma unroll
+    for (int q = 0; q < kDiagTileRows; q++) {
+        const int r = t.r0 + q;
+        if (r >= t.r1 || !covered[q])
+            continue;
         const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
         if (x < rg.lo || x >= rg.hi)
             continue;
-        double s = 0.0;
-        bool covered = false;
-        for (int64_t e = t.lb; e < t.le; e++) {
-            const Contrib ct = contribs[tlist[e]];
-            const int i = r - ct.row0, j = c - ct.col0;
-            if (i < 0 || i >= ct.m1 || j < 0 || j >= ct.n1)
-                continue;
-            covered = true;
-            const WorkDesc w = works[ct.u];
-            if (x < w.a0)
-                continue;
-            const uint64_t dy = x - w.a0;
-            const uint64_t k = dy / (uint64_t)w.lda0, l = dy % (uint64_t)w.lda0;
-            if (k >= (uint64_t)w.m0 || l >= (uint64_t)w.k0)
-                continue;
-            const double lv = ops[ct.a1 + (ct.ta1 ? k * ct.lda1 + i : (uint64_t)i * ct.lda1 + k)];
-            const double rv = ops[w.b0 + (w.tb0 ? (uint64_t)j * w.ldb0 + l : l * w.ldb0 + j)];
-            s = fma(ct.alpha * lv, rv, s);
-        }
-        if (covered)
-            diag[x] += s;
+        diag[x] += s[q];
     }
 }
 
@@ -73,8 +106,8 @@ cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cu
     if (p.n_diag_task > 0x7fffffff)
         return cudaErrorInvalidConfiguration;
     note_launch();
-    diag_kernel<<<(unsigned)p.n_diag_task, 256, 0, s>>>(p.diag_task, p.diag_tlist, p.regions, p.contribs,
-                                                         p.works, ops, diag);
+    diag_kernel<<<(unsigned)p.n_diag_task, kDiagTileCols, 0, s>>>(p.diag_task, p.diag_tlist, p.regions,
+                                                                   p.contribs, p.works, ops, diag);
     return cudaGetLastError();
 }
 

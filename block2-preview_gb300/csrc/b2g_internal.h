@@ -66,14 +66,15 @@ struct Task2 {
     int64_t lb, le;     // contribution list range of this chunk
     int64_t part;       // partial-tile slot (in 4 x 256 tiles) of chunk 0, -1: single chunk
 };
-// diag(H_eff): one row band [r0, r1) of region g and the diagonal
-// contributions whose overlap rows meet it, diag_tlist[lb .. le), in
-// contribution order (bands are disjoint: one owner per diagonal cell)
+// diag(H_eff): one tile (rows [r0, r1) x columns [c0, c1)) of region g and
+// the diagonal contributions that can reach a cell of it, diag_tlist[lb ..
+// le), in contribution order (tiles are disjoint: one owner per diagonal cell)
 struct DiagTask {
-    int32_t g, r0, r1, pad;
+    int32_t g, r0, r1, c0, c1, pad;
     int64_t lb, le;
 };
-constexpr int kDiagBandCells = 2048;   // cells per band (rows = max(1, this / region cols))
+constexpr int kDiagTileCols = 256;     // columns per tile (one per thread)
+constexpr int kDiagTileRows = 8;       // rows per tile
 struct Tile2 {          // a phase-2 tile split over several chunks (reduced after)
     int32_t g, rb, col0, n_chunks;
     int64_t part;

@@ -308,20 +308,21 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
     }
     plan.region_cb.push_back((int64_t)plan.contribs.size());
     // ---- diagonal tasks: a contribution reaches diag(H_eff) only where its
-    // psi sub-block and its sigma sub-block share offsets, i.e. inside the rows
-    // of the region frame that the flat overlap [max(x0, y0), min(x1, y1)) spans
-    // (a conservative row range; the diag kernel applies the exact index test).
-    // Each region is cut into row bands of about kDiagBandCells cells; a band
-    // lists the contributions whose overlap rows meet it, in contribution order.
+    // psi sub-block and its sigma sub-block share offsets, i.e. inside its
+    // sigma rectangle and on the rows of the region frame that the flat
+    // overlap [max(x0, y0), min(x1, y1)) spans (a conservative cell set; the
+    // diag kernel applies the exact index test).  Each region is cut into
+    // tiles of kDiagTileRows x kDiagTileCols cells; a tile lists the
+    // contributions whose cell set meets it, in contribution order.
     {
-        std::vector<std::vector<int32_t>> band;
+        std::vector<std::vector<int32_t>> tile;
         for (size_t g = 0; g < plan.regions.size(); g++) {
             const Region &rg = plan.regions[g];
             if (rg.rows <= 0 || rg.cols <= 0)
                 continue;
-            const int32_t bh = std::max<int32_t>(1, kDiagBandCells / rg.cols);
-            const int32_t nb = (rg.rows + bh - 1) / bh;
-            band.assign((size_t)nb, std::vector<int32_t>());
+            const int32_t nrb = (rg.rows + kDiagTileRows - 1) / kDiagTileRows;
+            const int32_t ncb = (rg.cols + kDiagTileCols - 1) / kDiagTileCols;
+            tile.assign((size_t)nrb * ncb, std::vector<int32_t>());
             for (int64_t q = plan.region_cb[g]; q < plan.region_cb[g + 1]; q++) {
                 const Contrib &ct = plan.contribs[q];
                 const WorkDesc &w = plan.works[ct.u];
@@ -335,19 +336,25 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 int64_t r_hi = (int64_t)((hi - 1 - rg.base) / (uint64_t)rg.ld) + 1;
                 r_lo = std::max<int64_t>(r_lo, ct.row0);
                 r_hi = std::min<int64_t>(r_hi, (int64_t)ct.row0 + ct.m1);
-                for (int64_t b = r_lo / bh; b < nb && b * bh < r_hi; b++)
-                    band[(size_t)b].push_back((int32_t)q);
+                const int64_t cb0 = ct.col0 / kDiagTileCols, cb1 = (ct.col0 + ct.n1 - 1) / kDiagTileCols;
+                for (int64_t rb = r_lo / kDiagTileRows; rb < nrb && rb * kDiagTileRows < r_hi; rb++)
+                    for (int64_t cb = cb0; cb <= cb1 && cb < ncb; cb++)
+                        tile[(size_t)(rb * ncb + cb)].push_back((int32_t)q);
             }
-            for (int32_t b = 0; b < nb; b++) {
-                if (band[(size_t)b].empty())
-                    continue;
-                DiagTask t;
-                t.g = (int32_t)g, t.r0 = b * bh, t.r1 = std::min(rg.rows, (b + 1) * bh), t.pad = 0;
-                t.lb = (int64_t)plan.diag_tlist.size();
-                plan.diag_tlist.insert(plan.diag_tlist.end(), band[(size_t)b].begin(), band[(size_t)b].end());
-                t.le = (int64_t)plan.diag_tlist.size();
-                plan.diag_task.push_back(t);
-            }
+            for (int32_t rb = 0; rb < nrb; rb++)
+                for (int32_t cb = 0; cb < ncb; cb++) {
+                    const auto &l = tile[(size_t)rb * ncb + cb];
+                    if (l.empty())
+                        continue;
+                    DiagTask t;
+                    t.g = (int32_t)g, t.pad = 0;
+                    t.r0 = rb * kDiagTileRows, t.r1 = std::min(rg.rows, (rb + 1) * kDiagTileRows);
+                    t.c0 = cb * kDiagTileCols, t.c1 = std::min(rg.cols, (cb + 1) * kDiagTileCols);
+                    t.lb = (int64_t)plan.diag_tlist.size();
+                    plan.diag_tlist.insert(plan.diag_tlist.end(), l.begin(), l.end());
+                    t.le = (int64_t)plan.diag_tlist.size();
+                    plan.diag_task.push_back(t);
+                }
         }
     }
     // ---- image-fed GEMM1: A images (one per distinct operator block and
