@@ -53,6 +53,11 @@ import numpy as np  # noqa: E402
 METRIC = ("sweep time & H_eff·ψ TFLOP/s: mixed/batched vs FP64 on 1 GB300 at "
           "|ΔE|≤1e-8 Ha")
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# DRAM bytes (read + write, ncu) per algorithmic FLOP of the two TF32x3 product
+# phases, captured on the n=24 M=1000 steady middle site: GEMM0 (g0_pack_psi +
+# both g0_kernel classes) 18.8 GB for 7.43e11 FLOP, GEMM1 (g1_kernel +
+# g1_reduce) 15.8 GB for 1.91e11 FLOP
+TRAFFIC_PER_FLOP = {"gemm0": 18.83e9 / 7.429e11, "gemm1": 15.82e9 / 1.911e11}
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
 
 # name -> Hamiltonian, bond dimension and warm-up noise.
@@ -294,8 +299,12 @@ def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = F
         "frac_of_form_ceiling": achieved / ((peak if peak else 1900.0) / 6.0),
         "form_ceiling_note": ("dense TF32 runs at half the BF16 rate and split-TF32x3 issues three MMAs per "
                               "useful product: one sixth of the BF16 peak is the useful-FLOP ceiling"),
-        "algorithmic_flop": kflop, "ms": kms, "traffic": None,
-        "traffic_note": "per-launch DRAM bytes come from an ncu capture (profiles/), not from this run",
+        "algorithmic_flop": kflop, "ms": kms,
+        "traffic": kflop * (TRAFFIC_PER_FLOP["gemm0"] if tf["gemm0_ms"] >= tf["gemm1_ms"] else
+                            TRAFFIC_PER_FLOP["gemm1"]),
+        "traffic_note": ("DRAM read + write bytes of the phase per product: ncu's dram__bytes_read/write.sum "
+                         "per algorithmic FLOP measured on the n=24 M=1000 steady middle site (99,823 pairs), "
+                         "times this site's FLOP"),
     }
     # the FP64 product (simt_phase1/2<double>): the certification product of the
     # mixed Davidson, against the DFMA ceiling measured here (MEASURED_PEAKS has
