@@ -50,6 +50,8 @@ struct Opts {
     bool pdm = false;
     vector<string> perturb;
     int perturb_site = -1;    // centre moved here first (-1: n/2 - 1)
+    int perturb_threads = 0;  // threads of the perturbed walks (0: --threads); 1 gives every
+                              // perturbed H_eff the same GEMM pair order
 };
 
 static void mkdirs(const string &p) {
@@ -807,6 +809,12 @@ void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>>
                        const shared_ptr<MPS<S, double>> &mps, int n) {
     typedef double FL;
     mps->save_data();
+    shared_ptr<Threading> saved_threading = threading_();
+    if (o.perturb_threads > 0) {
+        threading_() = make_shared<Threading>(ThreadingTypes::OperatorBatchedGEMM | ThreadingTypes::Global,
+                                              o.perturb_threads, o.perturb_threads, 1);
+        threading_()->seq_type = SeqTypes::Tasked;
+    }
     for (size_t k = 0; k < o.perturb.size(); k++) {
         auto fd = make_shared<FCIDUMP<FL>>();
         fd->read(o.perturb[k]);
@@ -845,6 +853,7 @@ void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>>
         mpo2->deallocate();
         me2->remove_partition_files();
     }
+    threading_() = saved_threading;
     if (o.pdm) {
         Writer w(o.out + "/pdm");
         for (int k = 1; k <= 2; k++) {
@@ -987,6 +996,7 @@ int main(int argc, char **argv) {
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
         else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
         else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
+        else if (k == "--perturb-threads") o.perturb_threads = atoi(v.c_str());
         else if (k == "--perturb") {
             stringstream ss(v);
             string x;

@@ -56,7 +56,7 @@ from make_fixtures import HARNESS, RAW, read_dump  # noqa: E402
 N, M, T, NDIR = 16, 500, 1e-5, 20
 SITE = N // 2 - 1
 ARGS = ["--M", str(M), "--sym", "su2", "--sweeps", "8", "--seed", "1234", "--dav", "1e-12",
-        "--dump-sweep", "99", "--pdm", "1", "--perturb-site", str(SITE)]
+        "--dump-sweep", "99", "--pdm", "1", "--perturb-site", str(SITE), "--perturb-threads", "1"]
 OUT_JSON = os.path.join(HERE, "syn16_M500_grad.json")
 
 
