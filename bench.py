@@ -183,6 +183,18 @@ def mean(v):
     return float(sum(v) / len(v)) if v else None
 
 
+def middle_site(rows: list, n_sites: int) -> dict | None:
+    """block2's own per-site record of the middle site (sites n/2-1, n/2) of the
+    first sweep: Davidson iterations and time, and its multiply-add rate
+    (block2 prints 'FLOPS' as multiply-adds per second of the Davidson)."""
+    mid = [x for x in rows if x["sweep"] == 0 and x["site"] == n_sites // 2 - 1]
+    if not mid:
+        return None
+    x = mid[0]
+    return {"site": x["site"], "ndav": x["ndav"], "tdav_s": x["tdav"], "site_s": x["t"],
+            "mnk_per_s": x["mnk_per_s"], "flop_per_s": 2.0 * x["mnk_per_s"]}
+
+
 def per_site_forms(sites: dict, mixed_tag: str, fp64_tag: str) -> dict:
     """Site by site, the first sweep of the two forms from the same MPS (block2's
     per-site lines): Davidson seconds of each form, the energy difference, and
@@ -657,6 +669,7 @@ def run_reference(args):
                          "host": host_info()},
         "e2e": {"value": v, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "phases": {k: p[k] for k in ("teff", "teig", "tmve", "tdm", "tsplt")},
+        "middle_site": middle_site(r["sites"].get("ARM0", []), r["n_sites"]),
         "energy": arm["sweep_energies"], "wall_s": wall,
     }
 

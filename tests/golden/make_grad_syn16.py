@@ -29,7 +29,8 @@ tests/golden/syn16_M500_grad.json; the dumps (about 22 GB) stay in
 tests/golden/_raw/grad16 unless --no-keep is given.  Test infrastructure: runs the
 reference; nothing of the product imports it.
 
-    python tests/golden/make_grad_syn16.py [--threads 8] [--gpu]
+    python tests/golden/make_grad_syn16.py [--threads 8] [--gpu] [--reuse]
+    python tests/golden/make_grad_syn16.py --gpu-check DUMP_DIR OUT.json   # GPU machine, copied dumps
 """
 from __future__ import annotations
 
@@ -58,6 +59,65 @@ SITE = N // 2 - 1
 ARGS = ["--M", str(M), "--sym", "su2", "--sweeps", "8", "--seed", "1234", "--dav", "1e-12",
         "--dump-sweep", "99", "--pdm", "1", "--perturb-site", str(SITE), "--perturb-threads", "1"]
 OUT_JSON = os.path.join(HERE, "syn16_M500_grad.json")
+NPROJ = 8   # seeded random projections of dE/dops (the GPU check compares these)
+
+
+def projection(k: int, size: int) -> np.ndarray:
+    return np.random.default_rng(9000 + k).standard_normal(size)
+
+
+def site_dump(out: str, k: int):
+    d = os.path.join(out, f"perturb{k}")
+    (sd,) = [x for x in os.listdir(d) if x.startswith("sweep")]
+    return read_dump(os.path.join(d, sd))
+
+
+def gpu_gradient(base_a: dict, base_s: dict):
+    """dE/dops = d<psi|H_eff(ops)|psi>/d ops at the normalised centre tensor,
+    by the library's adjoint kernel behind torch.autograd on cuda:0."""
+    import torch
+
+    import b2g
+    from b2g.autodiff import heff_apply
+    from b2g.capi import PairSeq
+    psi = np.array(base_a["psi"], dtype=np.float64)
+    psi_n = psi / np.linalg.norm(psi)
+    ctx = b2g.Context(0)
+    h = b2g.EffectiveHamiltonian(ctx, PairSeq({k: base_a[k] for k in PAIR_FIELDS}), base_a["ops"],
+                                 int(base_s["psi_size"]), int(base_s["sigma_size"]))
+    ops_t = torch.from_numpy(np.array(base_a["ops"])).to("cuda:0").requires_grad_(True)
+    x = torch.from_numpy(psi_n).to("cuda:0")
+    f = torch.dot(x, heff_apply(h, ops_t, x))
+    f.backward()   # warm-up (adjoint schedule built on first use)
+    ops_t.grad = None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f = torch.dot(x, heff_apply(h, ops_t, x))
+    f.backward()
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    g = ops_t.grad.cpu().numpy()
+    h.close()
+    ctx.close()
+    return g, t
+
+
+def gpu_check(dump_dir: str, out_path: str):
+    """On a GPU machine: the library's adjoint at the dumped base site against
+    the oracle adjoint's seeded projections stored in the summary."""
+    with open(OUT_JSON) as f:
+        summ = json.load(f)
+    base_a, base_s = site_dump(dump_dir, 0)
+    g, t = gpu_gradient(base_a, base_s)
+    proj = [float(g @ projection(k, g.size)) for k in range(NPROJ)]
+    cpu = summ["adjoint_projections"]["cpu"]
+    res = {"gpu": proj, "cpu": cpu, "grad_norm_gpu": float(np.linalg.norm(g)),
+           "grad_norm_cpu": summ["adjoint_projections"]["grad_norm_cpu"],
+           "max_rel_diff": max(abs(a - b) / max(abs(b), 1e-300) for a, b in zip(proj, cpu)),
+           "seconds_forward_backward": t}
+    with open(out_path, "w") as f:
+        json.dump(res, f, indent=1)
+    print(json.dumps(res), flush=True)
 
 
 def direction(k: int):
@@ -110,7 +170,13 @@ def main():
     ap.add_argument("--gpu", action="store_true", help="also the library's adjoint kernel on cuda:0")
     ap.add_argument("--reuse", action="store_true", help="reuse an existing harness run in _raw/grad16")
     ap.add_argument("--no-keep", action="store_true", help="delete the dumps afterwards")
+    ap.add_argument("--gpu-check", nargs=2, metavar=("DUMP_DIR", "OUT_JSON"),
+                    help="only compare the library's adjoint at DUMP_DIR's base site with the stored "
+                         "oracle projections (a GPU machine with a copy of the dumps)")
     a = ap.parse_args()
+    if a.gpu_check:
+        gpu_check(*a.gpu_check)
+        return
     from b2g.capi import PairSeq
     from oracle import oracle
     h0, eri0, ec = synthetic_integrals(N, seed=0)
@@ -147,9 +213,7 @@ def main():
     dm2 = pdm_a["dm2"].reshape(N, N, N, N)
 
     def site(k):
-        d = os.path.join(out, f"perturb{k}")
-        (sd,) = [x for x in os.listdir(d) if x.startswith("sweep")]
-        return read_dump(os.path.join(d, sd))
+        return site_dump(out, k)
 
     base_a, base_s = site(0)
     seq = PairSeq({k: base_a[k] for k in PAIR_FIELDS})
@@ -163,25 +227,10 @@ def main():
     t0 = time.perf_counter()
     g_cpu, _ = oracle.adjoint(seq, base_a["ops"], psi_n, psi_n)
     t_adj_cpu = time.perf_counter() - t0
+    projections = [float(g_cpu @ projection(k, g_cpu.size)) for k in range(NPROJ)]
     g_gpu, t_adj_gpu = None, None
     if a.gpu:
-        import torch
-
-        import b2g
-        from b2g.autodiff import heff_apply
-        ctx = b2g.Context(0)
-        h = b2g.EffectiveHamiltonian(ctx, seq, base_a["ops"], int(base_s["psi_size"]), nsig)
-        ops_t = torch.from_numpy(np.array(base_a["ops"])).to("cuda:0").requires_grad_(True)
-        x = torch.from_numpy(psi_n).to("cuda:0")
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        f = torch.dot(x, heff_apply(h, ops_t, x))
-        f.backward()
-        torch.cuda.synchronize()
-        t_adj_gpu = time.perf_counter() - t0
-        g_gpu = ops_t.grad.cpu().numpy()
-        h.close()
-        ctx.close()
+        g_gpu, t_adj_gpu = gpu_gradient(base_a, base_s)
     rows = []
     for k, (hd, ed) in enumerate(dirs):
         (ap_, _), (am_, _) = site(1 + 2 * k), site(2 + 2 * k)
@@ -213,6 +262,8 @@ def main():
         "max_rel_err": {"adjoint_cpu_vs_pdm": rel("adjoint_cpu", "pdm"), "fd_vs_pdm": rel("fd", "pdm"),
                         "adjoint_cpu_vs_fd": rel("adjoint_cpu", "fd")},
         "bound": 1e-6, "seconds": {"harness": t_h, "adjoint_cpu": t_adj_cpu, "adjoint_gpu": t_adj_gpu},
+        "adjoint_projections": {"seeds": [9000 + k for k in range(NPROJ)], "cpu": projections,
+                                "grad_norm_cpu": float(np.linalg.norm(g_cpu))},
     }
     if g_gpu is not None:
         summary["max_rel_err"]["adjoint_gpu_vs_pdm"] = rel("adjoint_gpu", "pdm")

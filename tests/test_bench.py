@@ -31,3 +31,6 @@ def test_reference_arm_line():
     # one sweep at M after two at M/4: variational, above the converged
     # Hubbard L=16 U=4 M=250 energy and well below the random start
     assert -8.818767454782 - 1e-8 < line["energy"][-1] < -8.0
+    # block2's own record of the middle site and the host the sweep ran on
+    assert line["middle_site"]["site"] == 7 and line["middle_site"]["flop_per_s"] > 0
+    assert line["cpu_baseline"]["host"]["affinity_cpus"] >= 1
