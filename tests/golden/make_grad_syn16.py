@@ -31,6 +31,7 @@ reference; nothing of the product imports it.
 
     python tests/golden/make_grad_syn16.py [--threads 8] [--gpu] [--reuse]
     python tests/golden/make_grad_syn16.py --gpu-check DUMP_DIR OUT.json   # GPU machine, copied dumps
+    python tests/golden/make_grad_syn16.py --gpu-vs-oracle DUMP OUT.json    # GPU machine, a drop-in dump
 """
 from __future__ import annotations
 
@@ -75,17 +76,21 @@ def site_dump(out: str, k: int):
 def gpu_gradient(base_a: dict, base_s: dict):
     """dE/dops = d<psi|H_eff(ops)|psi>/d ops at the normalised centre tensor,
     by the library's adjoint kernel behind torch.autograd on cuda:0."""
+    from b2g.capi import PairSeq
+    return gpu_gradient_of(PairSeq({k: base_a[k] for k in PAIR_FIELDS}), base_a["ops"], base_a["psi"],
+                           int(base_s["psi_size"]), int(base_s["sigma_size"]))
+
+
+def gpu_gradient_of(seq, ops, psi, psi_size: int, sigma_size: int):
     import torch
 
     import b2g
     from b2g.autodiff import heff_apply
-    from b2g.capi import PairSeq
-    psi = np.array(base_a["psi"], dtype=np.float64)
+    psi = np.array(psi, dtype=np.float64)
     psi_n = psi / np.linalg.norm(psi)
     ctx = b2g.Context(0)
-    h = b2g.EffectiveHamiltonian(ctx, PairSeq({k: base_a[k] for k in PAIR_FIELDS}), base_a["ops"],
-                                 int(base_s["psi_size"]), int(base_s["sigma_size"]))
-    ops_t = torch.from_numpy(np.array(base_a["ops"])).to("cuda:0").requires_grad_(True)
+    h = b2g.EffectiveHamiltonian(ctx, seq, ops, psi_size, sigma_size)
+    ops_t = torch.from_numpy(np.array(ops)).to("cuda:0").requires_grad_(True)
     x = torch.from_numpy(psi_n).to("cuda:0")
     f = torch.dot(x, heff_apply(h, ops_t, x))
     f.backward()   # warm-up (adjoint schedule built on first use)
@@ -100,6 +105,30 @@ def gpu_gradient(base_a: dict, base_s: dict):
     h.close()
     ctx.close()
     return g, t
+
+
+def gpu_vs_oracle(dump_dir: str, out_path: str):
+    """On a GPU machine: at an H_eff the drop-in dumped during a sweep
+    (b2g.problem.load_dump; e.g. bench.py --workload syn16 --keep-dump DIR),
+    dE/dops from the library's adjoint kernel against the oracle's numpy
+    adjoint, elementwise (the derivative the integral chain above uses)."""
+    from oracle import oracle
+
+    from b2g.problem import load_dump
+    prob = load_dump(dump_dir)
+    psi = np.array(prob.extra.get("psi_converged", prob.psi), dtype=np.float64)
+    g, t = gpu_gradient_of(prob.seq(), prob.ops, psi, prob.psi_size, prob.sigma_size)
+    psi_n = psi / np.linalg.norm(psi)
+    t0 = time.perf_counter()
+    gc, _ = oracle.adjoint(prob.seq(), prob.ops, psi_n, psi_n)
+    tc = time.perf_counter() - t0
+    res = {"site": int(prob.meta["site"]), "sweep": int(prob.meta["isweep"]), "n_pairs": int(prob.seq().n),
+           "ops_size": int(prob.ops.size), "rel_diff_norm": float(np.linalg.norm(g - gc) / np.linalg.norm(gc)),
+           "max_abs_diff_over_max": float(np.abs(g - gc).max() / np.abs(gc).max()),
+           "seconds_gpu_forward_backward": t, "seconds_oracle_adjoint": tc}
+    with open(out_path, "w") as f:
+        json.dump(res, f, indent=1)
+    print(json.dumps(res), flush=True)
 
 
 def gpu_check(dump_dir: str, out_path: str):
@@ -121,7 +150,12 @@ def gpu_check(dump_dir: str, out_path: str):
 
 
 def direction(k: int):
-    """Seeded random direction in integral space: symmetric h_D, 8-fold symmetric eri_D."""
+    """Seeded random direction in integral space: symmetric h_D, 8-fold symmetric
+    eri_D, scaled so that its largest element is 1 (each integral moves by at
+    most t): the energy at fixed MPS is linear in the integrals, so the central
+    difference has no truncation error and a larger signal only lowers its
+    rounding error (unit-norm directions move each integral by ~1e-7 t and
+    leave the differences of two 87 Ha energies at the 1e-6 relative level)."""
     rng = np.random.default_rng(7000 + k)
     h = rng.standard_normal((N, N))
     h = 0.5 * (h + h.T)
@@ -129,7 +163,7 @@ def direction(k: int):
     e = (x + x.transpose(1, 0, 2, 3) + x.transpose(0, 1, 3, 2) + x.transpose(1, 0, 3, 2)
          + x.transpose(2, 3, 0, 1) + x.transpose(3, 2, 0, 1) + x.transpose(2, 3, 1, 0)
          + x.transpose(3, 2, 1, 0)) / 8.0
-    s = 1.0 / np.sqrt(np.sum(h * h) + np.sum(e * e))
+    s = 1.0 / max(np.abs(h).max(), np.abs(e).max())
     return h * s, e * s
 
 
@@ -173,7 +207,13 @@ def main():
     ap.add_argument("--gpu-check", nargs=2, metavar=("DUMP_DIR", "OUT_JSON"),
                     help="only compare the library's adjoint at DUMP_DIR's base site with the stored "
                          "oracle projections (a GPU machine with a copy of the dumps)")
+    ap.add_argument("--gpu-vs-oracle", nargs=2, metavar=("DUMP_DIR", "OUT_JSON"),
+                    help="only compare the library's adjoint with the oracle's at an H_eff the drop-in "
+                         "dumped (bench.py --keep-dump)")
     a = ap.parse_args()
+    if a.gpu_vs_oracle:
+        gpu_vs_oracle(*a.gpu_vs_oracle)
+        return
     if a.gpu_check:
         gpu_check(*a.gpu_check)
         return
