@@ -55,7 +55,7 @@ static void free_plan(DevicePlan &p) {
     cudaFree(p.t2multi), cudaFree(p.g0tile), cudaFree(p.g0col);
     cudaFree(p.g1tile), cudaFree(p.g1stage), cudaFree(p.g1task), cudaFree(p.g1aimg);
     cudaFree(p.g1red), cudaFree(p.g1cover), cudaFree(p.region_cb);
-    cudaFree(p.diag_task), cudaFree(p.diag_tlist);
+    cudaFree(p.diag_task), cudaFree(p.diag_tlist), cudaFree(p.diag_item);
     p = DevicePlan();
 }
 
@@ -146,7 +146,8 @@ static int install_plan(b2g_heff *h, const HostPlan &hp) {
         (rc = upload(hp.g1aimg, &p.g1aimg, s)) ||
         (rc = upload(hp.g1red, &p.g1red, s)) || (rc = upload(hp.g1cover, &p.g1cover, s)) ||
         (rc = upload(hp.g0psi, &p.g0psi, s)) || (rc = upload(hp.region_cb, &p.region_cb, s)) ||
-        (rc = upload(hp.diag_task, &p.diag_task, s)) || (rc = upload(hp.diag_tlist, &p.diag_tlist, s)))
+        (rc = upload(hp.diag_task, &p.diag_task, s)) || (rc = upload(hp.diag_tlist, &p.diag_tlist, s)) ||
+        (rc = upload(hp.diag_item, &p.diag_item, s)))
         return rc;
     p.n_g1task = (int64_t)hp.g1task.size(), p.n_g1aimg = (int64_t)hp.g1aimg.size();
     p.n_g1red = (int64_t)hp.g1red.size(), p.n_g0tile = (int64_t)hp.g0tile.size();

@@ -19,7 +19,9 @@
 // One CTA per tile, one thread per tile column; a thread owns the column's
 // cells and loops over the tile's list in contribution order for each of
 // them (no atomics, reproducible; tiles are disjoint, so every cell has one
-// owner).  The list is staged through shared memory in chunks.
+// owner).  The list is staged through shared memory in chunks; each entry
+// carries the frame position of its psi sub-block, so the psi index of a cell
+// needs no division.
 #include <algorithm>
 
 #include "b2g_internal.h"
@@ -32,13 +34,11 @@ constexpr int kDiagChunk = 128;   // contributions staged in shared memory at a 
 
 __global__ void __launch_bounds__(kDiagTileCols) diag_kernel(const DiagTask *__restrict__ tasks,
                                                              const int32_t *__restrict__ tlist,
+                                                             const DiagItem *__restrict__ items,
                                                              const Region *__restrict__ regions,
-                                                             const Contrib *__restrict__ contribs,
-                                                             const WorkDesc *__restrict__ works,
                                                              const double *__restrict__ ops,
                                                              double *__restrict__ diag) {
-    __shared__ Contrib sc[kDiagChunk];
-    __shared__ WorkDesc sw[kDiagChunk];
+    __shared__ DiagItem si[kDiagChunk];
     const DiagTask t = tasks[blockIdx.x];
     const Region rg = regions[t.g];
     const int c = t.c0 + (int)threadIdx.x;
@@ -51,36 +51,46 @@ __global__ void __launch_bounds__(kDiagTileCols) diag_kernel(const DiagTask *__r
     for (int64_t e0 = t.lb; e0 < t.le; e0 += kDiagChunk) {
         const int n = (int)min((int64_t)kDiagChunk, t.le - e0);
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            sc[i] = contribs[tlist[e0 + i]];
-            sw[i] = works[sc[i].u];
-        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            si[i] = items[tlist[e0 + i]];
         __syncthreads();
         if (!col_ok)
             continue;
         for (int e = 0; e < n; e++) {
-            const Contrib &ct = sc[e];
-            const int j = c - ct.col0;
-            if (j < 0 || j >= ct.n1)
+            const DiagItem &it = si[e];
+            const int j = c - it.col0;
+            if (j < 0 || j >= it.n1)
                 continue;
-            const WorkDesc &w = sw[e];
+            // the psi column l of cell column c (and the row shift when the psi
+            // window wraps the frame), row-independent
+            int l = c - it.ca, kshift = 0;
+            if (l < 0)
+                l += rg.ld, kshift = 1;
 #pragma unroll
             for (int q = 0; q < kDiagTileRows; q++) {
                 const int r = t.r0 + q;
-                const int i = r - ct.row0;
-                if (r >= t.r1 || i < 0 || i >= ct.m1)
+                const int i = r - it.row0;
+                if (r >= t.r1 || i < 0 || i >= it.m1)
                     continue;
                 covered[q] = true;
-                const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
-                if (x < w.a0)
-                    continue;
-                const uint64_t dy = x - w.a0;
-                const uint64_t k = dy / (uint64_t)w.lda0, l = dy % (uint64_t)w.lda0;
-                if (k >= (uint64_t)w.m0 || l >= (uint64_t)w.k0)
-                    continue;
-                const double lv = ops[ct.a1 + (ct.ta1 ? k * ct.lda1 + i : (uint64_t)i * ct.lda1 + k)];
-                const double rv = ops[w.b0 + (w.tb0 ? (uint64_t)j * w.ldb0 + l : l * w.ldb0 + j)];
-                s[q] = fma(ct.alpha * lv, rv, s[q]);
+                uint64_t k, lu;
+                if (it.same_ld) {
+                    const int kk = r - it.ra - kshift;
+                    if (kk < 0 || kk >= it.m0 || l >= it.k0)
+                        continue;
+                    k = (uint64_t)kk, lu = (uint64_t)l;
+                } else {
+                    const uint64_t x = rg.base + (uint64_t)r * rg.ld + (uint64_t)c;
+                    if (x < it.a0)
+                        continue;
+                    const uint64_t dy = x - it.a0;
+                    k = dy / (uint64_t)it.lda0, lu = dy % (uint64_t)it.lda0;
+                    if (k >= (uint64_t)it.m0 || lu >= (uint64_t)it.k0)
+                        continue;
+                }
+                const double lv = ops[it.a1 + (it.ta1 ? k * it.lda1 + i : (uint64_t)i * it.lda1 + k)];
+                const double rv = ops[it.b0 + (it.tb0 ? (uint64_t)j * it.ldb0 + lu : lu * it.ldb0 + j)];
+                s[q] = fma(it.alpha * lv, rv, s[q]);
             }
         }
     }
@@ -106,8 +116,8 @@ cudaError_t launch_diag(const DevicePlan &p, const double *ops, double *diag, cu
     if (p.n_diag_task > 0x7fffffff)
         return cudaErrorInvalidConfiguration;
     note_launch();
-    diag_kernel<<<(unsigned)p.n_diag_task, kDiagTileCols, 0, s>>>(p.diag_task, p.diag_tlist, p.regions,
-                                                                   p.contribs, p.works, ops, diag);
+    diag_kernel<<<(unsigned)p.n_diag_task, kDiagTileCols, 0, s>>>(p.diag_task, p.diag_tlist, p.diag_item,
+                                                                   p.regions, ops, diag);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,22 @@ struct DiagTask {
     int32_t g, r0, r1, c0, c1, pad;
     int64_t lb, le;
 };
+// one contribution that can reach diag(H_eff), in its region's frame: the
+// diagonal cell (r, c) (flat x = base + r ld + c) takes alpha op(L)[i][k]
+// op(R)[l][j] with i = r - row0, j = c - col0 and x - a0 = k lda0 + l.  When
+// the psi sub-block lies in a block with the region's row stride (lda0 = ld,
+// always so for a square H_eff: overlapping psi and sigma sub-blocks are in
+// one wavefunction block), x - a0 = (r - ra) ld + (c - ca) and (k, l) follow
+// without a division (same_ld = 1).
+struct DiagItem {
+    uint64_t a1, b0, a0;    // op(L) / op(R) block offsets in the blob, psi offset
+    double alpha;           // alpha0 * alpha1
+    int32_t row0, col0, m1, n1;   // sigma rectangle in the frame
+    int32_t ra, ca;         // frame row / column of a0 (0 <= ca < ld) when same_ld
+    int32_t m0, k0, lda0, lda1, ldb0;
+    int16_t ta1, tb0;
+    int32_t same_ld, pad;
+};
 constexpr int kDiagTileCols = 256;     // columns per tile (one per thread)
 constexpr int kDiagTileRows = 8;       // rows per tile
 struct Tile2 {          // a phase-2 tile split over several chunks (reduced after)
@@ -186,7 +202,8 @@ struct HostPlan {
     // contributions whose psi sub-block overlaps their sigma sub-block (the
     // only ones that can reach diag(H_eff)), listed per row band of each region
     std::vector<DiagTask> diag_task;
-    std::vector<int32_t> diag_tlist;
+    std::vector<int32_t> diag_tlist;    // indices into diag_item
+    std::vector<DiagItem> diag_item;
     std::vector<Task1> t1;
     std::vector<Task2> t2;
     std::vector<Tile2> t2multi;
@@ -217,6 +234,7 @@ struct DevicePlan {
     int64_t *region_cb = nullptr;
     DiagTask *diag_task = nullptr;
     int32_t *diag_tlist = nullptr;
+    DiagItem *diag_item = nullptr;
     int64_t n_diag_task = 0;
     Task1 *t1 = nullptr;
     Task2 *t2 = nullptr;

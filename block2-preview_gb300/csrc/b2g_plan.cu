@@ -331,6 +331,20 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 const uint64_t y0 = w.a0, y1 = w.a0 + extent(false, w.m0, w.k0, w.lda0);
                 if (!(x0 < y1 && y0 < x1))
                     continue;
+                DiagItem it;
+                it.a1 = ct.a1, it.b0 = w.b0, it.a0 = w.a0, it.alpha = ct.alpha;
+                it.row0 = ct.row0, it.col0 = ct.col0, it.m1 = ct.m1, it.n1 = ct.n1;
+                it.m0 = w.m0, it.k0 = w.k0, it.lda0 = w.lda0, it.lda1 = ct.lda1, it.ldb0 = w.ldb0;
+                it.ta1 = (int16_t)ct.ta1, it.tb0 = (int16_t)w.tb0, it.pad = 0;
+                it.same_ld = w.lda0 == rg.ld ? 1 : 0, it.ra = 0, it.ca = 0;
+                if (it.same_ld) {
+                    // floor division of the (possibly negative) frame offset of a0
+                    const int64_t d = (int64_t)w.a0 - (int64_t)rg.base;
+                    const int64_t ra = d >= 0 ? d / rg.ld : -((-d + rg.ld - 1) / rg.ld);
+                    it.ra = (int32_t)ra, it.ca = (int32_t)(d - ra * rg.ld);
+                }
+                const int32_t item = (int32_t)plan.diag_item.size();
+                plan.diag_item.push_back(it);
                 const uint64_t lo = std::max(x0, y0), hi = std::min(x1, y1);
                 int64_t r_lo = (int64_t)((lo - rg.base) / (uint64_t)rg.ld);
                 int64_t r_hi = (int64_t)((hi - 1 - rg.base) / (uint64_t)rg.ld) + 1;
@@ -339,7 +353,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                 const int64_t cb0 = ct.col0 / kDiagTileCols, cb1 = (ct.col0 + ct.n1 - 1) / kDiagTileCols;
                 for (int64_t rb = r_lo / kDiagTileRows; rb < nrb && rb * kDiagTileRows < r_hi; rb++)
                     for (int64_t cb = cb0; cb <= cb1 && cb < ncb; cb++)
-                        tile[(size_t)(rb * ncb + cb)].push_back((int32_t)q);
+                        tile[(size_t)(rb * ncb + cb)].push_back(item);
             }
             for (int32_t rb = 0; rb < nrb; rb++)
                 for (int32_t cb = 0; cb < ncb; cb++) {
