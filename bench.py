@@ -4,32 +4,34 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload syn24|syn16|syn32|hub16] [--fp64-sweeps KF] [--dav THR]
 
-A step is one full two-site sweep of block2's own DMRG::solve (all sites,
-forward then backward alternating) on the named workload, run by the sweep
-program lib/dmrg_sweep (block2's DMRG with b2g_block2::GpuTensorFunctions /
-GpuDMRG installed: every Davidson solve on the device, block2's environment,
-truncation and bookkeeping on the host).  Default workload: the synthetic ab
-initio Hamiltonian n=24, N=24, S=0, SU(2), M=1000 (seeded integral recipe).
+A step is one full two-site sweep of block2's own DMRG::solve at bond
+dimension M (all sites, forward), run by the sweep program lib/dmrg_sweep
+(block2's DMRG with b2g_block2::GpuTensorFunctions / GpuDMRG installed: every
+Davidson solve on the device, block2's environment, truncation and
+bookkeeping on the host).  Default workload: the synthetic ab initio
+Hamiltonian n=24, N=24, S=0, SU(2), M=1000 (seeded integral recipe).
 
-Our arm: W warm-up sweeps (mixed form; two at M/4, the rest at M) from the
-seeded random MPS;
-then, from that same MPS (MPS::deep_copy per arm), K timed sweeps in the mixed
-form (split-TF32x3 tensor-core products + FP64 defect correction) and KF
-sweeps in the plain FP64 form.  `value` is the mean wall time of a mixed
-sweep; a block2 sweep is driven from host memory (every site's operators are
-uploaded as the sweep reaches it), so the sweep has no HBM-resident variant and
-`e2e` is the same measurement; `device_resident` gives the part spent in the
-device Davidson solves with the operators already in HBM.  The mixed/FP64
-sweep-time ratio and the per-sweep |dE| between the forms are reported beside
-it.  The middle-site H_eff of a sweep with M on both sides (the last warm-up
-sweep, or the mixed arm's second sweep when the warm-up is only the two M/4
-sweeps) is dumped by the drop-in and measured on its own (H_eff*psi TFLOP/s per form on the real operators,
-relative error against FP64, the roofline of the dominant kernel).
+The state every step starts from: two sweeps at M/4 (mixed form, Davidson
+1e-8) from the seeded random MPS.  The step is the first sweep at M from that
+MPS: W untimed and then K timed steps each run on their own copy of it
+(MPS::deep_copy, one arm of the sweep program each), so every step repeats the
+same work, and `--impl reference` times the same sweep with block2's CPU
+path.  Mixed form: split-TF32x3 tensor-core products with FP64 defect
+correction.  `value` is the mean wall time of the timed steps; block2 drives a
+sweep from host memory (every site's operators are uploaded when the sweep
+reaches it), so the sweep has no HBM-resident variant and `e2e` is the same
+measurement; `device_resident` is the part spent in the device Davidson
+solves.  From the same MPS the bench also runs the step in the plain FP64
+form (time ratio, |dE|, site by site) and one untimed mixed arm of two sweeps
+whose second, the first with M on both sides, gives the steady sweep time and
+the middle-site H_eff that is dumped by the drop-in and measured on its own
+(H_eff*psi TFLOP/s per form on the real operators, relative error against
+FP64, diag(H_eff), both Davidson forms, the roofline of the dominant kernel).
 
 `--impl reference` runs block2's own CPU path (oracle/_ref/dmrg_sweep_ref,
-built from block2's sources with no GPU code) on this host's cores: one full
-sweep of the same workload from the same seeded random MPS with the timed
-sweeps' schedule (a CPU sweep takes minutes, so the sample is one sweep).
+built from block2's sources with no GPU code) on this host's cores: the same
+two M/4 sweeps from the same seeded random MPS, then the step, timed (a CPU
+sweep takes minutes, so the sample is one step).
 Multi-GPU: a sweep does not shard here (replicas only); each rank runs its own
 sweep and the slowest rank's time is reported.
 """
@@ -463,6 +465,14 @@ def heff_only(dump_dir: str, form_name: str, products: int, dev_index: int) -> d
 
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, rank, local_rank, world, dist):
+    """One step = the first full sweep at M from the state that two sweeps at
+    M/4 leave (the seeded random MPS, Davidson 1e-8): every step (W untimed,
+    then K timed) is an arm of the sweep program that starts from its own copy
+    of that one MPS (MPS::deep_copy), so each repeats the same work, and
+    `--impl reference` times the same sweep of block2's CPU path.  Beside the
+    steps, from the same MPS: the FP64 form on the same sweep, and one untimed
+    mixed arm of two sweeps whose second (M on both sides) gives the steady
+    sweep time and the dumped middle-site H_eff."""
     import torch
 
     from b2g.sweep import SWEEP_BIN, run_sweep
@@ -470,68 +480,68 @@ def run_ours(args, rank, local_rank, world, dist):
     spec = WORKLOADS[args.workload]
     wd = tempfile.mkdtemp(prefix="b2g_bench_", dir=args.workdir)
     ham = hamiltonian(spec, wd)
-    warm = max(2, args.warmup + args.warmup % 2)  # even: the arms start forward from site 0
-    wn = tuple(spec["warm_noises"][min(i, len(spec["warm_noises"]) - 1)] for i in range(warm))
-    wm = (spec["M"] // 4,) * 2 + (spec["M"],) * (warm - 2)
-    wdv = (1e-8,) * 2 + (args.warm_dav or args.dav,) * (warm - 2)
-    kf = min(args.steps, args.fp64_sweeps)
-    arms = [f"gpu:tf32x3/{args.steps}"] + ([f"gpu:fp64/{kf}"] if kf > 0 else [])
+    prep = 2
+    wm, wn, wdv = (spec["M"] // 4,) * prep, (spec["warm_noises"][0],) * prep, (1e-8,) * prep
+    W, K, kf = max(0, args.warmup), max(1, args.steps), max(0, args.fp64_sweeps)
+    steady_sweep = args.dump_arm_sweep if args.dump_arm_sweep >= 0 else 1
+    arms = ["gpu:tf32x3/1"] * (W + K)            # W untimed steps, then the K timed ones
+    i_fp64 = len(arms)
+    arms += ["gpu:fp64/1"] * kf
+    i_steady = len(arms)
+    arms.append(f"gpu:tf32x3/{steady_sweep + 1}")
+    i_part = len(arms)
     if args.partial_end:
-        # the FP64 comparison on one partial forward sweep (sites 0 .. E-2) of
-        # both forms from the same MPS (a full FP64 sweep is too long here)
-        kf = 1
-        arms = [f"gpu:tf32x3/{args.steps}", f"gpu:fp64/1@{args.partial_end}",
-                f"gpu:tf32x3/1@{args.partial_end}",
-                f"gpu:tf32x3/1@{args.partial_end}"]   # a fourth, untimed arm writes the dump
-    n_main = len(arms)
+        # both forms on one partial forward sweep (sites 0 .. E-2) from the same MPS
+        arms += [f"gpu:fp64/1@{args.partial_end}", f"gpu:tf32x3/1@{args.partial_end}"]
+    i_tol = len(arms)
     if args.tol_study:
-        # both forms again from the same MPS at a tighter Davidson tolerance:
-        # how far each form's sweep energies move with the tolerance alone
-        arms += [f"gpu:tf32x3/{max(kf, 1)}%{args.tol_study:g}", f"gpu:fp64/{max(kf, 1)}%{args.tol_study:g}"]
+        # both forms again at a tighter Davidson tolerance: how far each form's
+        # sweep energy moves with the tolerance alone
+        arms += [f"gpu:tf32x3/1%{args.tol_study:g}", f"gpu:fp64/1%{args.tol_study:g}"]
+    i_cpu = len(arms)
     if args.cpu_arm:
         arms.append("cpu/1")
     dump = os.path.join(wd, "heff_dump")
-    dump_sweep_arm = (args.dump_arm_sweep if args.dump_arm_sweep >= 0 else
-                      -1 if warm >= 4 else min(1, args.steps - 1))
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler(local_rank)
     clocks.start()
     t0 = time.perf_counter()
-    r = run_sweep(binary=SWEEP_BIN, sym=spec["sym"], M=(spec["M"],), sweeps=args.steps, noises=(0.0,),
-                  dav=(args.dav,), arms=tuple(arms), warm_sweeps=warm, warm_noises=wn, warm_dav=wdv, warm_M=wm,
+    r = run_sweep(binary=SWEEP_BIN, sym=spec["sym"], M=(spec["M"],), sweeps=1, noises=(0.0,),
+                  dav=(args.dav,), arms=tuple(arms), warm_sweeps=prep, warm_noises=wn, warm_dav=wdv, warm_M=wm,
                   warm_device="gpu:tf32x3", threads=args.threads or host_threads(),
                   workdir=os.path.join(wd, "run"), dump_heff=dump,
-                  # the dumped site: with --partial-end the last site of an extra
-                  # mixed partial sweep; else the middle site of a sweep with M on
-                  # both sides: the last warm-up sweep when the warm-up reaches M
-                  # twice (warm >= 4), else the mixed arm's second sweep (its first
-                  # grows the bonds from M/4)
-                  dump_arm=3 if args.partial_end else (-1 if dump_sweep_arm < 0 else 0),
-                  dump_sweep=0 if args.partial_end else (warm - 1 if dump_sweep_arm < 0 else dump_sweep_arm),
+                  # the dumped site: the middle of the steady arm's sweep with M
+                  # on both sides, or with --partial-end the last site of the
+                  # mixed partial sweep
+                  dump_arm=i_part + 1 if args.partial_end else i_steady,
+                  dump_sweep=0 if args.partial_end else steady_sweep,
                   dump_site=args.partial_end - 2 if args.partial_end else -1,
                   env=rank_device_env(local_rank) if world > 1 else None,
                   stack_gb=spec.get("stack_gb", 4.0), **ham)
     wall = time.perf_counter() - t0
     ck = clocks.stop()
-    mixed = r["arms"][0]
-    fp64 = r["arms"][1] if kf > 0 else None
-    t_sweep = mean(mixed["sweep_time"])
+    timed = r["arms"][W:W + K]
+    first = timed[0]
+    t_sweep = mean([a["sweep_time"][0] for a in timed])
     tt = torch.tensor([t_sweep], dtype=torch.float64, device="cuda")
     if dist is not None:
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
     t_sweep = float(tt[0])
-    ph = mixed["phases"]
+    ph = [a["phases"][0] for a in timed]
+    steady = r["arms"][i_steady]
     res = {
-        "metric": METRIC, "value": t_sweep, "unit": "s/sweep", "n_gpus": world, "steps": args.steps,
-        "warmup": warm, "ms_per_step": t_sweep * 1e3, "higher_is_better": False, "scaling": "weak",
+        "metric": METRIC, "value": t_sweep, "unit": "s/sweep", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": t_sweep * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None,
         "dtype": "tf32x3 tensor-core products (f32 accumulate) + f64 Davidson, residual and truncation",
         "data": "synthetic: seeded integrals / Hubbard chain, seeded random initial MPS",
         "config": {"workload": f"{args.workload}: full two-site sweep of block2's DMRG::solve, "
                                f"{spec['desc']}", "n_sites": r["n_sites"], "bond_dim": spec["M"],
+                   "step": ("the first sweep at M from the MPS two sweeps at M/4 leave; every step starts "
+                            "from its own copy of that MPS"),
                    "davidson_conv_thrd": args.dav, "noise": 0.0,
-                   "warmup_schedule": {"M": wm, "noise": wn, "dav": wdv},
+                   "state_preparation": {"M": wm, "noise": wn, "dav": wdv},
                    "host_threads": r["threads"], "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (operator blobs of GBs per site)"},
         "e2e": {"value": t_sweep, "unit": "s/sweep", "h2d_bytes_per_step": mean([p["h2d_bytes"] for p in ph]),
@@ -544,69 +554,69 @@ def run_ours(args, rank, local_rank, world, dist):
         "sweep_breakdown_s": {k: mean([p[k] for p in ph]) for k in
                               ("teff", "teig", "tmve", "tdm", "tsplt", "gpu_davidson", "gpu_translate",
                                "gpu_plan_upload")},
-        "sweeps": {"mixed": {"energies": mixed["sweep_energies"], "discarded_weights": mixed["discarded_weights"],
-                             "seconds": mixed["sweep_time"], "gpu": mixed.get("gpu")},
-                   "warmup_seconds": r["warm"]["sweep_time"], "warmup_energies": r["warm"]["sweep_energies"]},
-        "first_full_M_sweep_s": (r["warm"]["sweep_time"][2] if warm > 2 else mixed["sweep_time"][0]),
-        "first_full_M_sweep_note": ("the first sweep at M after the two M/4 warm-up sweeps (mixed form): the "
-                                    "sweep `--impl reference` times on the host cores"),
-        "gpu_launches": int(mixed["gpu"]["kernel_launches"]),
+        "sweeps": {"mixed": {"seconds": [a["sweep_time"][0] for a in timed],
+                             "energies": [a["sweep_energies"][0] for a in timed],
+                             "discarded_weights": first["discarded_weights"], "gpu": first.get("gpu")},
+                   "untimed_steps_seconds": [a["sweep_time"][0] for a in r["arms"][:W]],
+                   "state_preparation_seconds": r["warm"]["sweep_time"],
+                   "state_preparation_energies": r["warm"]["sweep_energies"]},
+        "steady_sweep": {"seconds": steady["sweep_time"][steady_sweep],
+                         "energy": steady["sweep_energies"][steady_sweep],
+                         "breakdown_s": {k: steady["phases"][steady_sweep][k] for k in
+                                         ("teff", "teig", "tmve", "tsplt", "gpu_davidson", "gpu_plan_upload")},
+                         "what": (f"untimed: sweep {steady_sweep} of one more mixed arm from the same MPS, the "
+                                  "first with M on both sides (its middle site is the dumped H_eff)")},
+        "gpu_launches": int(sum(a["gpu"]["kernel_launches"] for a in timed)),
         "clocks": ck, "wall_s": wall,
     }
-    if fp64 is not None and args.partial_end:
-        part = r["arms"][2]
-        res["sweeps"]["fp64_partial"] = {"energies": fp64["sweep_energies"], "seconds": fp64["sweep_time"],
-                                         "gpu": fp64.get("gpu"), "end_site": args.partial_end}
-        res["sweeps"]["mixed_partial"] = {"energies": part["sweep_energies"], "seconds": part["sweep_time"],
-                                          "gpu": part.get("gpu"), "end_site": args.partial_end}
-        res["forms"] = {"what": f"one partial forward sweep (sites 0..{args.partial_end - 2}) of each form "
-                                "from the same MPS",
-                        "mixed_s": part["sweep_time"][0], "fp64_s": fp64["sweep_time"][0],
-                        "fp64_over_mixed": fp64["sweep_time"][0] / part["sweep_time"][0],
-                        "abs_dE": abs(part["sweep_energies"][0] - fp64["sweep_energies"][0]), "dE_bound": 1e-8,
-                        "fp64_davidson_s": fp64["phases"][0]["gpu_davidson"],
-                        "mixed_davidson_s": part["phases"][0]["gpu_davidson"]}
-    elif fp64 is not None:
-        dE = [abs(a - b) for a, b in zip(mixed["sweep_energies"][:kf], fp64["sweep_energies"])]
-        t64 = mean(fp64["sweep_time"])
-        res["sweeps"]["fp64"] = {"energies": fp64["sweep_energies"], "discarded_weights": fp64["discarded_weights"],
-                                 "seconds": fp64["sweep_time"], "gpu": fp64.get("gpu")}
-        res["forms"] = {"mixed_s_per_sweep": mean(mixed["sweep_time"][:kf]), "fp64_s_per_sweep": t64,
-                        "fp64_over_mixed": t64 / mean(mixed["sweep_time"][:kf]),
+    energies = res["sweeps"]["mixed"]["energies"]
+    res["sweeps"]["mixed"]["max_energy_spread"] = max(energies) - min(energies)
+    if kf > 0:
+        fps = r["arms"][i_fp64:i_fp64 + kf]
+        t64 = mean([a["sweep_time"][0] for a in fps])
+        dE = [abs(a["sweep_energies"][0] - first["sweep_energies"][0]) for a in fps]
+        res["sweeps"]["fp64"] = {"seconds": [a["sweep_time"][0] for a in fps],
+                                 "energies": [a["sweep_energies"][0] for a in fps],
+                                 "discarded_weights": fps[0]["discarded_weights"], "gpu": fps[0].get("gpu")}
+        res["forms"] = {"what": "the same step (first sweep at M from the same MPS) in the FP64 form",
+                        "mixed_s_per_sweep": t_sweep, "fp64_s_per_sweep": t64, "fp64_over_mixed": t64 / t_sweep,
                         "abs_dE_per_sweep": dE, "max_abs_dE": max(dE), "dE_bound": 1e-8,
-                        "first_sweep_sites": per_site_forms(r["sites"], "ARM0", "ARM1")}
+                        "first_sweep_sites": per_site_forms(r["sites"], f"ARM{W}", f"ARM{i_fp64}")}
+    if args.partial_end:
+        f64p, mxp = r["arms"][i_part], r["arms"][i_part + 1]
+        res["partial"] = {"what": f"one partial forward sweep (sites 0..{args.partial_end - 2}) of each form "
+                                  "from the same MPS",
+                          "mixed_s": mxp["sweep_time"][0], "fp64_s": f64p["sweep_time"][0],
+                          "fp64_over_mixed": f64p["sweep_time"][0] / mxp["sweep_time"][0],
+                          "abs_dE": abs(mxp["sweep_energies"][0] - f64p["sweep_energies"][0]), "dE_bound": 1e-8,
+                          "fp64_davidson_s": f64p["phases"][0]["gpu_davidson"],
+                          "mixed_davidson_s": mxp["phases"][0]["gpu_davidson"]}
     if args.tol_study:
-        tm, tf = r["arms"][n_main], r["arms"][n_main + 1]
-        nk = len(tf["sweep_energies"])
-
-        def diff(a, b):
-            return [abs(x - y) for x, y in zip(a["sweep_energies"][:nk], b["sweep_energies"][:nk])]
+        tm, tf = r["arms"][i_tol], r["arms"][i_tol + 1]
         res["tolerance_study"] = {
             "dav": args.dav, "tight_dav": args.tol_study,
             "what": ("both forms from the same MPS at the bench tolerance and at a tighter one: the "
                      "mixed-vs-FP64 energy difference at each tolerance, and how far each form's own "
-                     "sweep energies move when only the Davidson tolerance changes"),
-            "abs_dE_mixed_vs_fp64_tight": diff(tm, tf),
-            "fp64_tolerance_shift": diff(fp64, tf) if fp64 is not None and not args.partial_end else None,
-            "mixed_tolerance_shift": diff(mixed, tm),
-            "tight_energies": {"mixed": tm["sweep_energies"], "fp64": tf["sweep_energies"]},
-            "tight_seconds": {"mixed": tm["sweep_time"], "fp64": tf["sweep_time"]},
-            "tight_gpu": {"mixed": tm.get("gpu"), "fp64": tf.get("gpu")}}
-        if fp64 is not None and not args.partial_end:
-            res["tolerance_study"]["abs_dE_mixed_vs_fp64"] = diff(mixed, fp64)
-            res["tolerance_study"]["tight_fp64_over_mixed"] = mean(tf["sweep_time"]) / mean(tm["sweep_time"])
+                     "sweep energy moves when only the Davidson tolerance changes"),
+            "abs_dE_mixed_vs_fp64_tight": abs(tm["sweep_energies"][0] - tf["sweep_energies"][0]),
+            "mixed_tolerance_shift": abs(tm["sweep_energies"][0] - first["sweep_energies"][0]),
+            "tight_energies": {"mixed": tm["sweep_energies"][0], "fp64": tf["sweep_energies"][0]},
+            "tight_seconds": {"mixed": tm["sweep_time"][0], "fp64": tf["sweep_time"][0]}}
+        if kf > 0:
+            res["tolerance_study"]["fp64_tolerance_shift"] = abs(r["arms"][i_fp64]["sweep_energies"][0]
+                                                                 - tf["sweep_energies"][0])
     if args.cpu_arm:
-        cpu = r["arms"][-1]
+        cpu = r["arms"][i_cpu]
         res["sweeps"]["cpu"] = {"energies": cpu["sweep_energies"], "seconds": cpu["sweep_time"],
                                 "phases": cpu["phases"]}
         res["same_state_cpu"] = {
-            "cpu_s_per_sweep": cpu["sweep_time"][0], "mixed_s_per_sweep": mixed["sweep_time"][0],
-            "cpu_over_mixed": cpu["sweep_time"][0] / mixed["sweep_time"][0],
-            "abs_dE_mixed_vs_cpu": abs(cpu["sweep_energies"][0] - mixed["sweep_energies"][0]),
-            "what": "block2's CPU path, one sweep from the same warmed MPS as the timed sweeps"}
-        if fp64 is not None:
+            "cpu_s_per_sweep": cpu["sweep_time"][0], "mixed_s_per_sweep": t_sweep,
+            "cpu_over_mixed": cpu["sweep_time"][0] / t_sweep,
+            "abs_dE_mixed_vs_cpu": abs(cpu["sweep_energies"][0] - first["sweep_energies"][0]),
+            "what": "block2's CPU path on the same step from the same MPS"}
+        if kf > 0:
             res["same_state_cpu"]["abs_dE_fp64_gpu_vs_cpu"] = abs(cpu["sweep_energies"][0]
-                                                                  - fp64["sweep_energies"][0])
+                                                                  - r["arms"][i_fp64]["sweep_energies"][0])
     # the dumped middle-site H_eff (M on both sides), on its own
     if rank == 0 and not args.no_heff:
         hs, prob = heff_section(dump, local_rank, adjoint=args.adjoint or args.workload == "syn16")
@@ -615,16 +625,16 @@ def run_ours(args, rank, local_rank, world, dist):
         res["roofline_fp64"] = hs["roofline_fp64"]
         if world == 1 and not args.no_cpu_baseline:
             rate, nprod, nth, blas = cpu_port_rate(prob)
-            src = fp64 if fp64 is not None else mixed
-            flop_sweep = 2.0 * mean([p["mnk"] for p in src["phases"]])
-            host_part = mean([t - p["teig"] for t, p in zip(src["sweep_time"], src["phases"])])
+            src = r["arms"][i_fp64] if kf > 0 else first
+            flop_sweep = 2.0 * src["phases"][0]["mnk"]
+            host_part = src["sweep_time"][0] - src["phases"][0]["teig"]
             est = flop_sweep / rate + host_part
             res["cpu_baseline"] = {
                 "value": est, "unit": "s/sweep", "cores": nth, "kind": "port",
                 "sample": (f"{nprod} products of the dumped middle-site H_eff by the oracle's restatement of "
                            f"block2's Tasked replay ({'BLAS dgemm' if blas else 'loop'} per pair, {nth} OpenMP "
-                           f"threads): {rate / 1e12:.3f} TFLOP/s; scaled to a sweep as the FP64 sweep's "
-                           f"Davidson FLOP ({flop_sweep:.3e}) at that rate plus the FP64 sweep's host-side time "
+                           f"threads): {rate / 1e12:.3f} TFLOP/s; scaled to the step as the FP64 step's "
+                           f"Davidson FLOP ({flop_sweep:.3e}) at that rate plus its host-side time "
                            f"({host_part:.1f} s, block2's own code in both)"),
                 "cpu_heff_tflops": rate / 1e12, "host": host_info()}
     import shutil
@@ -656,15 +666,20 @@ def run_reference(args):
     import shutil
     shutil.rmtree(wd, ignore_errors=True)
     p = arm["phases"][0]
-    sample = (f"one full sweep at M of block2's CPU DMRG::solve (its OpenMP Tasked GEMM replay, scipy's "
-              f"OpenBLAS, {nth} threads) after two sweeps at M/4 from the seeded random MPS, Davidson "
-              f"{args.dav:g}; a CPU sweep of this workload takes minutes, so one sweep is the sample")
+    sample = (f"one step (the first full sweep at M) of block2's CPU DMRG::solve (its OpenMP Tasked GEMM "
+              f"replay, scipy's OpenBLAS, {nth} threads) after two sweeps at M/4 from the seeded random MPS, "
+              f"Davidson {args.dav:g}; a CPU sweep of this workload takes minutes, so one step is the sample")
     return {
         "metric": METRIC, "value": v, "unit": "s/sweep", "impl": "reference", "n_gpus": 0, "steps": 1,
         "warmup": 0, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic: seeded integrals / Hubbard chain, seeded random initial MPS",
         "config": {"workload": f"{args.workload}: full two-site sweep of block2's DMRG::solve, {spec['desc']}",
-                   "davidson_conv_thrd": args.dav, "host_threads": nth},
+                   "n_sites": r["n_sites"], "bond_dim": spec["M"],
+                   "step": ("the first sweep at M from the MPS two sweeps at M/4 leave; every step starts "
+                            "from its own copy of that MPS"),
+                   "davidson_conv_thrd": args.dav, "noise": 0.0,
+                   "state_preparation": {"M": (spec["M"] // 4,) * 2, "noise": (0.0,) * 2, "dav": (1e-8,) * 2},
+                   "host_threads": nth},
         "cpu_baseline": {"value": v, "unit": "s/sweep", "cores": nth, "kind": "reference", "sample": sample,
                          "host": host_info()},
         "e2e": {"value": v, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -677,15 +692,15 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2, help="timed sweeps (mixed form)")
-    ap.add_argument("--warmup", type=int, default=2, help="warm-up sweeps (rounded up to even, >= 2)")
+    ap.add_argument("--steps", type=int, default=3,
+                    help="timed steps: each the first sweep at M from the prepared MPS, mixed form")
+    ap.add_argument("--warmup", type=int, default=3, help="untimed steps before the timed ones")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="syn24", choices=sorted(WORKLOADS))
-    ap.add_argument("--fp64-sweeps", type=int, default=1, help="sweeps of the plain FP64 form for the ratio")
+    ap.add_argument("--fp64-sweeps", type=int, default=1,
+                    help="the same step in the plain FP64 form, this many times (for the ratio)")
     ap.add_argument("--dav", type=float, default=1e-12, help="Davidson threshold of the timed sweeps")
     ap.add_argument("--threads", type=int, default=0, help="host threads of block2 (default: all)")
-    ap.add_argument("--warm-dav", type=float, default=0.0,
-                    help="Davidson threshold of the warm-up sweeps (default: --dav)")
     ap.add_argument("--partial-end", type=int, default=0,
                     help="compare the forms on one partial forward sweep ending at this site")
     ap.add_argument("--cpu-arm", action="store_true",
@@ -699,8 +714,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
     ap.add_argument("--dump-arm-sweep", type=int, default=-1, metavar="S",
-                    help="measure the middle-site H_eff of the mixed arm's sweep S (default: of the last "
-                         "warm-up sweep); at n=32 M=2000 sweep 1 is the first with M=2000 on both sides")
+                    help="measure the middle-site H_eff of sweep S of the untimed steady arm (default 1, the "
+                         "first with M on both sides)")
     ap.add_argument("--keep-dump", default=None,
                     help="copy the dumped middle-site H_eff to this directory (for --heff-only runs)")
     ap.add_argument("--heff-only", default=None, metavar="DUMP",
