@@ -19,7 +19,6 @@
 // contribution, split-K chunks, and the cover lists of the reduction.
 #include <algorithm>
 #include <array>
-#include <map>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -45,6 +44,21 @@ struct WorkKeyHash {
         h ^= ((uint64_t)(uint32_t)k.k0 << 32 | (uint32_t)k.lda0) * 0x94D049BB133111EBULL;
         h ^= ((uint64_t)(uint32_t)k.ldb0 << 1 | (uint32_t)k.tb0) * 0xD6E8FEB86659FD93ULL;
         return (size_t)(h ^ (h >> 31));
+    }
+};
+
+struct Rect4Hash {
+    size_t operator()(const std::array<int32_t, 4> &k) const {
+        uint64_t h = ((uint64_t)(uint32_t)k[0] << 32 | (uint32_t)k[1]) * 0x9E3779B97F4A7C15ULL;
+        h ^= ((uint64_t)(uint32_t)k[2] << 32 | (uint32_t)k[3]) * 0xBF58476D1CE4E5B9ULL;
+        return (size_t)(h ^ (h >> 31));
+    }
+};
+struct Psi4Hash {
+    size_t operator()(const std::array<int64_t, 4> &k) const {
+        uint64_t h = (uint64_t)k[0] * 0x9E3779B97F4A7C15ULL;
+        h ^= ((uint64_t)k[1] << 40 ^ (uint64_t)k[2] << 20 ^ (uint64_t)k[3]) * 0xBF58476D1CE4E5B9ULL;
+        return (size_t)(h ^ (h >> 29));
     }
 };
 
@@ -246,7 +260,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         // contribution (stage offsets into the A / W images filled in below)
         {
             std::vector<std::array<int32_t, 4>> rkeys;   // rectangles, first-appearance order
-            std::map<std::array<int32_t, 4>, int32_t> rmap;
+            std::unordered_map<std::array<int32_t, 4>, int32_t, Rect4Hash> rmap;
             std::vector<std::vector<int32_t>> rlist;
             for (size_t q = c_begin; q < plan.contribs.size(); q++) {
                 const Contrib &c = plan.contribs[q];
@@ -290,16 +304,22 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             }
             const int32_t t_last = (int32_t)plan.g1tile.size();
             // reduction items: 4 region rows each (enough CTAs to keep the chunk
-            // loads in flight), with the tiles meeting those rows
-            for (int32_t r0 = 0; r0 < rows; r0 += 4) {
+            // loads in flight), with the tiles meeting those rows in tile order
+            // (each tile is added to the items its rows meet)
+            const int32_t nitems = (rows + 3) / 4;
+            std::vector<std::vector<int32_t>> cover((size_t)nitems);
+            for (int32_t t = t_first; t < t_last; t++) {
+                const G1Tile &tt = plan.g1tile[t];
+                const int32_t i0 = std::max(0, tt.row0) / 4;
+                const int32_t i1 = std::min(nitems - 1, (tt.row0 + tt.rows - 1) / 4);
+                for (int32_t i = i0; i <= i1; i++)
+                    cover[(size_t)i].push_back(t);
+            }
+            for (int32_t i = 0; i < nitems; i++) {
                 G1Red it;
-                it.g = g, it.r0 = r0, it.r1 = std::min(rows, r0 + 4);
+                it.g = g, it.r0 = 4 * i, it.r1 = std::min(rows, 4 * i + 4);
                 it.t0 = (int32_t)plan.g1cover.size();
-                for (int32_t t = t_first; t < t_last; t++) {
-                    const G1Tile &tt = plan.g1tile[t];
-                    if (tt.row0 < it.r1 && tt.row0 + tt.rows > it.r0)
-                        plan.g1cover.push_back(t);
-                }
+                plan.g1cover.insert(plan.g1cover.end(), cover[(size_t)i].begin(), cover[(size_t)i].end());
                 it.t1 = (int32_t)plan.g1cover.size(), it.pad = 0;
                 if (it.t1 > it.t0)
                     plan.g1red.push_back(it);
@@ -461,6 +481,10 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
     // heavy tasks first: shortens the tail of the phase-2 grid
     std::stable_sort(plan.t2.begin(), plan.t2.end(),
                      [](const Task2 &a, const Task2 &b) { return a.le - a.lb > b.le - b.lb; });
+    size_t nt1 = 0;
+    for (const WorkDesc &w : plan.works)
+        nt1 += (size_t)w.m0;
+    plan.t1.reserve(nt1);
     for (int32_t u = 0; u < (int32_t)plan.works.size(); u++)
         for (int32_t r = 0; r < plan.works[u].m0; r++)
             plan.t1.push_back(Task1{u, r});
@@ -484,7 +508,12 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             const WorkDesc &a = plan.works[x], &b = plan.works[y];
             return a.b0 == b.b0 && a.tb0 == b.tb0 && a.k0 == b.k0 && a.n0 == b.n0 && a.ldb0 == b.ldb0;
         };
-        std::map<std::array<int64_t, 4>, int32_t> pmap;  // distinct psi sub-blocks
+        std::unordered_map<std::array<int64_t, 4>, int32_t, Psi4Hash> pmap;  // distinct psi sub-blocks
+        pmap.reserve(plan.works.size() + 1);
+        size_t nrows = 0;   // stacked psi rows of all tiles (each product padded to 4)
+        for (const WorkDesc &w : plan.works)
+            nrows += (size_t)((w.m0 + 3) / 4 * 4);
+        plan.g0col.reserve(plan.g0col.size() + nrows);
         for (size_t gs = 0; gs < ord.size();) {
             size_t ge = gs + 1;
             while (ge < ord.size() && same_r(ord[gs], ord[ge]))
@@ -502,7 +531,7 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
             plan.g1aimg.push_back(im);
             // stacked psi rows, each product padded to a multiple of 4; the rows
             // point into the packed copy of their psi sub-block
-            std::vector<G0Col> cols;
+            const size_t col_begin = plan.g0col.size();
             for (size_t q = gs; q < ge; q++) {
                 const int32_t u = ord[q];
                 const WorkDesc &w = plan.works[u];
@@ -522,14 +551,14 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
                     G0Col c;
                     c.psi = i < w.m0 ? ps.dst + (uint64_t)i * ps.k0p : 0;
                     c.w = plan.g1wimg[u].dst, c.k = i, c.live = i < w.m0 ? 1 : 0;
-                    cols.push_back(c);
+                    plan.g0col.push_back(c);
                 }
             }
             const int32_t npad = (w0.n0 + 15) / 16 * 16;
-            for (size_t c0 = 0; c0 < cols.size(); c0 += (size_t)g0w) {
-                const int32_t nc = (int32_t)std::min<size_t>((size_t)g0w, cols.size() - c0);
-                const int64_t cb = (int64_t)plan.g0col.size();
-                plan.g0col.insert(plan.g0col.end(), cols.begin() + c0, cols.begin() + c0 + nc);
+            const size_t ncols = plan.g0col.size() - col_begin;
+            for (size_t c0 = 0; c0 < ncols; c0 += (size_t)g0w) {
+                const int32_t nc = (int32_t)std::min<size_t>((size_t)g0w, ncols - c0);
+                const int64_t cb = (int64_t)(col_begin + c0);
                 for (int32_t rp = 0; rp * 128 < w0.n0; rp++) {
                     G0Tile t;
                     t.rows = std::min(128, w0.n0 - 128 * rp);
