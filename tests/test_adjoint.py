@@ -417,3 +417,22 @@ def test_adjoint_argument_errors(problems, ctx):
     with pytest.raises(ValueError):
         h.adjoint(x, x, torch.zeros(3, dtype=torch.float64, device="cuda"), None)
     h.close()
+
+
+def test_config5_integral_gradients_record():
+    """The n=16 M=500 integral-derivative run (tests/golden/make_grad_syn16.py,
+    the reference's own DMRG and PDMs; its dumps are too large to keep): the
+    recorded summary holds the energy identity and, in all 20 directions, the
+    adjoint chain, the PDM contraction and the central differences agree to 1e-6."""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "syn16_M500_grad.json")) as f:
+        d = json.load(f)
+    assert len(d["rows"]) >= 20
+    assert abs(d["energy_mps"] - d["energy_from_pdms"]) < 1e-10
+    for k in ("adjoint_cpu_vs_pdm", "fd_vs_pdm", "adjoint_cpu_vs_fd"):
+        assert d["max_rel_err"][k] <= d["bound"] == 1e-6, (k, d["max_rel_err"][k])
+    for r in d["rows"]:
+        assert abs(r["adjoint_cpu"] - r["pdm"]) <= 1e-6 * abs(r["pdm"])
