@@ -292,6 +292,9 @@ def heff_section(dump_dir: str, dev_index: int, reps: int = 5, adjoint: bool = F
     ref = sig["fp64"]
     for name in sig:
         out["forms"][name]["rel_err_vs_fp64"] = float(torch.linalg.norm(sig[name] - ref) / torch.linalg.norm(ref))
+    # FP64 sigma on the host (the CPU replay of the reference algorithm is
+    # compared against it at this size)
+    out["_fp64_sigma"] = sig["fp64"].cpu().numpy()
     del sig
     # roofline of the dominant kernel phase of the mixed form
     pk = peaks()
@@ -407,24 +410,28 @@ def adjoint_section(h, prob, ctx, dev, stream, n_dirs: int = 20) -> dict:
             "bound": 1e-6}
 
 
-def cpu_port_rate(prob, budget_s: float = 25.0):
+def cpu_port_rate(prob, psi=None, ref_sigma=None, budget_s: float = 25.0):
     """FLOP/s of the CPU restatement of block2's Tasked replay (oracle port:
     BLAS dgemm per pair, OpenMP over pairs, per-thread sigma copies) on one
-    product of the dumped site, all host threads."""
+    product of the dumped site, all host threads; with ref_sigma, also the
+    relative difference of its sigma (psi given) from ref_sigma."""
     from oracle import oracle
     blas = oracle.load_blas()
     nth = host_threads()
     seq = prob.seq()
+    x = prob.psi if psi is None else psi
     flop = 2.0 * prob.mnk
-    times = []
+    times, rel = [], None
     t_all = time.perf_counter()
     while True:
         t0 = time.perf_counter()
-        oracle.replay(seq, prob.ops, prob.psi, prob.sigma_size, nthreads=nth)
+        sg = oracle.replay(seq, prob.ops, x, prob.sigma_size, nthreads=nth)
         times.append(time.perf_counter() - t0)
+        if rel is None and ref_sigma is not None:
+            rel = float(np.linalg.norm(sg - ref_sigma) / np.linalg.norm(sg))
         if time.perf_counter() - t_all > budget_s or len(times) >= 5:
             break
-    return flop / statistics.median(times), len(times), nth, blas
+    return flop / statistics.median(times), len(times), nth, blas, rel
 
 
 def heff_only(dump_dir: str, form_name: str, products: int, dev_index: int) -> dict:
@@ -620,11 +627,17 @@ def run_ours(args, rank, local_rank, world, dist):
     # the dumped middle-site H_eff (M on both sides), on its own
     if rank == 0 and not args.no_heff:
         hs, prob = heff_section(dump, local_rank, adjoint=args.adjoint or args.workload == "syn16")
+        sigma64 = hs.pop("_fp64_sigma")
         res["heff"] = hs
         res["roofline"] = hs["roofline"]
         res["roofline_fp64"] = hs["roofline_fp64"]
         if world == 1 and not args.no_cpu_baseline:
-            rate, nprod, nth, blas = cpu_port_rate(prob)
+            rate, nprod, nth, blas, rel = cpu_port_rate(prob, np.asarray(prob.extra.get("psi_converged", prob.psi)),
+                                                        sigma64)
+            hs["fp64_vs_cpu_replay_rel"] = rel
+            hs["fp64_vs_cpu_replay_note"] = ("the plain FP64 product on the GPU against the oracle's CPU replay of "
+                                             "block2's Tasked GEMM pairs (pinned to the reference's own sigma on "
+                                             "the golden fixtures) on this full-size site")
             src = r["arms"][i_fp64] if kf > 0 else first
             flop_sweep = 2.0 * src["phases"][0]["mnk"]
             host_part = src["sweep_time"][0] - src["phases"][0]["teig"]
