@@ -44,6 +44,7 @@ struct Opts {
     int dump_site = -1;       // -1: middle site (n/2-1); -2: all sites
     bool with_data = true;    // false: structure only (no operator blob)
     bool dump_dm = true;      // density-matrix / split data after Davidson
+    bool effprob = false;     // also the reference's EffectiveProblem export of the dumped H_eff
     // after the run: the reference's 1-/2-PDM of the final MPS, and for each
     // listed FCIDUMP the H_eff at the final MPS's centre with that Hamiltonian
     // (first site of one sweep on a copy of the final MPS: fixed MPS)
@@ -308,6 +309,20 @@ template <typename S> struct Dumper : CallbackKernel {
         w.scalar("total_memory", (double)h->ket->total_memory);
         w.scalar("su2", is_same<S, SU2>::value ? 1 : 0);
         dump_wfn_cinfo(w, h);
+        if (o.effprob) {
+            // the reference's own export of this H_eff (EffectiveHamiltonian::
+            // save_eff_problem, src/dmrg/effective_hamiltonian.hpp:254-261,
+            // writing the EFFPROB1 format of src/core/effective_problem.hpp),
+            // moved next to the connection infos above; sweeps alternate
+            // direction starting forward
+            const bool fw = d->isweep % 2 == 0;
+            h->save_eff_problem(c, fw);
+            const string src = frame_<double>()->save_dir + "/EFF-PROB." + (fw ? "FORW." : "BACKW.") +
+                               Parsing::to_string(c);
+            if (rename(src.c_str(), (site_dir() + "/qn/effprob.bin").c_str()) != 0)
+                throw runtime_error("harness: cannot move " + src);
+            w.scalar("effprob_isite", c), w.scalar("effprob_forward", fw ? 1 : 0);
+        }
         w.man.flush();
         lc = nullptr;
         lt.deallocate(), rr.deallocate(), ll.deallocate();
@@ -995,6 +1010,7 @@ int main(int argc, char **argv) {
         else if (k == "--dump-site") o.dump_site = atoi(v.c_str());
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
         else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
+        else if (k == "--effprob") o.effprob = atoi(v.c_str()) != 0;
         else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
         else if (k == "--perturb-threads") o.perturb_threads = atoi(v.c_str());
         else if (k == "--perturb") {
