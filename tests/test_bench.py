@@ -63,3 +63,59 @@ def test_bench_site_helpers():
     assert abs(f["rows"][1]["dE"] - 1e-8) < 1e-12 and f["fp64_tdav_sum"] == 4.02
     m = bench.middle_site(sites["ARM0"], 4)
     assert m["site"] == 1 and m["ndav"] == 5 and m["flop_per_s"] == 4.0e12
+
+
+def test_bench_step_bookkeeping(monkeypatch):
+    """run_ours on a stand-in sweep program: the arm list (W untimed steps, K
+    timed steps, the FP64 step, the steady arm, optional arms), which arm's
+    sweep is dumped, and which arms feed `value`, `forms` and the optional
+    sections.  No GPU: torch's device calls and the sweep program are replaced."""
+    import argparse
+
+    import torch
+    sys.path.insert(0, ROOT)
+    import bench
+    import b2g.sweep as sw
+    seen = {}
+
+    def fake_run_sweep(**kw):
+        arms = kw["arms"]
+        seen.update(arms=arms, dump_arm=kw["dump_arm"], dump_sweep=kw["dump_sweep"])
+        out = {"n_sites": 24, "threads": 8, "warm": {"sweep_time": [1.0, 1.0], "sweep_energies": [-1.0, -2.0]},
+               "arms": [], "sites": {}}
+        for i, a in enumerate(arms):
+            n = int(a.split("/")[1].split("@")[0].split("%")[0]) if "/" in a else 1
+            ph = {k: 0.1 for k in ("teff", "teig", "tmve", "tdm", "tsplt", "gpu_davidson", "gpu_translate",
+                                   "gpu_plan_upload", "mnk", "h2d_bytes", "d2h_bytes")}
+            out["arms"].append({"sweep_time": [10.0 + i] * n, "sweep_energies": [-3.0 - 1e-10 * i] * n,
+                                "discarded_weights": [0.0] * n, "phases": [dict(ph) for _ in range(n)],
+                                "gpu": {"kernel_launches": 5}})
+        return out
+
+    monkeypatch.setattr(sw, "run_sweep", fake_run_sweep)
+    monkeypatch.setattr(torch.cuda, "set_device", lambda *a, **k: None)
+    real_tensor = torch.tensor
+    monkeypatch.setattr(torch, "tensor", lambda *a, **k: real_tensor(*a, **{x: y for x, y in k.items()
+                                                                            if x != "device"}))
+    monkeypatch.setattr(bench.ClockSampler, "start", lambda self: None)
+    monkeypatch.setattr(bench.ClockSampler, "stop", lambda self: {"sm_mhz": 1.0})
+    ns = argparse.Namespace(workload="syn24", warmup=2, steps=3, fp64_sweeps=1, dump_arm_sweep=-1, partial_end=0,
+                            tol_study=1e-13, cpu_arm=True, workdir=None, dav=1e-12, threads=0, no_heff=True,
+                            keep_dump=None, adjoint=False, no_cpu_baseline=True)
+    res = bench.run_ours(ns, 0, 0, 1, None)
+    assert seen["arms"] == ("gpu:tf32x3/1",) * 5 + ("gpu:fp64/1", "gpu:tf32x3/2", "gpu:tf32x3/1%1e-13",
+                                                     "gpu:fp64/1%1e-13", "cpu/1")
+    assert (seen["dump_arm"], seen["dump_sweep"]) == (6, 1)      # the steady arm's second sweep
+    assert res["steps"] == 3 and res["warmup"] == 2
+    assert res["value"] == 13.0                                   # arms 2..4: 12, 13, 14 s
+    assert res["sweeps"]["untimed_steps_seconds"] == [10.0, 11.0]
+    assert res["forms"]["fp64_s_per_sweep"] == 15.0 and res["steady_sweep"]["seconds"] == 16.0
+    assert res["tolerance_study"]["tight_seconds"] == {"mixed": 17.0, "fp64": 18.0}
+    assert res["same_state_cpu"]["cpu_s_per_sweep"] == 19.0
+    assert res["gpu_launches"] == 15
+    # the partial-sweep comparison dumps the last site of its mixed partial arm
+    ns.partial_end, ns.tol_study, ns.cpu_arm = 10, 0.0, False
+    res = bench.run_ours(ns, 0, 0, 1, None)
+    assert seen["arms"][-2:] == ("gpu:fp64/1@10", "gpu:tf32x3/1@10")
+    assert (seen["dump_arm"], seen["dump_sweep"]) == (8, 0)
+    assert res["partial"]["fp64_s"] == 17.0 and res["partial"]["mixed_s"] == 18.0
