@@ -24,7 +24,8 @@ def all_ids():
 
 def fixture_ids():
     """Effective-Hamiltonian problems (H_eff*psi and Davidson)."""
-    return [n for n in all_ids() if not n.endswith(("_rot", "_dm", "_blk", "_qn", "_grad", "_fullgrad", "_cinfo"))]
+    return [n for n in all_ids() if not n.endswith(("_rot", "_dm", "_blk", "_qn", "_grad", "_fullgrad", "_cinfo",
+                                                     "_effprob"))]
 
 
 def rotation_ids():
@@ -36,4 +37,5 @@ def rotation_ids():
 def problems():
     from b2g.problem import load_problem
     return {os.path.basename(p)[:-4]: load_problem(p) for p in fixture_paths()
-            if not p.endswith(("_dm.npz", "_blk.npz", "_qn.npz", "_grad.npz", "_fullgrad.npz", "_cinfo.npz"))}
+            if not p.endswith(("_dm.npz", "_blk.npz", "_qn.npz", "_grad.npz", "_fullgrad.npz", "_cinfo.npz",
+                               "_effprob.npz"))}
