@@ -17,8 +17,10 @@
 //
 // Rules for callers:
 //   * the first call on a device looks up the device address of the array
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture is begun on the device;
+//     (cudaGetSymbolAddress) with that device current;
+//   * no call may be captured into a CUDA graph: the descriptors are copied
+//     from one host staging array that the next chunk or call overwrites, so
+//     a replay would run on stale descriptors;
 //   * every call shares the one array and leaves the last chunk's contents in
 //     it; calls whose work overlaps on the GPU (different streams, or
 //     different host threads on one device) race on it -- serialize them;

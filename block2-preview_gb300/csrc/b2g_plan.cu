@@ -69,6 +69,9 @@ inline uint64_t extent(bool trans, int64_t rows, int64_t cols, int64_t ld) {
     return trans ? (uint64_t)((cols - 1) * ld + rows) : (uint64_t)((rows - 1) * ld + cols);
 }
 
+// off + ext <= size, in a form no caller-supplied offset can make wrap around
+inline bool fits(uint64_t off, uint64_t ext, uint64_t size) { return ext <= size && off <= size - ext; }
+
 } // namespace
 
 static constexpr int kRowsPerTask = 4;    // warps per phase-2 CTA, one row each
@@ -104,13 +107,13 @@ int build_plan(const b2g_pair_seq *s, uint64_t ops_size, uint64_t psi_size, uint
         if (s->lda0[i] < k0 || s->ldc1[i] < n1 || s->ldb0[i] < (s->tb0[i] ? k0 : n0) ||
             s->lda1[i] < (s->ta1[i] ? m1 : k1))
             return fail(B2G_ERR_ARG, "pair " + std::to_string(i) + ": leading dimension too small");
-        if (s->a0[i] + extent(false, m0, k0, s->lda0[i]) > psi_size)
+        if (!fits(s->a0[i], extent(false, m0, k0, s->lda0[i]), psi_size))
             return fail(B2G_ERR_ARG, "pair " + std::to_string(i) + ": psi operand out of range");
-        if (s->b0[i] + extent(s->tb0[i], k0, n0, s->ldb0[i]) > ops_size)
+        if (!fits(s->b0[i], extent(s->tb0[i], k0, n0, s->ldb0[i]), ops_size))
             return fail(B2G_ERR_ARG, "pair " + std::to_string(i) + ": GEMM0 operator out of range");
-        if (s->a1[i] + extent(s->ta1[i], m1, k1, s->lda1[i]) > ops_size)
+        if (!fits(s->a1[i], extent(s->ta1[i], m1, k1, s->lda1[i]), ops_size))
             return fail(B2G_ERR_ARG, "pair " + std::to_string(i) + ": GEMM1 operator out of range");
-        if (s->c1[i] + extent(false, m1, n1, s->ldc1[i]) > sigma_size)
+        if (!fits(s->c1[i], extent(false, m1, n1, s->ldc1[i]), sigma_size))
             return fail(B2G_ERR_ARG, "pair " + std::to_string(i) + ": sigma operand out of range");
         live[i] = 1;
         plan.mnk += (double)m0 * n0 * k0 + (double)m1 * n1 * k1;

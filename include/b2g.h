@@ -226,9 +226,11 @@ int b2g_block_contract_device(b2g_context *ctx, const b2g_block_seq *seq, const 
  * (host arrays), and DEVICE pointers to the operator blob, psi and sigma;
  * the work matrices live in a 32 MiB file-scope device array that every GPU
  * loading this library holds until exit.  A pair whose work matrix exceeds
- * that array is rejected (B2G_ERR_ARG).  The first call on a device looks
- * the array's address up and should precede any stream capture on that
- * device; calls share the array, so calls that overlap on the GPU race.
+ * that array is rejected (B2G_ERR_ARG).  Calls share the array, so calls
+ * that overlap on the GPU race.  The call must not be captured into a CUDA
+ * graph: each chunk's pair descriptors are copied from one host array owned
+ * by the library, which the next chunk or call overwrites, so a replay would
+ * run on stale descriptors.
  * sigma is accumulated with FP64 atomics, so unlike the other FP64 entry
  * points the result is not bit-reproducible from call to call (it differs
  * in the last bits).  The pair descriptors reach the device through an

@@ -80,3 +80,31 @@ def test_context_without_gpu_fails_loudly():
         pytest.skip("GPU present")
     with pytest.raises(b2g.B2GError):
         b2g.Context(0)
+
+
+def test_plan_rejects_offsets_that_wrap(problems):
+    """An offset near 2^64 must not wrap the range check round to a small sum."""
+    p = problems[sorted(problems)[0]]
+    for field in ("a0", "b0", "a1", "c1"):
+        with pytest.raises(b2g.B2GError) as e:
+            b2g.plan_stats(_mutated(p, field, np.uint64(2**64 - 1)), p.ops.size, p.psi_size, p.sigma_size)
+        assert e.value.code == capi.B2G_ERR_ARG, field
+
+
+def test_noalloc_validates_before_touching_the_device(problems):
+    """b2g_heff_apply_noalloc checks every pair on the host before any CUDA
+    call, so out-of-range and wrapping offsets are refused here without a GPU
+    (the pointers are never dereferenced)."""
+    import ctypes as C
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("host-only check; the GPU suite covers the device path")
+    p = problems[sorted(problems)[0]]
+    fake = C.c_void_p(16)
+    for field, value in (("a0", p.psi_size), ("c1", p.sigma_size), ("b0", np.uint64(2**64 - 8)),
+                         ("a1", np.uint64(2**64 - 1))):
+        seq = _mutated(p, field, value)
+        rc = capi.lib().b2g_heff_apply_noalloc(C.byref(seq.c), fake, p.ops.size, fake, p.psi_size,
+                                               fake, p.sigma_size, 1.0, None)
+        assert rc == capi.B2G_ERR_ARG, field
+        assert b"out of range" in capi.lib().b2g_last_error()
