@@ -78,6 +78,22 @@ class TuneResultC(C.Structure):
                 "g1_wide_frac": self.g1_wide_frac, "g0_wide_frac": self.g0_wide_frac}
 
 
+class GemmListC(C.Structure):
+    """b2g_gemm_list: the single GEMMs of a perturbative-noise product."""
+
+    _fields_ = [("n_gemms", C.c_int64)] + [(k, _i32p) for k in ("ta", "tb", "m", "n", "k", "lda", "ldb", "ldc",
+                                                               "a_kind", "b_kind")] + \
+               [("alpha", _f64p), ("beta", _f64p), ("a", _u64p), ("b", _u64p), ("c", _u64p)]
+
+
+class PairArraysC(C.Structure):
+    """b2g_pair_arrays: writable pair arrays (the fields of b2g_pair_seq)."""
+
+    _fields_ = [(k, _i32p) for k in ("tb0", "m0", "n0", "k0", "lda0", "ldb0", "ta1", "m1", "n1", "k1",
+                                     "lda1", "ldc1")] + \
+               [("alpha0", _f64p), ("alpha1", _f64p), ("a0", _u64p), ("b0", _u64p), ("a1", _u64p), ("c1", _u64p)]
+
+
 class DmLayoutC(C.Structure):
     _fields_ = [
         ("trace_right", C.c_int32), ("n_psi_blocks", C.c_int32), ("psi_dm", C.c_void_p),
@@ -161,6 +177,9 @@ SIGNATURES = {
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "b2g_noise_pairs": (C.c_int, [C.POINTER(GemmListC), C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PairArraysC),
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "b2g_dm_truncate": (C.c_int, [C.c_void_p, C.POINTER(DmLayoutC), C.c_void_p, C.c_int, C.c_double,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.POINTER(DmResultC)]),

@@ -483,6 +483,61 @@ int b2g_wfn_connection(int sym, uint64_t cdq, uint64_t vdq, uint64_t opdq, int32
                        double *factor, uint32_t *ia, uint32_t *ib, uint32_t *ic, int64_t cap,
                        int64_t *nc);
 
+/*
+ * Perturbative noise (EffectiveHamiltonian::perturbative_noise,
+ * src/dmrg/effective_hamiltonian.hpp:262-433, called from
+ * DMRG::two_dot_eigs_and_perturb, src/dmrg/sweep_algorithm.hpp:1257-1260).
+ * In Tasked mode block2 records that product as single GEMMs in
+ * BatchGEMMSeq::batch[1] (BatchGEMMSeq::multiply, three_rotate_tr_left/right,
+ * src/core/batch_gemm.hpp:887-891, 1025-1107; the per-row form of
+ * AdvancedGEMM::multiply, batch_gemm.hpp:584-607), each, row-major,
+ *
+ *   group[c:](m x n, ld ldc) += alpha * op_a(A)(m x k) * op_b(B)(k x n)
+ *
+ * (beta = 1), one operand a block of the ket (kind B2G_NOISE_KET, offset into
+ * the ket), the other an operator block (B2G_NOISE_OP, offset into the
+ * operator blob), c an offset into the perturbed-wavefunction group.
+ */
+#define B2G_NOISE_KET 0
+#define B2G_NOISE_OP 1
+typedef struct {
+    int64_t n_gemms;
+    const int32_t *ta, *tb, *m, *n, *k, *lda, *ldb, *ldc;
+    const int32_t *a_kind, *b_kind;
+    const double *alpha, *beta;
+    const uint64_t *a, *b, *c;
+} b2g_gemm_list;
+/* Writable pair arrays (the fields of b2g_pair_seq), capacity n_gemms each. */
+typedef struct {
+    int32_t *tb0, *m0, *n0, *k0, *lda0, *ldb0;
+    int32_t *ta1, *m1, *n1, *k1, *lda1, *ldc1;
+    double *alpha0, *alpha1;
+    uint64_t *a0, *b0, *a1, *c1;
+} b2g_pair_arrays;
+/*
+ * Rewrites a noise GEMM list as the GEMM pairs of b2g_pair_seq over
+ * psi = the ket, sigma = the group, and the operator blob followed by an
+ * identity block, so that b2g_heff_create / b2g_heff_apply run it.  No
+ * reference counterpart (block2 replays the list with its batched BLAS):
+ *   ket on the left:   W = ket_blk op_b(B),  c += alpha I W
+ *   ket on the right:  W = ket_blk I,        c += alpha op_a(A) W
+ * (products with the identity are exact in FP64).  A transposed ket operand is
+ * accepted where it is one contiguous row; a GEMM whose transposed ket row is
+ * its B operand (output one contiguous column) is transposed as a whole.
+ * The caller appends the row-major identity block (*id_dim x *id_dim) at
+ * offset ops_size of the blob.  Group layout: n_blocks row-major blocks in
+ * ascending order, block i at blk_off[i] with blk_rows[i] x blk_cols[i]
+ * elements; a one-row output takes its block's leading dimension.  GEMMs with
+ * a zero dimension or alpha = 0 are dropped.  Outputs: *n_pairs pairs in out,
+ * *id_dim.  B2G_ERR_ARG: an operand out of range, beta != 1, not exactly one
+ * ket operand; B2G_ERR_UNSUPPORTED: a transposed ket operand that is not one
+ * row, an output that leaves its group block.  Host only.
+ */
+int b2g_noise_pairs(const b2g_gemm_list *g, uint64_t ket_size, uint64_t ops_size,
+                    uint64_t group_size, int64_t n_blocks, const uint64_t *blk_off,
+                    const int32_t *blk_rows, const int32_t *blk_cols, b2g_pair_arrays *out,
+                    int64_t *n_pairs, int32_t *id_dim);
+
 #ifdef __cplusplus
 }
 #endif

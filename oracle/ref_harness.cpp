@@ -24,6 +24,7 @@
 #include "block2_core.hpp"
 #include "block2_dmrg.hpp"
 #include <sys/stat.h>
+#include <functional>
 #include <mutex>
 
 using namespace block2;
@@ -45,6 +46,7 @@ struct Opts {
     bool with_data = true;    // false: structure only (no operator blob)
     bool dump_dm = true;      // density-matrix / split data after Davidson
     bool effprob = false;     // also the reference's EffectiveProblem export of the dumped H_eff
+    bool noise = false;       // also the perturbative-noise product of the dumped site's converged ket
     // after the run: the reference's 1-/2-PDM of the final MPS, and for each
     // listed FCIDUMP the H_eff at the final MPS's centre with that Hamiltonian
     // (first site of one sweep on a copy of the final MPS: fixed MPS)
@@ -92,6 +94,81 @@ struct Region {
     size_t blob_off = 0;
     bool used = false;
 };
+
+// Perturbative-noise recorder.  In Tasked mode
+// EffectiveHamiltonian::perturbative_noise (src/dmrg/effective_hamiltonian.hpp:262-433)
+// records single GEMMs c += alpha op(a) op(b) into BatchGEMMSeq::batch[1]
+// (BatchGEMMSeq::multiply, three_rotate_tr_left/right, src/core/batch_gemm.hpp:887-891,
+// 1025-1107, and AdvancedGEMM::multiply's per-row form, batch_gemm.hpp:584-607),
+// one operand a ket block, the other an operator block, c a block of the
+// perturbed-wavefunction group.  Each OperatorFunctions call that adds GEMMs is
+// followed here by reading the new entries; operand matrices that the
+// H_eff's operator tensors do not hold (built on the fly from a delayed
+// expression and freed after recording) are copied while they are alive.
+struct NoiseRecorder {
+    struct Gemm {
+        bool ta, tb;
+        int m, n, k, lda, ldb, ldc;
+        double alpha, beta;
+        const double *a, *b;
+        double *c;
+        int a_held = -1, b_held = -1;  // index into held (else: H_eff operator or ket)
+        size_t a_off = 0, b_off = 0;   // offset within the held copy
+    };
+    std::mutex mu;
+    const double *ket = nullptr;
+    size_t nket = 0;
+    std::function<bool(const double *, size_t)> known;  // inside an H_eff operator
+    // batch[1] groups / entries already read.  With more than one thread,
+    // TensorFunctions::parallel_for records into per-thread copies of the
+    // sequence and merges them (src/core/tensor_functions.hpp:68-130), so the
+    // recorder requires one sequence: run it with --threads 1.
+    const BatchGEMM<double> *src = nullptr;
+    size_t g_done = 0, p_done = 0;
+    vector<Gemm> gemms;
+    vector<vector<double>> held;
+    static bool trans(CBLAS_TRANSPOSE t) { return t == CblasTrans || t == CblasConjTrans; }
+    static size_t extent(bool t, int rows, int cols, int ld) {
+        if (rows == 0 || cols == 0)
+            return 0;
+        return t ? (size_t)(cols - 1) * ld + rows : (size_t)(rows - 1) * ld + cols;
+    }
+    void take(const BatchGEMM<double> &bt, const vector<pair<const double *, size_t>> &mats) {
+        lock_guard<std::mutex> lk(mu);
+        map<const double *, int> copied;  // operand matrix -> held index (this call)
+        auto place = [&](const double *p, size_t ext, int &hi, size_t &off) {
+            if ((p >= ket && p + ext <= ket + nket) || known(p, ext))
+                return;
+            for (auto &mm : mats)
+                if (p >= mm.first && p + ext <= mm.first + mm.second) {
+                    auto it = copied.find(mm.first);
+                    if (it == copied.end()) {
+                        held.emplace_back(mm.first, mm.first + mm.second);
+                        it = copied.emplace(mm.first, (int)held.size() - 1).first;
+                    }
+                    hi = it->second, off = (size_t)(p - mm.first);
+                    return;
+                }
+            throw runtime_error("noise recorder: operand outside the ket, the operators and the call's matrices");
+        };
+        if (src != nullptr && src != &bt)
+            throw runtime_error("noise recorder: GEMMs recorded into two sequences (use --threads 1)");
+        src = &bt;
+        for (; g_done < bt.gp.size(); g_done++)
+            for (MKL_INT q = 0; q < bt.gp[g_done]; q++, p_done++) {
+                Gemm g;
+                g.ta = trans(bt.ta[g_done]), g.tb = trans(bt.tb[g_done]);
+                g.m = bt.m[g_done], g.n = bt.n[g_done], g.k = bt.k[g_done];
+                g.lda = bt.lda[g_done], g.ldb = bt.ldb[g_done], g.ldc = bt.ldc[g_done];
+                g.alpha = bt.alpha[g_done], g.beta = bt.beta[g_done];
+                g.a = bt.a[p_done], g.b = bt.b[p_done], g.c = bt.c[p_done];
+                place(g.a, extent(g.ta, g.m, g.k, g.lda), g.a_held, g.a_off);
+                place(g.b, extent(g.tb, g.k, g.n, g.ldb), g.b_held, g.b_off);
+                gemms.push_back(g);
+            }
+    }
+};
+static NoiseRecorder *g_noise = nullptr;  // set while a perturbative-noise product is recorded
 
 template <typename S> struct Dumper : CallbackKernel {
     typedef DMRG<S, double, double> DMRGT;
@@ -397,6 +474,100 @@ template <typename S> struct Dumper : CallbackKernel {
         w.man.flush();
         dump_truncation(h);
     }
+    // The perturbative-noise product of the converged ket, requested the way
+    // DMRG::two_dot_eigs_and_perturb does (src/dmrg/sweep_algorithm.hpp:1257-1260) with
+    // NoiseTypes::ReducedPerturbative.  Written: the recorded GEMMs
+    // (c += alpha op(a) op(b); g_akind/g_bkind 0 = ket, 1 = operator blob; g_c an
+    // offset into the perturbed group), the operator blob they read, the ket
+    // ("psi"), the reference's perturbed-wavefunction group ("sigma") and the
+    // group's block layout.
+    void dump_noise(const shared_ptr<EffectiveHamiltonian<S, double>> &h) const {
+        const bool forward = d->isweep % 2 == 0;  // solve() starts forward and alternates
+        const int isite = d->me->center;
+        collect_regions(h);
+        auto seq = h->tf->opf->seq;
+        if (!seq->batch[0]->c.empty() || !seq->batch[1]->c.empty())
+            throw runtime_error("harness: GEMM sequence not empty before the noise product");
+        NoiseRecorder R;
+        R.ket = h->ket->data, R.nket = h->ket->total_memory;
+        R.known = [this](const double *p, size_t ext) { return find_region(p, ext) >= 0; };
+        g_noise = &R;
+        auto pket = h->perturbative_noise(forward, isite, isite + 1, FuseTypes::FuseLR,
+                                          d->me->ket->info, NoiseTypes::ReducedPerturbative);
+        g_noise = nullptr;
+        const double *vbase = pket->data;
+        const size_t nsig = pket->total_memory;
+        // blob: the H_eff operator regions the GEMMs read, then the held copies
+        for (auto &r : regions)
+            r.used = false;
+        auto in_ket = [&](const double *p, int held) { return held < 0 && p >= R.ket && p < R.ket + R.nket; };
+        for (auto &g : R.gemms)
+            for (auto pr : {make_pair(g.a, g.a_held), make_pair(g.b, g.b_held)})
+                if (pr.second < 0 && !in_ket(pr.first, pr.second))
+                    regions[find_region(pr.first, 1)].used = true;
+        size_t blob = 0;
+        for (auto &r : regions)
+            if (r.used)
+                r.blob_off = blob, blob += r.n;
+        vector<size_t> held_off(R.held.size());
+        for (size_t q = 0; q < R.held.size(); q++)
+            held_off[q] = blob, blob += R.held[q].size();
+        vector<double> ops(blob);
+        for (auto &r : regions)
+            if (r.used)
+                memcpy(ops.data() + r.blob_off, r.p, sizeof(double) * r.n);
+        for (size_t q = 0; q < R.held.size(); q++)
+            memcpy(ops.data() + held_off[q], R.held[q].data(), sizeof(double) * R.held[q].size());
+        const size_t ng = R.gemms.size();
+        vector<int32_t> ta(ng), tb(ng), m(ng), n(ng), k(ng), lda(ng), ldb(ng), ldc(ng), ak(ng), bk(ng);
+        vector<double> al(ng), be(ng);
+        vector<uint64_t> ga(ng), gb(ng), gc(ng);
+        auto where = [&](const double *p, int held, size_t hoff, int32_t &kind) -> uint64_t {
+            if (in_ket(p, held))
+                return kind = 0, (uint64_t)(p - R.ket);
+            kind = 1;
+            if (held >= 0)
+                return held_off[held] + hoff;
+            const long ri = find_region(p, 1);
+            return regions[ri].blob_off + (size_t)(p - regions[ri].p);
+        };
+        for (size_t q = 0; q < ng; q++) {
+            const auto &g = R.gemms[q];
+            if (g.c < vbase || g.c >= vbase + nsig)
+                throw runtime_error("harness: noise GEMM output outside the perturbed group");
+            ta[q] = g.ta, tb[q] = g.tb, m[q] = g.m, n[q] = g.n, k[q] = g.k;
+            lda[q] = g.lda, ldb[q] = g.ldb, ldc[q] = g.ldc, al[q] = g.alpha, be[q] = g.beta;
+            ga[q] = where(g.a, g.a_held, g.a_off, ak[q]);
+            gb[q] = where(g.b, g.b_held, g.b_off, bk[q]);
+            gc[q] = (uint64_t)(g.c - vbase);
+        }
+        vector<double> psi(R.ket, R.ket + R.nket), sigma(vbase, vbase + nsig);
+        vector<int32_t> vrows, vcols, vidx;
+        vector<uint64_t> vq, voff;
+        for (int j = 0; j < pket->n; j++) {
+            const auto &info = pket->infos[j];
+            vq.push_back(info->delta_quantum.data);
+            for (int b = 0; b < info->n; b++) {
+                vrows.push_back(info->n_states_bra[b]), vcols.push_back(info->n_states_ket[b]);
+                voff.push_back(pket->offsets[j] + info->block_shifts[b]), vidx.push_back(j);
+            }
+        }
+        Writer w(site_dir() + "/noise");
+        w.scalar("n_gemms", (double)ng), w.scalar("n_held", (double)R.held.size());
+        w.scalar("forward", forward), w.scalar("n_vectors", pket->n);
+        w.scalar("psi_size", (double)R.nket), w.scalar("sigma_size", (double)nsig);
+        w.scalar("ops_size", (double)blob);
+        w.vec("g_ta", ta, "i4"), w.vec("g_tb", tb, "i4"), w.vec("g_m", m, "i4"), w.vec("g_n", n, "i4");
+        w.vec("g_k", k, "i4"), w.vec("g_lda", lda, "i4"), w.vec("g_ldb", ldb, "i4"), w.vec("g_ldc", ldc, "i4");
+        w.vec("g_akind", ak, "i4"), w.vec("g_bkind", bk, "i4"), w.vec("g_alpha", al, "f8");
+        w.vec("g_beta", be, "f8"), w.vec("g_a", ga, "u8"), w.vec("g_b", gb, "u8"), w.vec("g_c", gc, "u8");
+        w.vec("psi", psi, "f8"), w.vec("ops", ops, "f8"), w.vec("sigma", sigma, "f8");
+        w.vec("vec_q", vq, "u8"), w.vec("blk_rows", vrows, "i4"), w.vec("blk_cols", vcols, "i4");
+        w.vec("blk_off", voff, "u8"), w.vec("blk_vec", vidx, "i4");
+        w.man.flush();
+        pket->deallocate();
+        pket->deallocate_infos();
+    }
     // Density matrix of the converged psi, its spectrum, and the reference's
     // truncation/split (MovingEnvironment::density_matrix / split_density_matrix,
     // src/dmrg/moving_environment.hpp:3554-3580, 4250-4345) on copies.
@@ -484,6 +655,8 @@ template <typename S> struct Dumper : CallbackKernel {
         }
         else if (name == "DMRG::sweep::iter.eff_ham.end") {
             dump_post(d->current_eff_ham);
+            if (o.noise)
+                dump_noise(d->current_eff_ham);
             want_rotation = true;
             want_blocking = true;
             rot_dir = site_dir() + "/rotation";
@@ -633,6 +806,28 @@ template <typename S> struct RecordingOpf : OperatorFunctions<S, double> {
             }
         }
         OPF::tensor_product(conj, a, b, c, scale);
+    }
+    // the GEMMs of a perturbative-noise product, read right after each call adds them
+    void tensor_product_multiply(uint8_t conj, const shared_ptr<SparseMatrix<S, double>> &a,
+                                 const shared_ptr<SparseMatrix<S, double>> &b,
+                                 const shared_ptr<SparseMatrix<S, double>> &c,
+                                 const shared_ptr<SparseMatrix<S, double>> &v, S opdq,
+                                 double scale = 1.0, TraceTypes tt = TraceTypes::None) const override {
+        OPF::tensor_product_multiply(conj, a, b, c, v, opdq, scale, tt);
+        if (g_noise != nullptr)
+            g_noise->take(*this->seq->batch[1], {{a->data, a->total_memory}, {b->data, b->total_memory}});
+    }
+    void three_tensor_product_multiply(uint8_t conj, const shared_ptr<SparseMatrix<S, double>> &a,
+                                       const shared_ptr<SparseMatrix<S, double>> &b,
+                                       const shared_ptr<SparseMatrix<S, double>> &c,
+                                       const shared_ptr<SparseMatrix<S, double>> &v, uint8_t dconj,
+                                       const shared_ptr<SparseMatrix<S, double>> &da,
+                                       const shared_ptr<SparseMatrix<S, double>> &db, bool dleft, S opdq,
+                                       double scale = 1.0, TraceTypes tt = TraceTypes::None) const override {
+        OPF::three_tensor_product_multiply(conj, a, b, c, v, dconj, da, db, dleft, opdq, scale, tt);
+        if (g_noise != nullptr)
+            g_noise->take(*this->seq->batch[1], {{a->data, a->total_memory}, {b->data, b->total_memory},
+                                                 {da->data, da->total_memory}, {db->data, db->total_memory}});
     }
 };
 
@@ -1011,6 +1206,7 @@ int main(int argc, char **argv) {
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
         else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
         else if (k == "--effprob") o.effprob = atoi(v.c_str()) != 0;
+        else if (k == "--noise-product") o.noise = atoi(v.c_str()) != 0;
         else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
         else if (k == "--perturb-threads") o.perturb_threads = atoi(v.c_str());
         else if (k == "--perturb") {
