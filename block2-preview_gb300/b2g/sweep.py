@@ -65,13 +65,15 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
               seed: int = 1234, start_site: int = 0, end_site: int = -1, workdir: str | None = None,
               timeout: float | None = None, env: dict | None = None, dump_heff: str | None = None,
               dump_arm: int = 0, dump_sweep: int = -1, dump_site: int = -1, nroots: int = 1,
-              stack_gb: float = 4.0) -> dict:
+              stack_gb: float = 4.0, noise_type: str = "dm", noise_on_device: bool = True) -> dict:
     """Runs one dmrg_sweep invocation and returns its JSON report with
     ``sites`` (parse_sites of its output), ``stdout`` and ``cmd``.  With
     dump_heff, GPU arm ``dump_arm`` writes the H_eff of ``dump_site`` (default:
     the middle site) in its sweep ``dump_sweep`` to that directory
     (b2g.problem.load_dump reads it).  stack_gb sizes block2's DataFrame stack
-    (4 GB is enough up to M = 1000; n = 32 M = 2000 needs more)."""
+    (4 GB is enough up to M = 1000; n = 32 M = 2000 needs more).  noise_type "dm"
+    is block2's NoiseTypes::DensityMatrix, "perturbative" its ReducedPerturbative
+    (GPU arms run that product on the device unless noise_on_device is false)."""
     if not os.path.exists(binary):
         raise FileNotFoundError(f"{binary} is not built (build() needs block2's headers)")
     lst = lambda v: ",".join(str(x) for x in v)  # noqa: E731
@@ -85,7 +87,8 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
            "--arms", ",".join(arms), "--threads", str(threads), "--seed", str(seed),
            "--iprint", "2", "--json", js, "--scratch", os.path.join(wd, "scratch"),
            "--start-site", str(start_site), "--end-site", str(end_site), "--nroots", str(nroots),
-           "--stack-gb", str(stack_gb)]
+           "--stack-gb", str(stack_gb), "--noise-type", noise_type,
+           "--noise-on-device", "1" if noise_on_device else "0"]
     if dump_heff:
         cmd += ["--dump-heff", os.path.abspath(dump_heff), "--dump-arm", str(dump_arm),
                 "--dump-sweep", str(dump_sweep), "--dump-site", str(dump_site)]

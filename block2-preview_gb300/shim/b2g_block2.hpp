@@ -30,6 +30,7 @@
 #include "b2g.h"
 
 #include <algorithm>
+#include <atomic>
 #include <fstream>
 #include <memory>
 #include <stdexcept>
@@ -53,6 +54,11 @@ struct Runtime {
     double t_plan = 0, t_upload = 0;
     double t_davidson = 0;      // wall time inside b2g_davidson (device-resident solves)
     double h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic of the drop-in
+    // perturbative noise (EffectiveHamiltonian::perturbative_noise) on the device;
+    // off: block2 replays its recorded GEMM list on the host
+    bool noise_on_device = false;
+    long long n_noise = 0;
+    std::atomic<int> noise_depth{0};  // nesting of tensor_product_partial_multiply
     explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
         check(b2g_context_create(device, &ctx), "b2g_context_create");
     }
@@ -292,6 +298,153 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
         rt->n_apply_fp64++;
         rt->h2d_bytes += 8.0 * (double)b.size(), rt->d2h_bytes += 8.0 * (double)c.size();
         sq.cumulative_nflop += (size_t)plan->mnk;
+    }
+    // EffectiveHamiltonian::perturbative_noise (src/dmrg/effective_hamiltonian.hpp:262-433)
+    // calls this once per noise product; block2's own version records single GEMMs
+    // (Tasked mode, batch[1]) that perturbative_noise then replays with
+    // BatchGEMMSeq::auto_perform.  With Runtime::noise_on_device the outermost call
+    // runs the recorded list on the GPU as H_eff pairs (b2g_noise_pairs) and
+    // empties batch[1], so auto_perform adds nothing.  Nested calls (the Sum
+    // branch, and the per-thread copies TensorFunctions::parallel_for uses,
+    // src/core/tensor_functions.hpp:68-130) only record: their lists are merged
+    // into this sequence before the outermost call returns.
+    void tensor_product_partial_multiply(
+        const std::shared_ptr<block2::OpExpr<S>> &expr, const std::shared_ptr<block2::OpExpr<S>> &xexpr,
+        const std::shared_ptr<block2::OperatorTensor<S, double>> &lopt,
+        const std::shared_ptr<block2::OperatorTensor<S, double>> &ropt, bool trace_right,
+        const std::shared_ptr<block2::SparseMatrix<S, double>> &cmat,
+        const std::vector<std::pair<uint8_t, S>> &psubsl,
+        const std::vector<std::vector<std::shared_ptr<typename block2::SparseMatrixInfo<S>::ConnectionInfo>>>
+            &cinfos,
+        const std::vector<S> &vdqs, const std::shared_ptr<block2::SparseMatrixGroup<S, double>> &vmats,
+        int &vidx, int tvidx, bool do_reduce) const override {
+        const bool outer = rt->noise_depth.fetch_add(1) == 0;
+        try {
+            TF::tensor_product_partial_multiply(expr, xexpr, lopt, ropt, trace_right, cmat, psubsl, cinfos, vdqs,
+                                                vmats, vidx, tvidx, do_reduce);
+        } catch (...) {
+            rt->noise_depth--;
+            throw;
+        }
+        rt->noise_depth--;
+        if (outer && rt->noise_on_device)
+            noise_on_device(cmat, vmats);
+    }
+    // the recorded noise GEMMs: ket operands -> offsets into the ket, operator
+    // operands -> a packed blob of their merged extents, outputs -> offsets into
+    // the group; then pairs, one device product, and the list is cleared
+    void noise_on_device(const std::shared_ptr<block2::SparseMatrix<S, double>> &ket,
+                         const std::shared_ptr<block2::SparseMatrixGroup<S, double>> &grp) const {
+        auto &sq = *this->opf->seq;
+        auto &g1 = *sq.batch[1];
+        if (!sq.batch[0]->c.empty())
+            throw std::runtime_error("b2g: GEMM pairs recorded next to the noise product");
+        const double *kb = ket->data, *vb = grp->data;
+        const uint64_t nk = ket->total_memory, nv = grp->total_memory;
+        auto trans = [](block2::CBLAS_TRANSPOSE t) { return t == block2::CblasTrans || t == block2::CblasConjTrans; };
+        std::vector<int32_t> ta, tb, m, n, k, lda, ldb, ldc, ak, bk;
+        std::vector<double> al, be;
+        std::vector<uint64_t> ga, gb, gc;
+        std::vector<RecordedPairs::Span> spans;
+        size_t p = 0;
+        for (size_t gi = 0; gi < g1.gp.size(); gi++)
+            for (int q = 0; q < (int)g1.gp[gi]; q++, p++) {
+                ta.push_back(trans(g1.ta[gi])), tb.push_back(trans(g1.tb[gi]));
+                m.push_back(g1.m[gi]), n.push_back(g1.n[gi]), k.push_back(g1.k[gi]);
+                lda.push_back(g1.lda[gi]), ldb.push_back(g1.ldb[gi]), ldc.push_back(g1.ldc[gi]);
+                al.push_back(g1.alpha[gi]), be.push_back(g1.beta[gi]);
+                if (g1.c[p] < vb || g1.c[p] >= vb + nv)
+                    throw std::runtime_error("b2g: a noise GEMM writes outside the perturbed group");
+                gc.push_back((uint64_t)(g1.c[p] - vb));
+                for (int side = 0; side < 2; side++) {
+                    const double *x = side == 0 ? g1.a[p] : g1.b[p];
+                    const bool is_ket = x >= kb && x < kb + nk;
+                    (side == 0 ? ak : bk).push_back(is_ket ? B2G_NOISE_KET : B2G_NOISE_OP);
+                    (side == 0 ? ga : gb).push_back(is_ket ? (uint64_t)(x - kb) : 0);
+                    if (!is_ket)
+                        spans.push_back(RecordedPairs::Span{
+                            x, side == 0 ? RecordedPairs::extent(ta.back(), m.back(), k.back(), lda.back())
+                                         : RecordedPairs::extent(tb.back(), k.back(), n.back(), ldb.back())});
+                }
+            }
+        const size_t ng = ta.size();
+        // operator blob: the operands' extents merged in address order
+        std::vector<RecordedPairs::Span> merged(spans);
+        std::sort(merged.begin(), merged.end(),
+                  [](const RecordedPairs::Span &x, const RecordedPairs::Span &y) { return x.p < y.p; });
+        std::vector<RecordedPairs::Span> reg;
+        for (auto &s : merged)
+            if (!reg.empty() && s.p <= reg.back().p + reg.back().n)
+                reg.back().n = (uint64_t)(std::max(reg.back().p + reg.back().n, s.p + s.n) - reg.back().p);
+            else
+                reg.push_back(s);
+        std::vector<uint64_t> roff(reg.size());
+        uint64_t nops = 0;
+        for (size_t r = 0; r < reg.size(); r++)
+            roff[r] = nops, nops += reg[r].n;
+        auto locate = [&](const double *x) {
+            auto it = std::upper_bound(reg.begin(), reg.end(), x,
+                                       [](const double *y, const RecordedPairs::Span &s) { return y < s.p; });
+            const size_t r = (size_t)(it - reg.begin()) - 1;
+            return roff[r] + (uint64_t)(x - reg[r].p);
+        };
+        p = 0;
+        for (size_t gi = 0, i = 0; gi < g1.gp.size(); gi++)
+            for (int q = 0; q < (int)g1.gp[gi]; q++, p++, i++) {
+                if (ak[i] == B2G_NOISE_OP)
+                    ga[i] = locate(g1.a[p]);
+                if (bk[i] == B2G_NOISE_OP)
+                    gb[i] = locate(g1.b[p]);
+            }
+        // the group's row-major blocks
+        std::vector<uint64_t> boff;
+        std::vector<int32_t> brows, bcols;
+        for (int j = 0; j < grp->n; j++) {
+            const auto &info = grp->infos[j];
+            for (int b = 0; b < info->n; b++) {
+                boff.push_back(grp->offsets[j] + info->block_shifts[b]);
+                brows.push_back((int32_t)info->n_states_bra[b]), bcols.push_back((int32_t)info->n_states_ket[b]);
+            }
+        }
+        b2g_gemm_list gl{(int64_t)ng, ta.data(), tb.data(), m.data(), n.data(), k.data(), lda.data(),
+                         ldb.data(), ldc.data(), ak.data(), bk.data(), al.data(), be.data(),
+                         ga.data(), gb.data(), gc.data()};
+        RecordedPairs rp;
+        rp.tb0.resize(ng), rp.m0.resize(ng), rp.n0.resize(ng), rp.k0.resize(ng), rp.lda0.resize(ng);
+        rp.ldb0.resize(ng), rp.ta1.resize(ng), rp.m1.resize(ng), rp.n1.resize(ng), rp.k1.resize(ng);
+        rp.lda1.resize(ng), rp.ldc1.resize(ng), rp.alpha0.resize(ng), rp.alpha1.resize(ng);
+        rp.a0.resize(ng), rp.b0.resize(ng), rp.a1.resize(ng), rp.c1.resize(ng);
+        b2g_pair_arrays out{rp.tb0.data(), rp.m0.data(), rp.n0.data(), rp.k0.data(), rp.lda0.data(),
+                            rp.ldb0.data(), rp.ta1.data(), rp.m1.data(), rp.n1.data(), rp.k1.data(),
+                            rp.lda1.data(), rp.ldc1.data(), rp.alpha0.data(), rp.alpha1.data(),
+                            rp.a0.data(), rp.b0.data(), rp.a1.data(), rp.c1.data()};
+        int64_t np = 0;
+        int32_t dim = 0;
+        check(b2g_noise_pairs(&gl, nk, nops, nv, (int64_t)boff.size(), boff.data(), brows.data(), bcols.data(),
+                              &out, &np, &dim),
+              "b2g_noise_pairs");
+        for (auto *v : {&rp.tb0, &rp.m0, &rp.n0, &rp.k0, &rp.lda0, &rp.ldb0, &rp.ta1, &rp.m1, &rp.n1, &rp.k1,
+                        &rp.lda1, &rp.ldc1})
+            v->resize((size_t)np);
+        rp.alpha0.resize((size_t)np), rp.alpha1.resize((size_t)np);
+        rp.a0.resize((size_t)np), rp.b0.resize((size_t)np), rp.a1.resize((size_t)np), rp.c1.resize((size_t)np);
+        std::vector<double> blob(nops + (uint64_t)dim * dim, 0.0);
+        for (size_t r = 0; r < reg.size(); r++)
+            std::copy(reg[r].p, reg[r].p + reg[r].n, blob.begin() + roff[r]);
+        for (int32_t d = 0; d < dim; d++)
+            blob[nops + (uint64_t)d * dim + d] = 1.0;
+        b2g_pair_seq ps = rp.seq();
+        b2g_heff *h = nullptr;
+        check(b2g_heff_create(rt->ctx, &ps, blob.data(), blob.size(), 0, nk, nv, &h), "b2g_heff_create");
+        const int rc = b2g_heff_apply_host(h, kb, grp->data, 1.0, B2G_FP64);
+        const std::string err = rc != B2G_OK ? b2g_last_error() : "";
+        b2g_heff_destroy(h);
+        if (rc != B2G_OK)
+            throw std::runtime_error("b2g_heff_apply_host (noise): " + err);
+        rt->n_noise++;
+        rt->h2d_bytes += 8.0 * (double)(blob.size() + nk + nv), rt->d2h_bytes += 8.0 * (double)nv;
+        sq.cumulative_nflop += g1.nflop;
+        g1.clear();
     }
 };
 

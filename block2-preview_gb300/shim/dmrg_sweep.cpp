@@ -58,6 +58,10 @@ struct Opts {
     double tol = 0.0;
     string json, scratch = "";
     double stack_gb = 4.0;  // block2's DataFrame stack (its second frame holds 30 % of it)
+    // noise: "dm" (NoiseTypes::DensityMatrix) or "perturbative" (ReducedPerturbative);
+    // noise_on_device: GPU arms run the perturbative-noise product on the device
+    string noise_type = "dm";
+    int noise_on_device = 1;
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
     // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
     // (-1: of the warm-up)
@@ -157,7 +161,8 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
         if (pb.rt == nullptr)
             pb.rt = make_shared<b2g_block2::Runtime>(0, f);
         pb.rt->form = f;
-        pb.rt->n_heff = pb.rt->n_apply_fp64 = pb.rt->n_apply_reduced = 0;
+        pb.rt->n_heff = pb.rt->n_apply_fp64 = pb.rt->n_apply_reduced = pb.rt->n_noise = 0;
+        pb.rt->noise_on_device = o.noise_on_device != 0;
         pb.rt->t_plan = pb.rt->t_upload = pb.rt->t_davidson = 0;
         b2g_block2::install<S>(pb.mpo, pb.rt);
     }
@@ -186,7 +191,9 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
 #endif
         dmrg = make_shared<DMRG<S, FL, FL>>(me, bdims, sc.noises);
     dmrg->davidson_conv_thrds = sc.dav_thrds;
-    dmrg->noise_type = NoiseTypes::DensityMatrix;
+    if (o.noise_type != "dm" && o.noise_type != "perturbative")
+        throw runtime_error("unknown noise type " + o.noise_type);
+    dmrg->noise_type = o.noise_type == "dm" ? NoiseTypes::DensityMatrix : NoiseTypes::ReducedPerturbative;
     dmrg->iprint = (uint8_t)o.iprint;
     dmrg->sweep_start_site = o.start_site;
     if (o.end_site > 0)
@@ -269,7 +276,8 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
     js << "]";
 #ifndef B2G_REFERENCE_ONLY
     if (gpu)
-        js << ", \"gpu\": {\"heff_plans\": " << pb.rt->n_heff << ", \"apply_fp64\": " << pb.rt->n_apply_fp64
+        js << ", \"gpu\": {\"heff_plans\": " << pb.rt->n_heff << ", \"noise_products\": " << pb.rt->n_noise
+           << ", \"apply_fp64\": " << pb.rt->n_apply_fp64
            << ", \"apply_reduced\": " << pb.rt->n_apply_reduced << ", \"t_translate\": " << pb.rt->t_plan
            << ", \"t_plan_upload\": " << pb.rt->t_upload << ", \"kernel_launches\": " << [&] {
                   uint64_t n1 = 0;
@@ -420,6 +428,8 @@ int main(int argc, char **argv) {
         else if (k == "--M") o.sched.bond_dims = parse_list(v);
         else if (k == "--sweeps") o.sched.nsweeps = atoi(v.c_str());
         else if (k == "--noises") o.sched.noises = parse_list(v);
+        else if (k == "--noise-type") o.noise_type = v;
+        else if (k == "--noise-on-device") o.noise_on_device = atoi(v.c_str());
         else if (k == "--dav") o.sched.dav_thrds = parse_list(v);
         else if (k == "--arms") o.arms = sweep_driver::parse_words(v);
         else if (k == "--warm-M") o.warm.bond_dims = parse_list(v);

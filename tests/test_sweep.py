@@ -163,3 +163,41 @@ def test_gpu_state_averaged_sweep_matches_reference_cpu(tmp_path):
         assert got.shape == ref.shape == (2, 4)
         assert np.abs(got - ref).max() <= tol, (got, ref)
         assert arm["gpu"]["heff_plans"] > 0
+
+
+# Perturbative noise (block2's NoiseTypes::ReducedPerturbative): the GPU arms
+# run EffectiveHamiltonian::perturbative_noise's recorded GEMM list on the
+# device (GpuTensorFunctions::tensor_product_partial_multiply); Hubbard L=8 U=4,
+# M=40, noise 1e-4 for two sweeps, then 1e-5, then none.
+HUB8_PN = dict(ham="hubbard", L=8, U=4.0, t=1.0, sym="su2", M=(40,), sweeps=4, noises=(1e-4, 1e-4, 1e-5, 0.0),
+               dav=(1e-10,), seed=1234, noise_type="perturbative")
+HUB8_E = -4.235806999127  # block2's converged energy of this Hamiltonian at M=40
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="block2 reference build absent")
+def test_reference_perturbative_noise_sweep(tmp_path):
+    r = run_sweep(binary=REF_BIN, arms=("cpu",), threads=_threads(), workdir=str(tmp_path), **HUB8_PN)
+    e = r["arms"][0]["sweep_energies"]
+    assert len(e) == 4 and abs(e[-1] - HUB8_E) < 1e-8
+
+
+@pytest.mark.gpu
+def test_gpu_perturbative_noise_sweep_matches_reference_cpu(tmp_path):
+    if not os.path.exists(SWEEP_BIN):
+        pytest.skip("sweep program not built (no block2 headers)")
+    r = run_sweep(binary=SWEEP_BIN, arms=("cpu", "gpu:fp64", "gpu:tf32x3"), threads=_threads(),
+                  workdir=str(tmp_path), **HUB8_PN)
+    cpu, g64, gtf = r["arms"]
+    floor = HUB8_PN["M"][0] * np.finfo(np.float64).eps
+    noisy = np.array(HUB8_PN["noises"]) > 0
+    dw = np.abs(np.array(cpu["discarded_weights"]))
+    for arm, tol in ((g64, 1e-9), (gtf, 1e-8)):
+        assert arm["gpu"]["noise_products"] > 0 and arm["gpu"]["heff_plans"] > 0, arm["gpu"]
+        de = _spread(arm["sweep_energies"], cpu["sweep_energies"])
+        assert np.all(de <= tol), de
+        # with noise the truncation follows the noise product (1e-3 relative);
+        # the noise-free sweep's weight carries the two Davidson solvers' own
+        # difference (measured 0.7 % of a 6.8e-10 weight, energies within 1e-9)
+        ddw = _spread(arm["discarded_weights"], cpu["discarded_weights"])
+        assert np.all(ddw[noisy] <= 1e-3 * dw[noisy] + floor), ddw
+        assert np.all(ddw[~noisy] <= 2e-2 * dw[~noisy] + floor), ddw
