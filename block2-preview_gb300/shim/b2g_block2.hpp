@@ -13,7 +13,11 @@
 //                          recorded the GEMM pairs (src/core/tensor_functions.hpp:59-62,
 //                          src/dmrg/effective_hamiltonian.hpp:514-532) --
 //                          replays the recorded pairs on the GPU instead of
-//                          BatchGEMMSeq::operator() (src/core/batch_gemm.hpp:1570-1690).
+//                          BatchGEMMSeq::operator() (src/core/batch_gemm.hpp:1570-1690);
+//                          its tensor_product_partial_multiply runs the
+//                          perturbative-noise product (the GEMM list
+//                          EffectiveHamiltonian::perturbative_noise records,
+//                          src/dmrg/effective_hamiltonian.hpp:262-433) on the GPU.
 //   GpuDMRG<S>             a DMRG<S, double, double> whose virtual
 //                          two_dot_eigs_and_perturb (src/dmrg/sweep_algorithm.hpp:1183-1268)
 //                          runs the whole Davidson solve on the device
@@ -55,8 +59,8 @@ struct Runtime {
     double t_davidson = 0;      // wall time inside b2g_davidson (device-resident solves)
     double h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic of the drop-in
     // perturbative noise (EffectiveHamiltonian::perturbative_noise) on the device;
-    // off: block2 replays its recorded GEMM list on the host
-    bool noise_on_device = false;
+    // false: block2 replays its recorded GEMM list on the host
+    bool noise_on_device = true;
     long long n_noise = 0;
     std::atomic<int> noise_depth{0};  // nesting of tensor_product_partial_multiply
     explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
