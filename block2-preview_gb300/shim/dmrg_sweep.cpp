@@ -58,7 +58,8 @@ struct Opts {
     double tol = 0.0;
     string json, scratch = "";
     double stack_gb = 4.0;  // block2's DataFrame stack (its second frame holds 30 % of it)
-    // noise: "dm" (NoiseTypes::DensityMatrix) or "perturbative" (ReducedPerturbative);
+    // noise: "dm" (NoiseTypes::DensityMatrix), "perturbative" (ReducedPerturbative),
+    // "perturbative-full" (Perturbative) or "perturbative-lowmem" (ReducedPerturbativeLowMem);
     // noise_on_device: GPU arms run the perturbative-noise product on the device
     string noise_type = "dm";
     int noise_on_device = 1;
@@ -191,9 +192,16 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
 #endif
         dmrg = make_shared<DMRG<S, FL, FL>>(me, bdims, sc.noises);
     dmrg->davidson_conv_thrds = sc.dav_thrds;
-    if (o.noise_type != "dm" && o.noise_type != "perturbative")
+    if (o.noise_type == "dm")
+        dmrg->noise_type = NoiseTypes::DensityMatrix;
+    else if (o.noise_type == "perturbative")
+        dmrg->noise_type = NoiseTypes::ReducedPerturbative;
+    else if (o.noise_type == "perturbative-full")
+        dmrg->noise_type = NoiseTypes::Perturbative;
+    else if (o.noise_type == "perturbative-lowmem")
+        dmrg->noise_type = NoiseTypes::ReducedPerturbativeLowMem;
+    else
         throw runtime_error("unknown noise type " + o.noise_type);
-    dmrg->noise_type = o.noise_type == "dm" ? NoiseTypes::DensityMatrix : NoiseTypes::ReducedPerturbative;
     dmrg->iprint = (uint8_t)o.iprint;
     dmrg->sweep_start_site = o.start_site;
     if (o.end_site > 0)

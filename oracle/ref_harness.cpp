@@ -46,7 +46,8 @@ struct Opts {
     bool with_data = true;    // false: structure only (no operator blob)
     bool dump_dm = true;      // density-matrix / split data after Davidson
     bool effprob = false;     // also the reference's EffectiveProblem export of the dumped H_eff
-    bool noise = false;       // also the perturbative-noise product of the dumped site's converged ket
+    int noise = 0;            // also the perturbative-noise product of the dumped site's converged ket:
+                              // 1 = NoiseTypes::ReducedPerturbative, else that NoiseTypes value
     // after the run: the reference's 1-/2-PDM of the final MPS, and for each
     // listed FCIDUMP the H_eff at the final MPS's centre with that Hamiltonian
     // (first site of one sweep on a copy of the final MPS: fixed MPS)
@@ -476,7 +477,8 @@ template <typename S> struct Dumper : CallbackKernel {
     }
     // The perturbative-noise product of the converged ket, requested the way
     // DMRG::two_dot_eigs_and_perturb does (src/dmrg/sweep_algorithm.hpp:1257-1260) with
-    // NoiseTypes::ReducedPerturbative.  Written: the recorded GEMMs
+    // NoiseTypes::ReducedPerturbative (or the NoiseTypes value --noise-product
+    // gives, e.g. 4 = Perturbative, 76 = ReducedPerturbativeLowMem).  Written: the recorded GEMMs
     // (c += alpha op(a) op(b); g_akind/g_bkind 0 = ket, 1 = operator blob; g_c an
     // offset into the perturbed group), the operator blob they read, the ket
     // ("psi"), the reference's perturbed-wavefunction group ("sigma") and the
@@ -492,8 +494,11 @@ template <typename S> struct Dumper : CallbackKernel {
         R.ket = h->ket->data, R.nket = h->ket->total_memory;
         R.known = [this](const double *p, size_t ext) { return find_region(p, ext) >= 0; };
         g_noise = &R;
+        const NoiseTypes nt = o.noise == 1 ? NoiseTypes::ReducedPerturbative : (NoiseTypes)o.noise;
+        if (!(nt & NoiseTypes::Perturbative))
+            throw runtime_error("harness: --noise-product needs a perturbative noise type");
         auto pket = h->perturbative_noise(forward, isite, isite + 1, FuseTypes::FuseLR,
-                                          d->me->ket->info, NoiseTypes::ReducedPerturbative);
+                                          d->me->ket->info, nt);
         g_noise = nullptr;
         const double *vbase = pket->data;
         const size_t nsig = pket->total_memory;
@@ -554,7 +559,7 @@ template <typename S> struct Dumper : CallbackKernel {
         }
         Writer w(site_dir() + "/noise");
         w.scalar("n_gemms", (double)ng), w.scalar("n_held", (double)R.held.size());
-        w.scalar("forward", forward), w.scalar("n_vectors", pket->n);
+        w.scalar("forward", forward), w.scalar("n_vectors", pket->n), w.scalar("noise_type", (double)(uint16_t)nt);
         w.scalar("psi_size", (double)R.nket), w.scalar("sigma_size", (double)nsig);
         w.scalar("ops_size", (double)blob);
         w.vec("g_ta", ta, "i4"), w.vec("g_tb", tb, "i4"), w.vec("g_m", m, "i4"), w.vec("g_n", n, "i4");
@@ -655,7 +660,7 @@ template <typename S> struct Dumper : CallbackKernel {
         }
         else if (name == "DMRG::sweep::iter.eff_ham.end") {
             dump_post(d->current_eff_ham);
-            if (o.noise)
+            if (o.noise != 0)
                 dump_noise(d->current_eff_ham);
             want_rotation = true;
             want_blocking = true;
@@ -1206,7 +1211,7 @@ int main(int argc, char **argv) {
         else if (k == "--with-data") o.with_data = atoi(v.c_str()) != 0;
         else if (k == "--pdm") o.pdm = atoi(v.c_str()) != 0;
         else if (k == "--effprob") o.effprob = atoi(v.c_str()) != 0;
-        else if (k == "--noise-product") o.noise = atoi(v.c_str()) != 0;
+        else if (k == "--noise-product") o.noise = atoi(v.c_str());
         else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
         else if (k == "--perturb-threads") o.perturb_threads = atoi(v.c_str());
         else if (k == "--perturb") {

@@ -47,6 +47,8 @@ def test_fixtures_cover_both_directions_and_symmetries():
     assert {m["forward"] for m in metas} == {0, 1}
     assert any(m["n_ket_left"] > 0 for m in metas) and any(m["n_ket_right"] > 0 for m in metas)
     assert any("_sz" in m["name"] for m in metas) and any("_su2" in m["name"] for m in metas)
+    # ReducedPerturbative, Perturbative (one vector per perturbation) and the LowMem variant
+    assert {m["noise_type"] for m in metas} == {12, 4, 76}
 
 
 @pytest.mark.parametrize("name", noise_ids())

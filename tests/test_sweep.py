@@ -174,19 +174,25 @@ HUB8_PN = dict(ham="hubbard", L=8, U=4.0, t=1.0, sym="su2", M=(40,), sweeps=4, n
 HUB8_E = -4.235806999127  # block2's converged energy of this Hamiltonian at M=40
 
 
+NOISE_TYPES = ("perturbative", "perturbative-full", "perturbative-lowmem")
+
+
 @pytest.mark.skipif(not os.path.exists(REF_BIN), reason="block2 reference build absent")
-def test_reference_perturbative_noise_sweep(tmp_path):
-    r = run_sweep(binary=REF_BIN, arms=("cpu",), threads=_threads(), workdir=str(tmp_path), **HUB8_PN)
+@pytest.mark.parametrize("noise_type", NOISE_TYPES)
+def test_reference_perturbative_noise_sweep(tmp_path, noise_type):
+    r = run_sweep(binary=REF_BIN, arms=("cpu",), threads=_threads(), workdir=str(tmp_path),
+                  **dict(HUB8_PN, noise_type=noise_type))
     e = r["arms"][0]["sweep_energies"]
     assert len(e) == 4 and abs(e[-1] - HUB8_E) < 1e-8
 
 
 @pytest.mark.gpu
-def test_gpu_perturbative_noise_sweep_matches_reference_cpu(tmp_path):
+@pytest.mark.parametrize("noise_type", NOISE_TYPES)
+def test_gpu_perturbative_noise_sweep_matches_reference_cpu(tmp_path, noise_type):
     if not os.path.exists(SWEEP_BIN):
         pytest.skip("sweep program not built (no block2 headers)")
     r = run_sweep(binary=SWEEP_BIN, arms=("cpu", "gpu:fp64", "gpu:tf32x3"), threads=_threads(),
-                  workdir=str(tmp_path), **HUB8_PN)
+                  workdir=str(tmp_path), **dict(HUB8_PN, noise_type=noise_type))
     cpu, g64, gtf = r["arms"]
     floor = HUB8_PN["M"][0] * np.finfo(np.float64).eps
     noisy = np.array(HUB8_PN["noises"]) > 0
