@@ -73,7 +73,8 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
     (b2g.problem.load_dump reads it).  stack_gb sizes block2's DataFrame stack
     (4 GB is enough up to M = 1000; n = 32 M = 2000 needs more).  noise_type "dm"
     is block2's NoiseTypes::DensityMatrix, "perturbative" its ReducedPerturbative,
-    "perturbative-full" Perturbative and "perturbative-lowmem" ReducedPerturbativeLowMem
+    "perturbative-full" Perturbative, "perturbative-lowmem" ReducedPerturbativeLowMem and
+    "perturbative-collected" ReducedPerturbativeCollected (pyblock2's driver default)
     (GPU arms run that product on the device unless noise_on_device is false)."""
     if not os.path.exists(binary):
         raise FileNotFoundError(f"{binary} is not built (build() needs block2's headers)")

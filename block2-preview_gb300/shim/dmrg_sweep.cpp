@@ -59,7 +59,8 @@ struct Opts {
     string json, scratch = "";
     double stack_gb = 4.0;  // block2's DataFrame stack (its second frame holds 30 % of it)
     // noise: "dm" (NoiseTypes::DensityMatrix), "perturbative" (ReducedPerturbative),
-    // "perturbative-full" (Perturbative) or "perturbative-lowmem" (ReducedPerturbativeLowMem);
+    // "perturbative-full" (Perturbative), "perturbative-lowmem" (ReducedPerturbativeLowMem) or
+    // "perturbative-collected" (ReducedPerturbativeCollected, pyblock2's driver default);
     // noise_on_device: GPU arms run the perturbative-noise product on the device
     string noise_type = "dm";
     int noise_on_device = 1;
@@ -200,6 +201,8 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
         dmrg->noise_type = NoiseTypes::Perturbative;
     else if (o.noise_type == "perturbative-lowmem")
         dmrg->noise_type = NoiseTypes::ReducedPerturbativeLowMem;
+    else if (o.noise_type == "perturbative-collected")
+        dmrg->noise_type = NoiseTypes::ReducedPerturbativeCollected;
     else
         throw runtime_error("unknown noise type " + o.noise_type);
     dmrg->iprint = (uint8_t)o.iprint;

@@ -174,7 +174,7 @@ HUB8_PN = dict(ham="hubbard", L=8, U=4.0, t=1.0, sym="su2", M=(40,), sweeps=4, n
 HUB8_E = -4.235806999127  # block2's converged energy of this Hamiltonian at M=40
 
 
-NOISE_TYPES = ("perturbative", "perturbative-full", "perturbative-lowmem")
+NOISE_TYPES = ("perturbative", "perturbative-full", "perturbative-lowmem", "perturbative-collected")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_BIN), reason="block2 reference build absent")
