@@ -46,6 +46,19 @@ extern "C" int b2g_noise_pairs(const b2g_gemm_list *g, uint64_t ket_size, uint64
     if (g == nullptr || out == nullptr || n_pairs == nullptr || id_dim == nullptr || g->n_gemms < 0 ||
         n_blocks < 0 || (n_blocks > 0 && (blk_off == nullptr || blk_rows == nullptr || blk_cols == nullptr)))
         return fail(B2G_ERR_ARG, "b2g_noise_pairs: null or negative argument");
+    if (g->n_gemms > 0) {
+        const void *in[] = {g->ta, g->tb, g->m, g->n, g->k, g->lda, g->ldb, g->ldc, g->a_kind, g->b_kind,
+                            g->alpha, g->beta, g->a, g->b, g->c};
+        const void *outp[] = {out->tb0, out->m0, out->n0, out->k0, out->lda0, out->ldb0, out->ta1, out->m1,
+                              out->n1, out->k1, out->lda1, out->ldc1, out->alpha0, out->alpha1, out->a0,
+                              out->b0, out->a1, out->c1};
+        for (const void *x : in)
+            if (x == nullptr)
+                return fail(B2G_ERR_ARG, "b2g_noise_pairs: null GEMM-list array");
+        for (const void *x : outp)
+            if (x == nullptr)
+                return fail(B2G_ERR_ARG, "b2g_noise_pairs: null pair array");
+    }
     for (int64_t b = 0; b < n_blocks; b++) {
         const uint64_t sz = (uint64_t)std::max(blk_rows[b], 0) * (uint64_t)std::max(blk_cols[b], 0);
         if (blk_rows[b] < 0 || blk_cols[b] < 0 || !fits(blk_off[b], sz, group_size) ||

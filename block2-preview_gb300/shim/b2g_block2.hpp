@@ -427,6 +427,10 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
         check(b2g_noise_pairs(&gl, nk, nops, nv, (int64_t)boff.size(), boff.data(), brows.data(), bcols.data(),
                               &out, &np, &dim),
               "b2g_noise_pairs");
+        if (np == 0) {  // nothing to add (e.g. a site without the identity operator on one side)
+            g1.clear();
+            return;
+        }
         for (auto *v : {&rp.tb0, &rp.m0, &rp.n0, &rp.k0, &rp.lda0, &rp.ldb0, &rp.ta1, &rp.m1, &rp.n1, &rp.k1,
                         &rp.lda1, &rp.ldc1})
             v->resize((size_t)np);

@@ -110,6 +110,14 @@ def test_noise_pairs_rejects_bad_lists():
         assert e.value.code in (capi.B2G_ERR_UNSUPPORTED, capi.B2G_ERR_ARG)
 
 
+def test_noise_pairs_of_an_empty_list():
+    """A site whose noise product records nothing (block2 skips a site without
+    the identity operator on one side) gives no pairs."""
+    gl = GemmList({k: [] for k in FIELDS})
+    seq, dim = noise_pairs(gl, 4, 0, 4, [0], [2], [2])
+    assert seq.n == 0 and dim == 0
+
+
 def test_per_row_form_is_transposed_as_a_whole():
     """AdvancedGEMM::multiply's per-row form (src/core/batch_gemm.hpp:584-607):
     c[r, :] (as an m x 1 column, ld 1) += alpha op(A)^T (m x k) * ket[r, :]^T
