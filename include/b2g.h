@@ -25,9 +25,10 @@
  *                        (src/dmrg/effective_hamiltonian.hpp:481-568)
  *   (further entries below: diag, multi-root products and Davidson, density-
  *    matrix truncation, environment blocking, quantum-number bookkeeping and
- *    connection infos, term partition; and, without a reference counterpart,
- *    the adjoint of H_eff*psi, the tile autotuner and the allocation-free
- *    product -- each with the interface it replaces or the reason it exists)
+ *    connection infos, term partition, the perturbative-noise product as
+ *    GEMM pairs; and, without a reference counterpart, the adjoint of
+ *    H_eff*psi, the tile autotuner and the allocation-free product -- each
+ *    with the interface it replaces or the reason it exists)
  *
  * Conventions: row-major matrices (as GMatrix, src/core/matrix.hpp:94-106);
  * offsets and sizes count doubles; every function returns 0 on success and a
@@ -311,7 +312,7 @@ int b2g_heff_set_params(b2g_heff *h, const b2g_pair_seq *seq, const int32_t *par
 
 /* Measured compute ceiling of one arithmetic form on this device (a
  * register-resident FMA/MMA loop, no memory traffic), in TFLOP/s; used as
- * the roofline denominator where no measured peak exists (FP64).
+ * the roofline denominator for forms without a measured copy or GEMM peak (FP64).
  * form = B2G_FP64: FP64 FMA on the CUDA cores (DFMA); B2G_PROBE_FP64_MMA: the
  * FP64 tensor-core instruction (mma.sync m8n8k4 f64, DMMA). */
 #define B2G_PROBE_FP64_MMA 16
