@@ -42,6 +42,9 @@ def test_oracle_replay_matches_reference_blocking(path):
 
 @pytest.fixture(scope="module")
 def ctx():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
     from b2g.heff import Context
     c = Context(0)
     yield c
