@@ -15,6 +15,10 @@
 //     computed by the reference's Tasked replay (batch_gemm.hpp:1613-1689),
 //     diag(H_eff) (effective_hamiltonian.hpp:172-182);
 //   * after Davidson: the converged psi and its energy;
+//   * optionally the perturbative-noise product of that converged psi
+//     (EffectiveHamiltonian::perturbative_noise, --noise-product): the single
+//     GEMMs it records, the operator blob they read and the reference's
+//     perturbed-wavefunction group;
 //   * per sweep: energies, discarded weights, bond dimensions.
 //
 // Output: one directory per dumped site, holding raw little-endian arrays and
