@@ -191,20 +191,22 @@ def test_reference_perturbative_noise_sweep(tmp_path, noise_type):
 def test_gpu_perturbative_noise_sweep_matches_reference_cpu(tmp_path, noise_type):
     if not os.path.exists(SWEEP_BIN):
         pytest.skip("sweep program not built (no block2 headers)")
-    r = run_sweep(binary=SWEEP_BIN, arms=("cpu", "gpu:fp64", "gpu:tf32x3"), threads=_threads(),
+    r = run_sweep(binary=SWEEP_BIN, arms=("cpu", "cpu", "gpu:fp64", "gpu:tf32x3"), threads=_threads(),
                   workdir=str(tmp_path), **dict(HUB8_PN, noise_type=noise_type))
-    cpu, g64, gtf = r["arms"]
+    cpu, cpu2, g64, gtf = r["arms"]
+    spread = _spread(cpu["sweep_energies"], cpu2["sweep_energies"])
+    dw_spread = _spread(cpu["discarded_weights"], cpu2["discarded_weights"])
     floor = HUB8_PN["M"][0] * np.finfo(np.float64).eps
     noisy = np.array(HUB8_PN["noises"]) > 0
     dw = np.abs(np.array(cpu["discarded_weights"]))
     for arm, tol in ((g64, 1e-9), (gtf, 1e-8)):
         assert arm["gpu"]["noise_products"] > 0 and arm["gpu"]["heff_plans"] > 0, arm["gpu"]
         de = _spread(arm["sweep_energies"], cpu["sweep_energies"])
-        assert np.all(de <= tol), de
+        assert np.all(de <= np.maximum(tol, 10 * spread)), (de, spread)
         # discarded weights carry the two Davidson solvers' own difference on top
         # of the noise product (which tests/test_noise.py pins to 1e-12): measured
         # FP64 GPU vs CPU 8e-14, 7e-14, 2e-14 on the noisy sweeps (weights 1.1e-9,
         # 4.7e-10, 3.6e-11) and 0.7 % of the 6.8e-10 weight of the noise-free one
         ddw = _spread(arm["discarded_weights"], cpu["discarded_weights"])
-        assert np.all(ddw <= 2e-2 * dw + floor), ddw
+        assert np.all(ddw <= 10 * dw_spread + 2e-2 * dw + floor), (ddw, dw_spread)
         assert np.any(noisy)
