@@ -60,6 +60,8 @@ struct Opts {
     int perturb_site = -1;    // centre moved here first (-1: n/2 - 1)
     int perturb_threads = 0;  // threads of the perturbed walks (0: --threads); 1 gives every
                               // perturbed H_eff the same GEMM pair order
+    int npdm_call = -1;       // with --pdm: record the C-th fast expectation of the PDM sweep
+    int npdm_order = 1;       // of the 1-PDM (1) or the 2-PDM (2) sweep
 };
 
 static void mkdirs(const string &p) {
@@ -719,6 +721,44 @@ struct BlockRecorder {
 };
 static BlockRecorder *g_blk = nullptr;  // set while a contraction is recorded
 
+// Fast-expectation recorder (TensorFunctions::tensor_product_expectation,
+// src/core/tensor_functions.hpp:1701-1877, the algorithm Expect uses for PDM
+// MPOs).  For every unique left operator a it builds a partial
+// b = <bra| a |ket> (OperatorFunctions::tensor_left_partial_expectation,
+// src/core/operator_functions.hpp:354-410: per connected block,
+// work = op(a) ket, then b += bra^T work or work^T bra, through
+// BatchGEMMSeq::left_partial_rotate, src/core/batch_gemm.hpp:904-922), and
+// each expectation is a sum of factor * dot(partial, right operator).  The
+// block loop is restated here and every block written as a GEMM pair of the
+// H_eff format with the left operator as the pair's left GEMM0 operand
+// ("psi"), ket and bra in the operator blob ("ops") and the partials as the
+// output ("sigma"); a partial whose blocks come out transposed (conj bits
+// differ) is stored block-transposed.
+struct NpdmRecorder {
+    std::mutex mu;
+    int calls = 0, want = -1;
+    bool active = false;
+    string out;
+    const double *ket = nullptr, *bra = nullptr;
+    size_t nket = 0, nbra = 0;
+    map<const double *, size_t> lop_off;  // left operator data -> offset in lops
+    vector<double> lops;
+    struct Part {
+        size_t off;
+        bool trans;
+        vector<int32_t> rows, cols;
+        vector<uint64_t> boff;  // block offsets within the partial
+    };
+    map<tuple<int, uint64_t, uint64_t, const double *>, int> part_key;  // (conj, rdq, opdq, a data)
+    vector<Part> parts;
+    size_t sig = 0;
+    vector<double> ref;  // the reference's partials, in the storage layout
+    vector<int32_t> tb0, m0, n0, k0, lda0, ldb0, ta1, m1, n1, k1, lda1, ldc1;
+    vector<double> al0, al1;
+    vector<uint64_t> a0, b0, a1, c1;
+};
+static NpdmRecorder *g_npdm = nullptr;  // set while a PDM expectation sweep runs
+
 template <typename S> struct RecordingOpf : OperatorFunctions<S, double> {
     typedef OperatorFunctions<S, double> OPF;
     explicit RecordingOpf(const shared_ptr<CG<S>> &cg) : OPF(cg) {}
@@ -838,6 +878,84 @@ template <typename S> struct RecordingOpf : OperatorFunctions<S, double> {
             g_noise->take(*this->seq->batch[1], {{a->data, a->total_memory}, {b->data, b->total_memory},
                                                  {da->data, da->total_memory}, {db->data, db->total_memory}});
     }
+    // one partial of the fast expectation (see NpdmRecorder): the reference
+    // computes it, then its blocks are recorded as GEMM pairs
+    void tensor_left_partial_expectation(uint8_t conj, const shared_ptr<SparseMatrix<S, double>> &a,
+                                         const shared_ptr<SparseMatrix<S, double>> &b,
+                                         const shared_ptr<SparseMatrix<S, double>> &c,
+                                         const shared_ptr<SparseMatrix<S, double>> &v, S opdq,
+                                         double scale = 1.0) const override {
+        OPF::tensor_left_partial_expectation(conj, a, b, c, v, opdq, scale);
+        NpdmRecorder *R = g_npdm;
+        if (R == nullptr || !R->active)
+            return;
+        lock_guard<std::mutex> lk(R->mu);
+        if (c->data != R->ket || v->data != R->bra)
+            throw runtime_error("npdm recorder: partial of another ket or bra");
+        const bool ca = conj & 1, cc = (conj & 2) >> 1;
+        // the partial (sigma role), its blocks and the reference's values
+        const int pid = (int)R->parts.size();
+        NpdmRecorder::Part P;
+        P.off = R->sig, P.trans = ca != cc;
+        for (int ib = 0; ib < b->info->n; ib++) {
+            P.rows.push_back((int32_t)b->info->n_states_bra[ib]);
+            P.cols.push_back((int32_t)b->info->n_states_ket[ib]);
+            P.boff.push_back(b->info->block_shifts[ib]);
+        }
+        R->ref.resize(R->sig + b->total_memory, 0.0);
+        for (int ib = 0; ib < b->info->n; ib++) {
+            const double *src = b->data + P.boff[ib];
+            double *dst = R->ref.data() + P.off + P.boff[ib];
+            const int rr = P.rows[ib], cl = P.cols[ib];
+            for (int i = 0; i < rr; i++)
+                for (int j = 0; j < cl; j++)
+                    (P.trans ? dst[(size_t)j * rr + i] : dst[(size_t)i * cl + j]) = src[(size_t)i * cl + j];
+        }
+        R->sig += b->total_memory;
+        R->parts.push_back(P);
+        R->part_key[make_tuple((int)conj, (uint64_t)b->info->delta_quantum.data, (uint64_t)opdq.data,
+                               (const double *)a->data)] = pid;
+        // restating the block loop (operator_functions.hpp:364-394); FL is real,
+        // so the conjugations there are the identity
+        const double s0 = scale * a->factor * v->factor * c->factor;
+        if (abs(s0) < TINY)
+            return;
+        if (R->lop_off.count(a->data) == 0) {
+            R->lop_off[a->data] = R->lops.size();
+            R->lops.insert(R->lops.end(), a->data, a->data + a->total_memory);
+        }
+        const size_t abase = R->lop_off[a->data];
+        const size_t vbase = R->bra == R->ket ? 0 : R->nket;
+        S adq = a->info->delta_quantum, bdq = b->info->delta_quantum;
+        auto cinfo = c->info->cinfo;
+        S abdq = opdq.combine((conj & 1) ? -adq : adq, (conj & 2) ? bdq : -bdq);
+        const int ik = (int)(lower_bound(cinfo->quanta + cinfo->n[conj], cinfo->quanta + cinfo->n[conj + 1], abdq) -
+                             cinfo->quanta);
+        const int ixa = cinfo->idx[ik], ixb = ik == cinfo->n[4] - 1 ? cinfo->nc : cinfo->idx[ik + 1];
+        for (int il = ixa; il < ixb; il++) {
+            const int ia = cinfo->ia[il], ib = cinfo->ib[il], ic = cinfo->ic[il], iv = (int)cinfo->stride[il];
+            const double sc = s0 * cinfo->factor[il];
+            GMatrix<double> A = (*a)[ia], C = (*b)[ib], V = (*v)[iv], K = (*c)[ic];
+            const uint64_t offA = abase + (uint64_t)(A.data - a->data);
+            const uint64_t offK = (uint64_t)(K.data - R->ket), offV = vbase + (uint64_t)(V.data - R->bra);
+            const uint64_t offC = P.off + (uint64_t)(C.data - b->data);
+            // W = A op2 with op2 = ket (no ca) or bra (ca); out (+)= op1^T W with op1 the other one
+            const GMatrix<double> &X = ca ? V : K, &Y = ca ? K : V;
+            if (A.n != X.m || Y.m != A.m)
+                throw runtime_error("npdm recorder: block shapes do not chain");
+            const bool out_t = ca != cc;  // block written transposed
+            const int orow = out_t ? C.n : C.m, ocol = out_t ? C.m : C.n;
+            if (orow != Y.n || ocol != X.n)
+                throw runtime_error("npdm recorder: partial block shape");
+            R->tb0.push_back(0), R->m0.push_back(A.m), R->k0.push_back(A.n), R->n0.push_back(X.n);
+            R->lda0.push_back(A.n), R->ldb0.push_back(X.n), R->a0.push_back(offA);
+            R->b0.push_back(ca ? offV : offK);
+            R->ta1.push_back(1), R->m1.push_back(Y.n), R->k1.push_back(Y.m), R->n1.push_back(X.n);
+            R->lda1.push_back(Y.n), R->a1.push_back(ca ? offK : offV);
+            R->ldc1.push_back(ocol), R->c1.push_back(offC);
+            R->al0.push_back(1.0), R->al1.push_back(sc);
+        }
+    }
 };
 
 // Operator rotation recorder: TensorFunctions::left_rotate / right_rotate
@@ -926,6 +1044,92 @@ template <typename S> struct RecordingTF : TensorFunctions<S, double> {
         w.vec("env", R.env, "f8"), w.vec("site", R.site, "f8"), w.vec("out", out, "f8");
         w.man.flush();
         blk.reset();
+    }
+    // the fast expectation of one site (see NpdmRecorder): the reference's values,
+    // its partials recorded by RecordingOpf, and the dot terms that combine them
+    vector<pair<shared_ptr<OpExpr<S>>, double>>
+    tensor_product_expectation(const vector<shared_ptr<OpExpr<S>>> &names,
+                               const vector<shared_ptr<OpExpr<S>>> &exprs,
+                               const shared_ptr<OperatorTensor<S, double>> &lopt,
+                               const shared_ptr<OperatorTensor<S, double>> &ropt,
+                               const shared_ptr<SparseMatrix<S, double>> &cmat,
+                               const shared_ptr<SparseMatrix<S, double>> &vmat,
+                               bool all_reduce) const override {
+        NpdmRecorder *R = g_npdm;
+        const bool rec = R != nullptr && R->calls++ == R->want;
+        if (rec) {
+            R->active = true;
+            R->ket = cmat->data, R->nket = cmat->total_memory;
+            R->bra = vmat->data, R->nbra = vmat->total_memory;
+        }
+        auto res = TF::tensor_product_expectation(names, exprs, lopt, ropt, cmat, vmat, all_reduce);
+        if (!rec)
+            return res;
+        R->active = false;
+        // dot terms, restating the last loops of tensor_product_expectation
+        // (tensor_functions.hpp:1809-1872): expectation k = sum over its products
+        // a x b of factor * dot(partial(conj, dq(b), opdq, a), b)
+        vector<int32_t> t_k, t_part;
+        vector<uint64_t> t_roff, t_rsize;
+        vector<double> t_f, rblob, expect(names.size(), 0.0);
+        map<const double *, size_t> roff;
+        S ket_dq = cmat->info->delta_quantum, bra_dq = vmat->info->delta_quantum;
+        for (size_t k = 0; k < exprs.size(); k++) {
+            expect[k] = res[k].second;
+            S opdq = dynamic_pointer_cast<OpElement<S, double>>(names[k])->q_label;
+            if (opdq.combine(bra_dq, ket_dq) == S(S::invalid))
+                continue;
+            vector<shared_ptr<OpProduct<S, double>>> prods;
+            if (exprs[k]->get_type() == OpTypes::Prod)
+                prods.push_back(dynamic_pointer_cast<OpProduct<S, double>>(exprs[k]));
+            else if (exprs[k]->get_type() == OpTypes::Sum)
+                prods = dynamic_pointer_cast<OpSum<S, double>>(exprs[k])->strings;
+            else if (exprs[k]->get_type() != OpTypes::Zero)
+                throw runtime_error("npdm recorder: unexpected expression type");
+            for (auto &op : prods) {
+                auto rmat = ropt->ops.at(op->b);
+                auto lmat = lopt->ops.at(op->a);
+                auto it = R->part_key.find(make_tuple((int)op->conj, (uint64_t)rmat->info->delta_quantum.data,
+                                                      (uint64_t)opdq.data, (const double *)lmat->data));
+                if (it == R->part_key.end())
+                    throw runtime_error("npdm recorder: a term without its partial");
+                if (roff.count(rmat->data) == 0) {
+                    roff[rmat->data] = rblob.size();
+                    rblob.insert(rblob.end(), rmat->data, rmat->data + rmat->total_memory);
+                }
+                t_k.push_back((int32_t)k), t_part.push_back(it->second);
+                t_roff.push_back(roff[rmat->data]), t_rsize.push_back(rmat->total_memory);
+                t_f.push_back(op->factor);
+            }
+        }
+        vector<double> ops(R->ket, R->ket + R->nket);
+        if (R->bra != R->ket)
+            ops.insert(ops.end(), R->bra, R->bra + R->nbra);
+        vector<uint64_t> p_off, b_off;
+        vector<int32_t> p_trans, p_nblk, b_rows, b_cols;
+        for (auto &P : R->parts) {
+            p_off.push_back(P.off), p_trans.push_back(P.trans), p_nblk.push_back((int32_t)P.rows.size());
+            for (size_t q = 0; q < P.rows.size(); q++)
+                b_rows.push_back(P.rows[q]), b_cols.push_back(P.cols[q]), b_off.push_back(P.off + P.boff[q]);
+        }
+        Writer w(R->out);
+        w.scalar("n_pairs", (double)R->tb0.size()), w.scalar("n_partials", (double)R->parts.size());
+        w.scalar("n_expect", (double)names.size()), w.scalar("n_terms", (double)t_k.size());
+        w.scalar("psi_size", (double)R->lops.size()), w.scalar("ops_size", (double)ops.size());
+        w.scalar("sigma_size", (double)R->sig), w.scalar("bra_is_ket", R->bra == R->ket);
+        w.vec("tb0", R->tb0, "i4"), w.vec("m0", R->m0, "i4"), w.vec("n0", R->n0, "i4"), w.vec("k0", R->k0, "i4");
+        w.vec("lda0", R->lda0, "i4"), w.vec("ldb0", R->ldb0, "i4"), w.vec("ta1", R->ta1, "i4");
+        w.vec("m1", R->m1, "i4"), w.vec("n1", R->n1, "i4"), w.vec("k1", R->k1, "i4"), w.vec("lda1", R->lda1, "i4");
+        w.vec("ldc1", R->ldc1, "i4"), w.vec("alpha0", R->al0, "f8"), w.vec("alpha1", R->al1, "f8");
+        w.vec("a0", R->a0, "u8"), w.vec("b0", R->b0, "u8"), w.vec("a1", R->a1, "u8"), w.vec("c1", R->c1, "u8");
+        w.vec("psi", R->lops, "f8"), w.vec("ops", ops, "f8"), w.vec("sigma", R->ref, "f8");
+        w.vec("p_off", p_off, "u8"), w.vec("p_trans", p_trans, "i4"), w.vec("p_nblk", p_nblk, "i4");
+        w.vec("b_off", b_off, "u8"), w.vec("b_rows", b_rows, "i4"), w.vec("b_cols", b_cols, "i4");
+        w.vec("t_k", t_k, "i4"), w.vec("t_part", t_part, "i4"), w.vec("t_roff", t_roff, "u8");
+        w.vec("t_rsize", t_rsize, "u8"), w.vec("t_f", t_f, "f8"), w.vec("rmats", rblob, "f8");
+        w.vec("expect", expect, "f8");
+        w.man.flush();
+        return res;
     }
     void left_rotate(const shared_ptr<OperatorTensor<S, double>> &a,
                      const shared_ptr<SparseMatrix<S, double>> &bra,
@@ -1083,10 +1287,21 @@ void fixed_mps_outputs(const Opts &o, const shared_ptr<HamiltonianQC<S, double>>
                 pmpo = make_shared<PDM2MPOQC<S, FL>>(hamil);
             pmpo = make_shared<SimplifiedMPO<S, FL>>(pmpo, make_shared<RuleQC<S, FL>>(), true, true,
                                                     OpNamesSet({OpNames::R, OpNames::RD}));
+            NpdmRecorder npdm;
+            if (k == o.npdm_order && o.npdm_call >= 0) {
+                // the fast expectations of that PDM sweep go through the recording
+                // tensor functions; the chosen one is written (NpdmRecorder)
+                auto ropf = make_shared<RecordingOpf<S>>(pmpo->tf->opf->cg);
+                ropf->seq = pmpo->tf->opf->seq;
+                pmpo->tf = make_shared<RecordingTF<S>>(ropf, nullptr);
+                npdm.want = o.npdm_call, npdm.out = o.out + "/npdm_product";
+                g_npdm = &npdm;
+            }
             auto pme = make_shared<MovingEnvironment<S, FL, FL>>(pmpo, mps, mps, k == 1 ? "1PDM" : "2PDM");
             pme->init_environments(false);
             auto ex = make_shared<Expect<S, FL, FL>>(pme, (ubond_t)o.M, (ubond_t)o.M);
             ex->solve(true, mps->center == 0);
+            g_npdm = nullptr;
             if (k == 1) {
                 GMatrix<FL> dm = ex->get_1pdm_spatial();
                 vector<double> v(dm.data, dm.data + (size_t)n * n);
@@ -1218,6 +1433,8 @@ int main(int argc, char **argv) {
         else if (k == "--noise-product") o.noise = atoi(v.c_str());
         else if (k == "--perturb-site") o.perturb_site = atoi(v.c_str());
         else if (k == "--perturb-threads") o.perturb_threads = atoi(v.c_str());
+        else if (k == "--npdm-product") o.npdm_call = atoi(v.c_str());
+        else if (k == "--npdm-order") o.npdm_order = atoi(v.c_str());
         else if (k == "--perturb") {
             stringstream ss(v);
             string x;

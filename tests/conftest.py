@@ -50,12 +50,17 @@ def all_ids():
 def fixture_ids():
     """Effective-Hamiltonian problems (H_eff*psi and Davidson)."""
     return [n for n in all_ids() if not n.endswith(("_rot", "_dm", "_blk", "_qn", "_grad", "_fullgrad", "_cinfo",
-                                                     "_effprob", "_noise"))]
+                                                     "_effprob", "_noise", "_npdm"))]
 
 
 def noise_ids():
     """Perturbative-noise products (single-GEMM lists, tests/golden/make_noise_fixtures.py)."""
     return [n for n in all_ids() if n.endswith("_noise")]
+
+
+def npdm_ids():
+    """One site of the reference's PDM expectation sweep (tests/golden/make_npdm_fixtures.py)."""
+    return [n for n in all_ids() if n.endswith("_npdm")]
 
 
 def rotation_ids():
@@ -68,4 +73,4 @@ def problems():
     from b2g.problem import load_problem
     return {os.path.basename(p)[:-4]: load_problem(p) for p in fixture_paths()
             if not p.endswith(("_dm.npz", "_blk.npz", "_qn.npz", "_grad.npz", "_fullgrad.npz", "_cinfo.npz",
-                               "_effprob.npz", "_noise.npz"))}
+                               "_effprob.npz", "_noise.npz", "_npdm.npz"))}
