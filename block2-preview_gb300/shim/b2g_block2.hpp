@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <atomic>
 #include <fstream>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -62,6 +63,7 @@ struct Runtime {
     // false: block2 replays its recorded GEMM list on the host
     bool noise_on_device = true;
     long long n_noise = 0;
+    long long n_expect = 0;  // fast-expectation products (PDM sweeps) run on the device
     std::atomic<int> noise_depth{0};  // nesting of tensor_product_partial_multiply
     explicit Runtime(int device = 0, int form = B2G_FP64) : form(form) {
         check(b2g_context_create(device, &ctx), "b2g_context_create");
@@ -453,6 +455,165 @@ template <typename S> struct GpuTensorFunctions : block2::TensorFunctions<S, dou
         rt->h2d_bytes += 8.0 * (double)(blob.size() + nk + nv), rt->d2h_bytes += 8.0 * (double)nv;
         sq.cumulative_nflop += g1.nflop;
         g1.clear();
+    }
+    // Expect's fast expectation algorithm (TensorFunctions::tensor_product_expectation,
+    // src/core/tensor_functions.hpp:1701-1877, used for the PDM MPOs) with its partials
+    // on the GPU.  Each unique left operator a (per conj, dq of the right operator and
+    // operator quantum) gets a partial <bra| a |ket>; the block loop of
+    // OperatorFunctions::tensor_left_partial_expectation (src/core/operator_functions.hpp:354-410)
+    // is written as H_eff pairs: a on the left of GEMM0 ("psi"), the ket and bra blocks
+    // in the operator blob, the partials as sigma.  With a transposed (which GEMM0's
+    // left operand cannot be) the pair uses bra^T a^T ket = (ket^T a bra)^T and writes
+    // the block transposed; a partial whose conj bits differ is stored block-transposed.
+    // One FP64 product computes every partial; the expectations are then the
+    // reference's sums of factor * dot(partial, right operator) on the host.
+    std::vector<std::pair<std::shared_ptr<block2::OpExpr<S>>, double>>
+    tensor_product_expectation(const std::vector<std::shared_ptr<block2::OpExpr<S>>> &names,
+                               const std::vector<std::shared_ptr<block2::OpExpr<S>>> &exprs,
+                               const std::shared_ptr<block2::OperatorTensor<S, double>> &lopt,
+                               const std::shared_ptr<block2::OperatorTensor<S, double>> &ropt,
+                               const std::shared_ptr<block2::SparseMatrix<S, double>> &cmat,
+                               const std::shared_ptr<block2::SparseMatrix<S, double>> &vmat,
+                               bool all_reduce) const override {
+        typedef block2::OpProduct<S, double> Prod;
+        if (lopt->get_type() == block2::OperatorTensorTypes::Delayed ||
+            ropt->get_type() == block2::OperatorTensorTypes::Delayed)
+            throw std::runtime_error("GpuTensorFunctions: expectation with delayed contraction "
+                                     "(the reference does not support it either)");
+        std::vector<std::pair<std::shared_ptr<block2::OpExpr<S>>, double>> expectations(names.size());
+        const S ket_dq = cmat->info->delta_quantum, bra_dq = vmat->info->delta_quantum;
+        auto products = [&](size_t k) {
+            std::vector<std::shared_ptr<Prod>> ps;
+            if (exprs[k]->get_type() == block2::OpTypes::Prod)
+                ps.push_back(std::dynamic_pointer_cast<Prod>(exprs[k]));
+            else if (exprs[k]->get_type() == block2::OpTypes::Sum)
+                ps = std::dynamic_pointer_cast<block2::OpSum<S, double>>(exprs[k])->strings;
+            else if (exprs[k]->get_type() == block2::OpTypes::SumProd)
+                throw std::runtime_error("GpuTensorFunctions: expectation with delayed contraction");
+            return ps;
+        };
+        auto opdq_of = [&](size_t k) { return std::dynamic_pointer_cast<block2::OpElement<S, double>>(names[k])->q_label; };
+        // the partials, in first-appearance order
+        struct Part {
+            uint8_t conj;
+            S opdq;
+            std::shared_ptr<block2::SparseMatrix<S, double>> lmat;
+            std::shared_ptr<block2::SparseMatrixInfo<S>> info;
+            uint64_t off;
+            bool trans;
+        };
+        std::vector<Part> parts;
+        std::map<std::tuple<int, uint64_t, uint64_t, const double *>, int> pidx;
+        uint64_t nsig = 0;
+        for (size_t k = 0; k < exprs.size(); k++) {
+            const S opdq = opdq_of(k);
+            if (opdq.combine(bra_dq, ket_dq) == S(S::invalid))
+                continue;
+            for (auto &op : products(k)) {
+                auto info = ropt->ops.at(op->b)->info;
+                auto lmat = lopt->ops.at(op->a);
+                const auto key = std::make_tuple((int)op->conj, (uint64_t)info->delta_quantum.data,
+                                                 (uint64_t)opdq.data, (const double *)lmat->data);
+                if (pidx.count(key))
+                    continue;
+                pidx[key] = (int)parts.size();
+                parts.push_back(Part{op->conj, opdq, lmat, info, nsig, (op->conj & 1) != ((op->conj & 2) >> 1)});
+                nsig += info->template get_total_memory<double>();
+            }
+        }
+        // the pairs of every partial block
+        std::vector<double> lblob, oblob(cmat->data, cmat->data + cmat->total_memory);
+        const bool same = vmat->data == cmat->data;
+        if (!same)
+            oblob.insert(oblob.end(), vmat->data, vmat->data + vmat->total_memory);
+        const uint64_t vbase = same ? 0 : cmat->total_memory;
+        std::map<const double *, uint64_t> loff;
+        RecordedPairs rp;
+        auto cinfo = cmat->info->cinfo;
+        if (!parts.empty() && cinfo == nullptr)
+            throw std::runtime_error("GpuTensorFunctions: expectation without the wavefunction connection info");
+        for (auto &P : parts) {
+            const double s0 = P.lmat->factor * vmat->factor * cmat->factor;
+            if (std::abs(s0) < TINY)  // block2's TINY macro (1e-20)
+                continue;
+            if (!loff.count(P.lmat->data)) {
+                loff[P.lmat->data] = lblob.size();
+                lblob.insert(lblob.end(), P.lmat->data, P.lmat->data + P.lmat->total_memory);
+            }
+            const uint64_t abase = loff[P.lmat->data];
+            const bool ca = P.conj & 1, cc = (P.conj & 2) >> 1;
+            const S adq = P.lmat->info->delta_quantum, bdq = P.info->delta_quantum;
+            const S abdq = P.opdq.combine(ca ? -adq : adq, cc ? bdq : -bdq);
+            const int ik = (int)(std::lower_bound(cinfo->quanta + cinfo->n[P.conj], cinfo->quanta + cinfo->n[P.conj + 1],
+                                                  abdq) - cinfo->quanta);
+            if (ik >= cinfo->n[P.conj + 1])
+                throw std::runtime_error("GpuTensorFunctions: no connection for a partial expectation");
+            const int ixa = cinfo->idx[ik], ixb = ik == cinfo->n[4] - 1 ? cinfo->nc : cinfo->idx[ik + 1];
+            for (int il = ixa; il < ixb; il++) {
+                const int ia = cinfo->ia[il], ib = cinfo->ib[il], ic = cinfo->ic[il], iv = (int)cinfo->stride[il];
+                const block2::GMatrix<double> A = (*P.lmat)[ia], V = (*vmat)[iv], K = (*cmat)[ic];
+                const int crow = (int)P.info->n_states_bra[ib], ccol = (int)P.info->n_states_ket[ib];
+                const uint64_t offA = abase + (uint64_t)(A.data - P.lmat->data);
+                const uint64_t offK = (uint64_t)(K.data - cmat->data), offV = vbase + (uint64_t)(V.data - vmat->data);
+                const block2::GMatrix<double> &X = ca ? V : K, &Y = ca ? K : V;
+                const bool out_t = ca != cc;
+                if (A.n != X.m || Y.m != A.m || (out_t ? ccol : crow) != Y.n || (out_t ? crow : ccol) != X.n)
+                    throw std::runtime_error("GpuTensorFunctions: partial expectation block shapes");
+                rp.tb0.push_back(0), rp.m0.push_back(A.m), rp.k0.push_back(A.n), rp.n0.push_back(X.n);
+                rp.lda0.push_back(A.n), rp.ldb0.push_back(X.n), rp.a0.push_back(offA);
+                rp.b0.push_back(ca ? offV : offK);
+                rp.ta1.push_back(1), rp.m1.push_back(Y.n), rp.k1.push_back(Y.m), rp.n1.push_back(X.n);
+                rp.lda1.push_back(Y.n), rp.a1.push_back(ca ? offK : offV);
+                rp.ldc1.push_back(out_t ? crow : ccol), rp.c1.push_back(P.off + P.info->block_shifts[ib]);
+                rp.alpha0.push_back(1.0), rp.alpha1.push_back(s0 * cinfo->factor[il]);
+            }
+        }
+        std::vector<double> part(nsig, 0.0);
+        if (!rp.tb0.empty()) {
+            b2g_pair_seq ps = rp.seq();
+            b2g_heff *h = nullptr;
+            check(b2g_heff_create(rt->ctx, &ps, oblob.data(), oblob.size(), 0, lblob.size(), nsig, &h),
+                  "b2g_heff_create (expectation)");
+            const int rc = b2g_heff_apply_host(h, lblob.data(), part.data(), 1.0, B2G_FP64);
+            const std::string err = rc != B2G_OK ? b2g_last_error() : "";
+            b2g_heff_destroy(h);
+            if (rc != B2G_OK)
+                throw std::runtime_error("b2g_heff_apply_host (expectation): " + err);
+            rt->n_expect++;
+            rt->h2d_bytes += 8.0 * (double)(oblob.size() + lblob.size() + nsig), rt->d2h_bytes += 8.0 * (double)nsig;
+        }
+        // transposed partials back to row-major blocks
+        for (auto &P : parts)
+            if (P.trans)
+                for (int ib = 0; ib < P.info->n; ib++) {
+                    const int r = (int)P.info->n_states_bra[ib], c = (int)P.info->n_states_ket[ib];
+                    double *x = part.data() + P.off + P.info->block_shifts[ib];
+                    std::vector<double> t(x, x + (size_t)r * c);
+                    for (int i = 0; i < r; i++)
+                        for (int j = 0; j < c; j++)
+                            x[(size_t)i * c + j] = t[(size_t)j * r + i];
+                }
+        // expectation k = sum of factor * dot(partial, right operator) over its products
+        for (size_t k = 0; k < exprs.size(); k++) {
+            expectations[k] = std::make_pair(names[k], 0.0);
+            const S opdq = opdq_of(k);
+            if (opdq.combine(bra_dq, ket_dq) == S(S::invalid))
+                continue;
+            double r = 0.0;
+            for (auto &op : products(k)) {
+                auto rmat = ropt->ops.at(op->b);
+                auto lmat = lopt->ops.at(op->a);
+                const int p = pidx.at(std::make_tuple((int)op->conj, (uint64_t)rmat->info->delta_quantum.data,
+                                                      (uint64_t)opdq.data, (const double *)lmat->data));
+                const double *x = part.data() + parts[p].off;
+                double d = 0.0;
+                for (uint64_t q = 0; q < rmat->total_memory; q++)
+                    d += x[q] * rmat->data[q];
+                r += op->factor * d;
+            }
+            expectations[k].second = r;
+        }
+        return expectations;
     }
 };
 

@@ -64,6 +64,10 @@ struct Opts {
     // noise_on_device: GPU arms run the perturbative-noise product on the device
     string noise_type = "dm";
     int noise_on_device = 1;
+    // after each arm: block2's 1-PDM (Expect with PDM1MPOQC) of the arm's final MPS,
+    // on the arm's device (GPU arms: the fast expectation's partials on the GPU);
+    // 2: GPU arms also compute it with block2's own tensor functions
+    int pdm = 0;
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
     // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
     // (-1: of the warm-up)
@@ -296,6 +300,55 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
                   return n1 - launches0;
               }() << "}";
 #endif
+    if (o.pdm) {
+        // the 1-PDM of this arm's final MPS (as block2's Expect computes it), on the
+        // arm's device; --pdm 2 on a GPU arm also computes it with block2's own
+        // tensor functions on the same MPS ("pdm1_host")
+        mps->save_data();
+        auto one_pdm = [&](bool on_gpu, const string &label, double &secs) {
+            shared_ptr<MPO<S, FL>> pmpo = make_shared<PDM1MPOQC<S, FL>>(pb.hamil);
+            pmpo = make_shared<SimplifiedMPO<S, FL>>(pmpo, make_shared<RuleQC<S, FL>>(), true, true,
+                                                    OpNamesSet({OpNames::R, OpNames::RD}));
+#ifndef B2G_REFERENCE_ONLY
+            if (on_gpu)
+                b2g_block2::install<S>(pmpo, pb.rt);
+#else
+            (void)on_gpu;
+#endif
+            auto pme = make_shared<MovingEnvironment<S, FL, FL>>(pmpo, mps, mps, tag + label);
+            pme->init_environments(false);
+            const ubond_t bd = (ubond_t)sc.bond_dims.back();
+            auto ex = make_shared<Expect<S, FL, FL>>(pme, bd, bd);
+            ex->iprint = 0;
+            Timer tp;
+            tp.get_time();
+            ex->solve(true, mps->center == 0);
+            secs = tp.get_time();
+            GMatrix<FL> dm = ex->get_1pdm_spatial();
+            vector<double> v(dm.data, dm.data + (size_t)dm.m * dm.n);
+            dm.deallocate();
+            pme->remove_partition_files();
+            pmpo->deallocate();
+            return v;
+        };
+#ifndef B2G_REFERENCE_ONLY
+        const long long nexp0 = gpu ? pb.rt->n_expect : 0;
+#endif
+        double tpdm = 0;
+        js << ", \"pdm1\": ";
+        json_list(js, one_pdm(gpu, "PDM", tpdm));
+        js << ", \"pdm1_time\": " << tpdm;
+#ifndef B2G_REFERENCE_ONLY
+        if (gpu) {
+            js << ", \"pdm1_device_products\": " << pb.rt->n_expect - nexp0;
+            if (o.pdm == 2) {
+                js << ", \"pdm1_host\": ";
+                json_list(js, one_pdm(false, "PDMH", tpdm));
+                js << ", \"pdm1_host_time\": " << tpdm;
+            }
+        }
+#endif
+    }
     js << "}";
     pb.mpo->tf = pb.cpu_tf;
     me->remove_partition_files();
@@ -441,6 +494,7 @@ int main(int argc, char **argv) {
         else if (k == "--noises") o.sched.noises = parse_list(v);
         else if (k == "--noise-type") o.noise_type = v;
         else if (k == "--noise-on-device") o.noise_on_device = atoi(v.c_str());
+        else if (k == "--pdm") o.pdm = atoi(v.c_str());
         else if (k == "--dav") o.sched.dav_thrds = parse_list(v);
         else if (k == "--arms") o.arms = sweep_driver::parse_words(v);
         else if (k == "--warm-M") o.warm.bond_dims = parse_list(v);

@@ -8,10 +8,12 @@ of every unique left operator recorded as pairs, the reference's partials,
 the dot terms and the reference's expectation values.  Here the oracle (the
 reference's Tasked pair replay restated) runs the pairs; the partials and the
 expectation values built from them must equal the reference's."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import npdm_ids
+from conftest import ROOT, npdm_ids
 import b2g
 from b2g.npdm import expectations, normal_layout
 from npdm_fixture import load
@@ -50,3 +52,17 @@ def test_partial_blocks_tile_the_partials():
         np.testing.assert_array_equal(L["b_off"], np.concatenate([[0], np.cumsum(size)[:-1]]))
         assert int(size.sum()) == d["sigma"].size
         assert int(L["p_nblk"].sum()) == L["b_off"].size
+
+
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dmrg_sweep_ref")
+# Hubbard L=8 U=4 at half filling, M=40: the 1-PDM after the sweeps (block2's Expect)
+HUB8_PDM = dict(ham="hubbard", L=8, U=4.0, t=1.0, sym="su2", M=(40,), sweeps=4, noises=(1e-4, 1e-5, 0.0, 0.0),
+                dav=(1e-10,), seed=1234, pdm=1)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="block2 reference build absent")
+def test_reference_sweep_reports_the_1pdm(tmp_path):
+    from b2g.sweep import run_sweep
+    r = run_sweep(binary=REF_BIN, arms=("cpu",), threads=2, workdir=str(tmp_path), **HUB8_PDM)
+    p = np.array(r["arms"][0]["pdm1"]).reshape(8, 8)
+    assert abs(np.trace(p) - 8.0) < 1e-10 and np.abs(p - p.T).max() < 1e-12

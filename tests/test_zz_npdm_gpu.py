@@ -2,6 +2,11 @@
 run by the H_eff engine must give the reference's partials and expectation
 values (FP64 to 1e-12, TF32x3 to 2e-5 relative on the partials).
 
+Through block2's own Expect sweep (the sweep program's --pdm 2): the GPU arm's
+1-PDM, whose fast-expectation partials run on the device
+(GpuTensorFunctions::tensor_product_expectation), equals block2's 1-PDM of the
+same MPS to 1e-12.
+
 This file is collected after the other GPU tests."""
 import numpy as np
 import pytest
@@ -31,3 +36,19 @@ def test_gpu_pdm_site_matches_reference(name):
         assert np.abs(site.values(form) - d["expect"]).max() <= tol * emax, form
     site.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_pdm_in_block2_expect_sweep(tmp_path):
+    import os
+    from b2g.sweep import SWEEP_BIN, run_sweep
+    from test_npdm import HUB8_PDM
+    if not os.path.exists(SWEEP_BIN):
+        pytest.skip("sweep program not built (no block2 headers)")
+    r = run_sweep(binary=SWEEP_BIN, arms=("gpu:fp64",), threads=4, workdir=str(tmp_path),
+                  **dict(HUB8_PDM, pdm=2))
+    arm = r["arms"][0]
+    assert arm["pdm1_device_products"] > 0
+    dev, host = np.array(arm["pdm1"]), np.array(arm["pdm1_host"])
+    assert np.abs(dev - host).max() <= 1e-12, np.abs(dev - host).max()
+    assert abs(np.trace(dev.reshape(8, 8)) - 8.0) < 1e-10
