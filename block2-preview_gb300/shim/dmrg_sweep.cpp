@@ -68,6 +68,7 @@ struct Opts {
     // on the arm's device (GPU arms: the fast expectation's partials on the GPU);
     // 2: GPU arms also compute it with block2's own tensor functions
     int pdm = 0;
+    int pdm_on_gpu = 0;  // 1: the PDM goes through the drop-in after CPU arms too
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
     // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
     // (-1: of the warm-up)
@@ -331,15 +332,22 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
             pmpo->deallocate();
             return v;
         };
+        bool pdm_gpu = gpu;
 #ifndef B2G_REFERENCE_ONLY
-        const long long nexp0 = gpu ? pb.rt->n_expect : 0;
+        if (o.pdm_on_gpu && !pb.rt)
+            pb.rt = make_shared<b2g_block2::Runtime>(0, B2G_FP64);
+        pdm_gpu = gpu || o.pdm_on_gpu;
+        const long long nexp0 = pdm_gpu ? pb.rt->n_expect : 0;
+#else
+        if (o.pdm_on_gpu)
+            throw runtime_error("this build is block2's CPU path only (B2G_REFERENCE_ONLY)");
 #endif
         double tpdm = 0;
         js << ", \"pdm1\": ";
-        json_list(js, one_pdm(gpu, "PDM", tpdm));
+        json_list(js, one_pdm(pdm_gpu, "PDM", tpdm));
         js << ", \"pdm1_time\": " << tpdm;
 #ifndef B2G_REFERENCE_ONLY
-        if (gpu) {
+        if (pdm_gpu) {
             js << ", \"pdm1_device_products\": " << pb.rt->n_expect - nexp0;
             if (o.pdm == 2) {
                 js << ", \"pdm1_host\": ";
@@ -495,6 +503,7 @@ int main(int argc, char **argv) {
         else if (k == "--noise-type") o.noise_type = v;
         else if (k == "--noise-on-device") o.noise_on_device = atoi(v.c_str());
         else if (k == "--pdm") o.pdm = atoi(v.c_str());
+        else if (k == "--pdm-on-gpu") o.pdm_on_gpu = atoi(v.c_str());
         else if (k == "--dav") o.sched.dav_thrds = parse_list(v);
         else if (k == "--arms") o.arms = sweep_driver::parse_words(v);
         else if (k == "--warm-M") o.warm.bond_dims = parse_list(v);
