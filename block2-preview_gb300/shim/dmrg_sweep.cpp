@@ -156,7 +156,9 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
     string dev = device, form = "fp64";
     if (dev.find(':') != string::npos)
         form = dev.substr(dev.find(':') + 1), dev = dev.substr(0, dev.find(':'));
-    const bool gpu = dev == "gpu";
+    // gpu: GpuDMRG (device Davidson); gpuop: the drop-in's tensor functions under
+    // block2's own DMRG and host Davidson (every product through the C ABI)
+    const bool gpu = dev == "gpu" || dev == "gpuop", host_davidson = dev == "gpuop";
     if (!gpu && dev != "cpu")
         throw runtime_error("unknown device " + device);
     pb.mpo->tf = pb.cpu_tf;
@@ -186,7 +188,7 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
     me->cached_contraction = true;
     shared_ptr<DMRG<S, FL, FL>> dmrg;
 #ifndef B2G_REFERENCE_ONLY
-    if (gpu) {
+    if (gpu && !host_davidson) {
         auto gd = make_shared<b2g_block2::GpuDMRG<S>>(me, bdims, sc.noises, pb.rt);
         if (!o.dump_dir.empty() && tag == (o.dump_arm < 0 ? string("WARM") : "ARM" + to_string(o.dump_arm))) {
             mkdirs(o.dump_dir);

@@ -1,5 +1,6 @@
-// CPU stand-in for the C-ABI calls the shim makes on its expectation path:
-// contexts are empty objects and b2g_heff_apply_host replays the recorded pairs with
+// CPU stand-in for the C-ABI calls the shim makes when block2's own Davidson drives
+// GpuTensorFunctions (operator(), the perturbative-noise product, the PDM expectation):
+// contexts hold a host staging buffer and b2g_heff_apply_host replays the recorded pairs with
 // the oracle (oracle/b2g_oracle.c), so the shim's host-side translation of block2's
 // products into pairs runs, and is checked, without a GPU.  Test infrastructure only.
 #include <cstring>
@@ -8,14 +9,48 @@
 #include "b2g.h"
 extern "C" int b2g_oracle_replay(const b2g_pair_seq *s, const double *ops, const double *psi, double *sigma,
                                  uint64_t sigma_size, double scale, int nthreads);
-struct b2g_context { int dev; };
+struct b2g_context {
+    int dev;
+    std::vector<double> stage;  // b2g_host_buffer
+};
 struct b2g_heff {
     std::vector<int32_t> i[12]; std::vector<double> f[2]; std::vector<uint64_t> u[4];
     b2g_pair_seq s; std::vector<double> ops; uint64_t np, ns;
 };
 static std::string err;
+// the library's error channel, used by the host-only translator linked in
+// (b2g_noise_pairs, block2-preview_gb300/csrc/b2g_noise.cu)
+namespace b2g {
+int fail(int code, const std::string &msg) {
+    err = msg;
+    return code;
+}
+} // namespace b2g
 extern "C" {
-int b2g_context_create(int device, b2g_context **out) { *out = new b2g_context{device}; return 0; }
+// device-only entries of GpuDMRG: not on the paths this stand-in serves
+int b2g_heff_diag_host(b2g_heff *, double *) { return b2g::fail(B2G_ERR_UNSUPPORTED, "stand-in"); }
+int b2g_davidson(b2g_heff *, const double *, double *, double, int, int, int, int, b2g_davidson_result *) {
+    return b2g::fail(B2G_ERR_UNSUPPORTED, "stand-in");
+}
+int b2g_davidson_multi(b2g_heff *, const double *, double *, int, double, int, int, int, int, double *,
+                       b2g_davidson_result *) {
+    return b2g::fail(B2G_ERR_UNSUPPORTED, "stand-in");
+}
+int b2g_context_create(int device, b2g_context **out) {
+    *out = new b2g_context();
+    (*out)->dev = device;
+    return 0;
+}
+int b2g_host_buffer(b2g_context *c, uint64_t bytes, void **out) {
+    if (c->stage.size() * 8 < bytes)
+        c->stage.assign((bytes + 7) / 8, 0.0);
+    *out = c->stage.data();
+    return 0;
+}
+int b2g_heff_set_ops(b2g_heff *h, const double *ops, int) {
+    std::memcpy(h->ops.data(), ops, sizeof(double) * h->ops.size());
+    return 0;
+}
 int b2g_context_destroy(b2g_context *c) { delete c; return 0; }
 const char *b2g_last_error(void) { return err.c_str(); }
 int b2g_launch_count(uint64_t *o) { *o = 0; return 0; }
@@ -33,7 +68,11 @@ int b2g_heff_create(b2g_context *, const b2g_pair_seq *s, const double *ops, uin
     h->s.n1 = h->i[8].data(), h->s.k1 = h->i[9].data(), h->s.lda1 = h->i[10].data(), h->s.ldc1 = h->i[11].data();
     h->s.alpha0 = h->f[0].data(), h->s.alpha1 = h->f[1].data();
     h->s.a0 = h->u[0].data(), h->s.b0 = h->u[1].data(), h->s.a1 = h->u[2].data(), h->s.c1 = h->u[3].data();
-    h->ops.assign(ops, ops + ops_size); h->np = np; h->ns = ns;
+    if (ops != nullptr)
+        h->ops.assign(ops, ops + ops_size);
+    else
+        h->ops.assign(ops_size, 0.0);  // B2G_OPS_DEFERRED: filled by b2g_heff_set_ops
+    h->np = np, h->ns = ns;
     *out = h; return 0;
 }
 int b2g_heff_destroy(b2g_heff *h) { delete h; return 0; }
