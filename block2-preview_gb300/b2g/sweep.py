@@ -66,7 +66,7 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
               timeout: float | None = None, env: dict | None = None, dump_heff: str | None = None,
               dump_arm: int = 0, dump_sweep: int = -1, dump_site: int = -1, nroots: int = 1,
               stack_gb: float = 4.0, noise_type: str = "dm", noise_on_device: bool = True,
-              pdm: int = 0) -> dict:
+              pdm: int = 0, pdm_order: int = 1) -> dict:
     """Runs one dmrg_sweep invocation and returns its JSON report with
     ``sites`` (parse_sites of its output), ``stdout`` and ``cmd``.  With
     dump_heff, GPU arm ``dump_arm`` writes the H_eff of ``dump_site`` (default:
@@ -78,7 +78,8 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
     "perturbative-collected" ReducedPerturbativeCollected (pyblock2's driver default)
     (GPU arms run that product on the device unless noise_on_device is false).  pdm=1
     adds each arm's 1-PDM (block2's Expect on the arm's final MPS, on the arm's device:
-    "pdm1"); pdm=2 also gives GPU arms block2's own 1-PDM of the same MPS ("pdm1_host")."""
+    "pdm1"); pdm=2 also gives GPU arms block2's own 1-PDM of the same MPS ("pdm1_host").
+    pdm_order=2 computes the 2-PDM instead (keys "pdm2", "pdm2_host", ...)."""
     if not os.path.exists(binary):
         raise FileNotFoundError(f"{binary} is not built (build() needs block2's headers)")
     lst = lambda v: ",".join(str(x) for x in v)  # noqa: E731
@@ -93,7 +94,8 @@ def run_sweep(*, binary: str = SWEEP_BIN, ham: str = "hubbard", L: int = 16, U: 
            "--iprint", "2", "--json", js, "--scratch", os.path.join(wd, "scratch"),
            "--start-site", str(start_site), "--end-site", str(end_site), "--nroots", str(nroots),
            "--stack-gb", str(stack_gb), "--noise-type", noise_type,
-           "--noise-on-device", "1" if noise_on_device else "0", "--pdm", str(int(pdm))]
+           "--noise-on-device", "1" if noise_on_device else "0", "--pdm", str(int(pdm)),
+           "--pdm-order", str(int(pdm_order))]
     if dump_heff:
         cmd += ["--dump-heff", os.path.abspath(dump_heff), "--dump-arm", str(dump_arm),
                 "--dump-sweep", str(dump_sweep), "--dump-site", str(dump_site)]

@@ -69,6 +69,7 @@ struct Opts {
     // 2: GPU arms also compute it with block2's own tensor functions
     int pdm = 0;
     int pdm_on_gpu = 0;  // 1: the PDM goes through the drop-in after CPU arms too
+    int pdm_order = 1;   // 1: the 1-PDM (PDM1MPOQC); 2: the 2-PDM (PDM2MPOQC)
     int start_site = 0, end_site = -1;  // restricts every arm's sweeps (timing samples)
     // GPU stages: dump the H_eff of one site of one sweep of arm dump_arm
     // (-1: of the warm-up)
@@ -309,7 +310,11 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
         // tensor functions on the same MPS ("pdm1_host")
         mps->save_data();
         auto one_pdm = [&](bool on_gpu, const string &label, double &secs) {
-            shared_ptr<MPO<S, FL>> pmpo = make_shared<PDM1MPOQC<S, FL>>(pb.hamil);
+            shared_ptr<MPO<S, FL>> pmpo;
+            if (o.pdm_order == 2)
+                pmpo = make_shared<PDM2MPOQC<S, FL>>(pb.hamil);
+            else
+                pmpo = make_shared<PDM1MPOQC<S, FL>>(pb.hamil);
             pmpo = make_shared<SimplifiedMPO<S, FL>>(pmpo, make_shared<RuleQC<S, FL>>(), true, true,
                                                     OpNamesSet({OpNames::R, OpNames::RD}));
 #ifndef B2G_REFERENCE_ONLY
@@ -327,9 +332,15 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
             tp.get_time();
             ex->solve(true, mps->center == 0);
             secs = tp.get_time();
-            GMatrix<FL> dm = ex->get_1pdm_spatial();
-            vector<double> v(dm.data, dm.data + (size_t)dm.m * dm.n);
-            dm.deallocate();
+            vector<double> v;
+            if (o.pdm_order == 2) {
+                shared_ptr<GTensor<FL>> dm2 = ex->get_2pdm_spatial();
+                v.assign(dm2->data->begin(), dm2->data->end());
+            } else {
+                GMatrix<FL> dm = ex->get_1pdm_spatial();
+                v.assign(dm.data, dm.data + (size_t)dm.m * dm.n);
+                dm.deallocate();
+            }
             pme->remove_partition_files();
             pmpo->deallocate();
             return v;
@@ -345,16 +356,17 @@ void solve_stage(Problem<S> &pb, const shared_ptr<MPS<S, double>> &mps, const st
             throw runtime_error("this build is block2's CPU path only (B2G_REFERENCE_ONLY)");
 #endif
         double tpdm = 0;
-        js << ", \"pdm1\": ";
+        const string key = o.pdm_order == 2 ? "pdm2" : "pdm1";  // JSON keys: pdm1* or pdm2*
+        js << ", \"" << key << "\": ";
         json_list(js, one_pdm(pdm_gpu, "PDM", tpdm));
-        js << ", \"pdm1_time\": " << tpdm;
+        js << ", \"" << key << "_time\": " << tpdm;
 #ifndef B2G_REFERENCE_ONLY
         if (pdm_gpu) {
-            js << ", \"pdm1_device_products\": " << pb.rt->n_expect - nexp0;
+            js << ", \"" << key << "_device_products\": " << pb.rt->n_expect - nexp0;
             if (o.pdm == 2) {
-                js << ", \"pdm1_host\": ";
+                js << ", \"" << key << "_host\": ";
                 json_list(js, one_pdm(false, "PDMH", tpdm));
-                js << ", \"pdm1_host_time\": " << tpdm;
+                js << ", \"" << key << "_host_time\": " << tpdm;
             }
         }
 #endif
@@ -506,6 +518,7 @@ int main(int argc, char **argv) {
         else if (k == "--noise-on-device") o.noise_on_device = atoi(v.c_str());
         else if (k == "--pdm") o.pdm = atoi(v.c_str());
         else if (k == "--pdm-on-gpu") o.pdm_on_gpu = atoi(v.c_str());
+        else if (k == "--pdm-order") o.pdm_order = atoi(v.c_str());
         else if (k == "--dav") o.sched.dav_thrds = parse_list(v);
         else if (k == "--arms") o.arms = sweep_driver::parse_words(v);
         else if (k == "--warm-M") o.warm.bond_dims = parse_list(v);

@@ -81,3 +81,20 @@ def test_shim_operator_and_noise_paths_under_block2_davidson(standin_sweep, tmp_
     de = np.abs(np.array(op["sweep_energies"]) - np.array(cpu["sweep_energies"]))
     assert np.all(de <= np.maximum(1e-9, 10 * spread)), (de, spread)
     assert op["gpu"]["heff_plans"] > 0 and op["gpu"]["noise_products"] > 0, op["gpu"]
+
+
+def test_shim_expectation_path_2pdm(standin_sweep, tmp_path):
+    """The 2-PDM (PDM2MPOQC: sums of products, many more partials) through the
+    drop-in's expectation path equals block2's own 2-PDM of the same MPS."""
+    js = str(tmp_path / "r.json")
+    cmd = [standin_sweep, "--L", "6", "--M", "30", "--sweeps", "4", "--noises", "1e-4,1e-5,0,0", "--dav", "1e-10",
+           "--arms", "cpu", "--threads", "2", "--seed", "1234", "--pdm", "2", "--pdm-on-gpu", "1",
+           "--pdm-order", "2", "--json", js, "--scratch", str(tmp_path / "scr")]
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=str(tmp_path),
+                       env=dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="2"))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    arm = json.load(open(js))["arms"][0]
+    assert arm["pdm2_device_products"] > 0
+    dev, host = np.array(arm["pdm2"]), np.array(arm["pdm2_host"])
+    assert dev.size == 6 ** 4 and np.abs(host).max() > 0.1
+    assert np.abs(dev - host).max() <= 1e-12, np.abs(dev - host).max()
